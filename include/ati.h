@@ -1,0 +1,188 @@
+/*
+ * ati.h — C ABI of the GB300 per-Runge–Kutta-stage hot path of the ATI3D
+ * compressible Navier–Stokes solver (rpt1g12/tandemProject).
+ *
+ * The reference exposes this path as Fortran module procedures that take only
+ * small integer selectors and work on module-global arrays:
+ *   mpigo(nt,nrt,n45,itag)   src/Subroutines3D.f90:16-80
+ *   deriv(nn,nz,m)           src/Subroutines3D.f90:84-141
+ *   filte(nn,nz)             src/Subroutines3D.f90:145-206
+ * and as inline code in the time loop of program main3d
+ *   per-step filter          src/Main3D.f90:555-561
+ *   one RK stage             src/Main3D.f90:567-958
+ *   one time step            src/Main3D.f90:552-965
+ * Here the globals become a handle that owns every device array of one case
+ * (all blocks of the multi-block grid live on one GPU), and each entry point
+ * keeps the reference's selector arguments and meaning.
+ *
+ * Conventions
+ *  - Every call returns an int status (ATI_OK == 0); ati_last_error() gives text.
+ *  - Host pointers are borrowed for the duration of the call only.
+ *  - Arrays cross the boundary in the reference's Fortran layout: a block field
+ *    f(0:lmx,ncomp) is ncomp contiguous planes of (lxi+1)(let+1)(lze+1)
+ *    doubles, point index l = i + (lxi+1)*(j + (let+1)*k), i = xi fastest
+ *    (src/Subroutineso.f90:364-375 indx3, nn=1).
+ *  - One CUDA stream per handle; calls on one handle must not run
+ *    concurrently; different handles are independent.  Calls are asynchronous
+ *    on that stream except the ati_get_* copies, which synchronise.
+ *  - No CPU fallback: a handle cannot be created without a CUDA device.
+ */
+#ifndef ATI_H
+#define ATI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ATI_ABI_VERSION 1
+#define ATI_MAX_BK 8 /* max blocks per grid direction */
+
+/* ---- status codes ------------------------------------------------------ */
+#define ATI_OK 0
+#define ATI_EINVAL 1      /* bad argument or configuration                   */
+#define ATI_ENOMEM 2      /* device or host allocation failed                */
+#define ATI_ECUDA 3       /* CUDA runtime error                              */
+#define ATI_ENONFINITE 4  /* NaN/Inf or non-positive rho/p seen on device    */
+#define ATI_ETIMEDOUT 5   /* a bounded device or host wait gave up           */
+#define ATI_ESTATE 6      /* call out of order (e.g. step before init)       */
+
+/* ---- precision of the fused stage (ati_config_t.precision) -------------- */
+#define ATI_FP64 0  /* every array and operation in FP64 (the reference's nr=ieee64) */
+#define ATI_MIXED 1 /* line solves, filters, fluxes in FP32; metrics, Jacobian and
+                       RK state (qa, qo) in FP64 */
+
+/* ---- field identifiers (the reference's module arrays) ------------------
+ * src/MainVar3D.f90:78-85.  ncomp in brackets. */
+#define ATI_F_QA 0    /* qa   [5] conservative state (rho, rho u, rho v, rho w, rho E) */
+#define ATI_F_QO 1    /* qo   [5] state at the start of the time step          */
+#define ATI_F_DE 2    /* de   [5] primitives / right-hand side                  */
+#define ATI_F_RR 3    /* rr   [3] line-sweep work field                          */
+#define ATI_F_SS 4    /* ss   [3] work field (grid coordinates at set-up)        */
+#define ATI_F_XIM 5   /* xim  [3] d(xi)/dx etc. times J^-1 (non-conservative)    */
+#define ATI_F_ETM 6   /* etm  [3]                                                */
+#define ATI_F_ZEM 7   /* zem  [3]                                                */
+#define ATI_F_P 8     /* p    [1] pressure                                       */
+#define ATI_F_YACO 9  /* yaco [1] Jacobian J = 3 / sum(...)                       */
+#define ATI_F_STRESS 10 /* [9] txx,tyy,tzz,txy,tyz,tzx,hxx,hyy,hzz              */
+#define ATI_F_SPONGE 11 /* [2] dense sponge coefficients asz, bsz (0 outside)    */
+#define ATI_NFIELDS 12
+
+/* ---- face buffers: drva/drvb/recv/cm (src/MainVar3D.f90:96-102) --------
+ * Layout as in the reference: buf(0:nbsize(nn)-1, ncomp, 0:1), face index
+ * jk = k*(ijk(2,nn)+1) + j (src/Main3D.f90:203-207). */
+#define ATI_FACE_DRVA 0 /* [5] boundary derivatives / characteristic R      */
+#define ATI_FACE_DRVB 1 /* [5] neighbour's drva (GCIC) / packed qa (averaging) */
+#define ATI_FACE_RECV 2 /* [3] sub-domain closure received by mpigo           */
+#define ATI_FACE_CM 3   /* [3] unit face normals                              */
+
+/* ---- boundary-condition codes (src/SingleTurbulence3D.f90:121-164) ------ */
+#define ATI_BC_INOUT 10    /* non-reflecting inflow/outflow GCBC */
+#define ATI_BC_WALL_INV 20 /* inviscid wall                      */
+#define ATI_BC_WALL 25     /* isothermal no-slip wall            */
+#define ATI_BC_INTER 30    /* characteristic interface (GCIC)    */
+#define ATI_BC_AVG 35      /* averaged interface                 */
+#define ATI_BC_SPLIT 40    /* internal split                     */
+#define ATI_BC_PERIODIC 45 /* periodic (self exchange)           */
+
+/* ---- configuration: the hot-path fields of inputo.dat / inputp.dat ------
+ * src/Main3D.f90:34-58 and src/SingleTurbulence3D.f90:39-62.  The block
+ * topology is the reference's H-grid (domdcomp, src/SingleTurbulence3D.f90:
+ * 121-164) with one sub-block per block (npc = 1): bkx*bky*bkz blocks,
+ * block mb = j*bkx + i, spanwise periodic, wall on top of block 1 and under
+ * block 4, inflow/outflow on the outer faces, interfaces elsewhere. */
+typedef struct ati_config {
+  int32_t bkx, bky, bkz;      /* blocks per direction (inputo.dat line 1)      */
+  int32_t lxibk[ATI_MAX_BK];  /* last xi index per block column (lxi0-to-bkx)  */
+  int32_t letbk[ATI_MAX_BK];  /* last eta index per block row                  */
+  int32_t lzebk[ATI_MAX_BK];  /* last zeta index per block plane               */
+  int32_t nkrk;               /* RK stages (4)                                 */
+  int32_t nviscous;           /* 1: Navier–Stokes, 0: Euler                    */
+  int32_t nsmf;               /* 1: frame velocity = freestream at once        */
+  int32_t les;                /* 1: Smagorinsky LES branch                     */
+  int32_t precision;          /* ATI_FP64 or ATI_MIXED                         */
+  int32_t reserved_i[7];
+  double reoo, tempoo;          /* Reynolds number, freestream temperature (K) */
+  double amach1, amach2, amach3;/* freestream Mach components                 */
+  double wtemp;                 /* wall temperature ratio                      */
+  double cfl;                   /* CFL number (used when dto < 0)              */
+  double timf;                  /* frame ramp time (nsmf = 0)                  */
+  double fltk, fltkbc;          /* filter cut-offs as fractions of pi          */
+  double dto;                   /* fixed dt if > 0, CFL mode if < 0            */
+  double aoa0, aoa1, tps, tp;   /* pitching (active when tp > 0)               */
+  double smago1, smago2;        /* LES constants                               */
+  double domlen, span;          /* domain length, span (inputp.dat)            */
+  double szth1, szth2, szxt, szco; /* sponge thicknesses and strength         */
+  double reserved_d[8];
+} ati_config_t;
+
+/* Time-marching scalars (src/MainVar3D.f90:121,141), restart header order
+ * of wrRsta (src/rpt.f90:589-600). */
+typedef struct ati_time {
+  int64_t n, ndt;
+  double dt, dts, dte, timo;
+} ati_time_t;
+
+typedef struct ati_handle ati_handle_t;
+
+/* ---- lifetime ----------------------------------------------------------- */
+/* Allocate all device arrays of one case (src/Main3D.f90:270-291) and build
+ * the scheme coefficients (penta, fcbcm, fcint, sbcco: src/Main3D.f90:295-332). */
+int ati_create(const ati_config_t *cfg, ati_handle_t **out);
+int ati_destroy(ati_handle_t *h);
+const char *ati_last_error(const ati_handle_t *h);
+int ati_abi_version(void);
+int ati_synchronize(ati_handle_t *h);
+
+/* Grid coordinates of block blk: xyz(0:lmx,3) = x,y,z planes, as rdGrid
+ * leaves them in ss(:,1:3) (src/rpt.f90:673-696). */
+int ati_set_grid(ati_handle_t *h, int blk, const double *xyz);
+
+/* After every block's grid is set: metrics and Jacobian on the device
+ * (src/Main3D.f90:365-413), face normals (:429-439), GCBC weights
+ * (:443-480), sponge (spongeup, src/SingleTurbulence3D.f90:209-249), and
+ * the initial condition of initialo (:203) with n = 0, dt = 0. */
+int ati_init(ati_handle_t *h);
+
+/* State and field copies (block blk, Fortran layout, all components). */
+int ati_set_state(ati_handle_t *h, int blk, const double *q);
+int ati_get_state(ati_handle_t *h, int blk, double *q);
+int ati_set_field(ati_handle_t *h, int blk, int field, const double *v);
+int ati_get_field(ati_handle_t *h, int blk, int field, double *v);
+int ati_get_face(ati_handle_t *h, int blk, int which, int nn, double *v);
+int ati_get_time(ati_handle_t *h, ati_time_t *t);
+int ati_set_time(ati_handle_t *h, const ati_time_t *t);
+/* Sizes: npts of block blk, and nbsize(nn) of its faces. */
+int ati_block_dims(ati_handle_t *h, int blk, int32_t dims[3], int64_t *npts);
+
+/* ---- granular calls, one per reference procedure, over all blocks ------- */
+/* mpigo(nt,nrt,n45,itag), src/Subroutines3D.f90:16-80: closure values of the
+ * faces with ndf = 1, exchanged on the device (BC 45: the line's other end). */
+int ati_mpigo(ati_handle_t *h, int nt, int nrt, int n45);
+/* deriv(nn,nz,m), src/Subroutines3D.f90:84-141: rr(:,nn) = d rr(:,nz) / d
+ * xi_nn on every line; boundary values to drva_nn(:,m,0:1). */
+int ati_deriv(ati_handle_t *h, int nn, int nz, int m);
+/* filte(nn,nz), src/Subroutines3D.f90:145-206: rr(:,nz) += filter correction. */
+int ati_filte(ati_handle_t *h, int nn, int nz);
+
+/* ---- fused calls -------------------------------------------------------- */
+/* Per-step filter of the five conservative variables, then qo = qa
+ * (src/Main3D.f90:555-561). */
+int ati_filter_step(ati_handle_t *h);
+/* One RK stage nk = 1..nkrk (src/Main3D.f90:567-958). */
+int ati_rk_stage(ati_handle_t *h, int nk);
+/* nsteps full time steps: filter, nkrk stages, n += 1, timo += dt
+ * (src/Main3D.f90:552-965).  Returns ATI_ENONFINITE if the state blew up. */
+int ati_step(ati_handle_t *h, int nsteps);
+
+/* Lift and drag of the wall blocks as clpost computes them
+ * (src/rpt.f90:1017-1056), from the p and stresses of the last stage:
+ * out[0] = force coefficient along x, out[1] = along y. */
+int ati_forces(ati_handle_t *h, double out[2]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ATI_H */
