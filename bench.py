@@ -1,0 +1,304 @@
+"""Benchmark: grid-point-stage updates/s of the ATI3D per-RK-stage hot path.
+
+A step is one full time step of the solver (per-step filter + 4 RK stages,
+src/Main3D.f90:552-965) over every block of one aerofoil case resident in HBM.
+The default workload is the 8.85 M-point NACA 0012 case in FP64
+(6 blocks 384x120x32, the reference's plain-FP64 larger-size configuration);
+grid-point-stage updates/s = points * 4 * steps / time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm prints one JSON line with the device-timed value (CUDA events on the
+solver's own stream), the end-to-end value through the C ABI with host
+buffers (pinned host -> device copy of the state and device -> host copy of
+the result inside every step), the roofline of the dominant kernel measured
+live from profiled launches, a CPU baseline (the CPU restatement of the
+reference, all host cores, bounded sample), clocks sampled during the timed
+region and the number of kernel launches.  Under torchrun every rank runs an
+independent replica of the case (the path has no exchange between GPUs);
+value is the sum over ranks divided by the slowest rank's time.
+
+--impl reference times the CPU restatement of the reference (the Fortran
+reference has no compiler on this system) with all host threads on the same
+workload, on rank 0 only.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt-stage updates/s FP64 vs mixed (rel L2 ≤1e-6); p50/p99 solve latency"
+UNIT = "grid-pt-stage updates/s"
+L2_BYTES = 129 * 2 ** 20
+
+# algorithmic work per point of one line-sweep launch (one input plane read,
+# one output plane written; flops of the 7-point RHS + forward + backward pass)
+SWEEP_BYTES = {"deriv": 16, "filter": 16}
+SWEEP_FLOPS = {"deriv": 17, "filter": 22}
+# canonical FP64 bytes per grid-point-stage of the whole stage (141 words)
+STAGE_BYTES_FP64 = 1128
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r for r in self.rows if len(r) >= 9]
+        idxs = sorted({r[0] for r in rows})
+        if len(idxs) > 1:
+            rows = [r for r in rows if r[0] == str(self.idx)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(cfg, grid, sample_steps=2, warm_steps=1):
+    """The CPU restatement of the reference, all host threads, on the same case."""
+    from oracle import oracle as orc
+    o = orc.OracleCase(cfg)
+    for mb in range(cfg.nblocks):
+        o.set_grid(mb, grid[mb])
+    o.init()
+    o.step(warm_steps)
+    t0 = time.perf_counter()
+    o.step(sample_steps)
+    dt = time.perf_counter() - t0
+    cores = orc.get_threads()
+    o.close()
+    return {"value": cfg.npoints * cfg.nkrk * sample_steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{sample_steps} time steps ({sample_steps * cfg.nkrk} RK stages) of the full "
+                      f"{cfg.npoints}-point case after {warm_steps} warm-up step, CPU restatement (oracle/), "
+                      f"OpenMP over lines, {cores} threads"}
+
+
+def run_reference(args, cfg, grid):
+    """--impl reference: the CPU restatement timed alone (rank 0 only)."""
+    from oracle import oracle as orc
+    o = orc.OracleCase(cfg)
+    for mb in range(cfg.nblocks):
+        o.set_grid(mb, grid[mb])
+    o.init()
+    t0 = time.perf_counter()
+    o.step(args.warmup)
+    t_warm = (time.perf_counter() - t0) / max(args.warmup, 1)
+    # bound the timed sample to about two minutes of CPU work
+    k = args.steps
+    if t_warm * k > 120.0:
+        k = max(1, int(120.0 / max(t_warm, 1e-9)))
+    t0 = time.perf_counter()
+    o.step(k)
+    dt = time.perf_counter() - t0
+    cores = orc.get_threads()
+    value = cfg.npoints * cfg.nkrk * k / dt
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
+            "ms_per_step": dt / k * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic: NACA 0012 grid from the reference's grid generator, uniform "
+                                    "freestream initial state",
+            "impl": "reference",
+            "config": {"workload": args.preset, "points": cfg.npoints},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{k} time steps of the full case after {args.warmup} warm-up steps "
+                                       f"(CPU restatement of the reference; the Fortran reference has no compiler "
+                                       f"here)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    o.close()
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--preset", default="naca0012_8p8m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    from tandemproject_gb300.config import PRESETS, FP64
+    from tandemproject_gb300.grid import aerofoil_grid
+    cfg = PRESETS[args.preset]
+    ws, rank, local = dist_env()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        grid = aerofoil_grid(cfg)
+        print(json.dumps(run_reference(args, cfg, grid)), flush=True)
+        return
+
+    import numpy as np
+    import torch
+    from tandemproject_gb300 import build as _b
+    from tandemproject_gb300.solver import Case, probe_fma_tflops
+
+    _b.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    grid = aerofoil_grid(cfg)
+    case = Case(cfg)
+    for mb in range(cfg.nblocks):
+        case.set_grid(mb, grid[mb])
+    case.init()
+    npts = cfg.npoints
+    stream = torch.cuda.ExternalStream(case.stream())
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up (includes the dt = 0 start-up steps of the reference's schedule)
+    case.step(args.warmup)
+    barrier()
+    l0 = case.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        e0.record(stream)
+        case.step(args.steps)
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1)
+    launches = case.launch_count() - l0
+    t_dev = ms / 1e3
+    if dist is not None:
+        tt = torch.tensor([t_dev], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = npts * cfg.nkrk * args.steps * ws / t_dev
+
+    # end to end through the C ABI: pinned host state in, step, state out
+    host = [torch.empty(5 * case.npts(mb), dtype=torch.float64, pin_memory=True) for mb in range(cfg.nblocks)]
+    hnp = [h.numpy() for h in host]
+    for mb in range(cfg.nblocks):
+        case.get_state(mb, out=hnp[mb])
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        for mb in range(cfg.nblocks):
+            case.set_state(mb, hnp[mb])
+        case.step(1)
+        for mb in range(cfg.nblocks):
+            case.get_state(mb, out=hnp[mb])
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    if dist is not None:
+        tt = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    bytes_state = 5 * npts * 8
+    e2e = {"value": npts * cfg.nkrk * args.e2e_steps * ws / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state, "steps": args.e2e_steps}
+
+    # roofline of the dominant kernel class from profiled launches
+    case.profile(True)
+    case.step(2)
+    prof = case.profile_read()
+    case.profile(False)
+    tot = sum(v[0] for v in prof.values())
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    kind = "filter" if dom.startswith("filter") else "deriv"
+    hbm_peak, peak_src = measured_peaks()
+    t_launch = dom_ms / max(dom_n, 1) / 1e3
+    achieved = SWEEP_BYTES[kind] * npts / t_launch / 1e9
+    fp64_peak = probe_fma_tflops(True)
+    fp64_ach = SWEEP_FLOPS[kind] * npts / t_launch / 1e12
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": None, "kernel": f"k_sweep<{dom}> (one launch = every line of one direction over all "
+                                            f"blocks, {SWEEP_BYTES[kind]} B and {SWEEP_FLOPS[kind]} flop per point)",
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
+                         "peak_source": "measured FP64 FMA throughput of this GPU (ati_probe_fma_tflops)"},
+                "stage_hbm_frac": STAGE_BYTES_FP64 * value / ws / 1e9 / hbm_peak,
+                "kernel_share": {k: round(v[0] / tot, 4) for k, v in prof.items() if v[1]}}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: NACA 0012 grid from the reference's grid generator (restated), uniform freestream "
+                    "initial state, impulsive start (nsmf = 1)",
+            "config": {"workload": f"{args.preset}: NACA 0012, 6 blocks "
+                                   f"{'x'.join(str(v + 1) for v in (cfg.lxibk[0], cfg.letbk[0], cfg.lzebk[0]))}, "
+                                   f"{npts} points, FP64, RK4, Re 4e5, M 0.24",
+                       "points": npts, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                       "l2": "no flush: the state alone (5 x 8 B x points) exceeds the 129 MB L2"},
+            "e2e": e2e, "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches}
+    case.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(cfg, grid)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

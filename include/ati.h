@@ -53,6 +53,9 @@ extern "C" {
 #define ATI_FP64 0  /* every array and operation in FP64 (the reference's nr=ieee64) */
 #define ATI_MIXED 1 /* line solves, filters, fluxes in FP32; metrics, Jacobian and
                        RK state (qa, qo) in FP64 */
+#define ATI_FP64_STRICT 2 /* FP64 with every operation rounded as written (no fused
+                             multiply-add contraction): matches the CPU restatement
+                             to the last bit except where libm differs */
 
 /* ---- field identifiers (the reference's module arrays) ------------------
  * src/MainVar3D.f90:78-85.  ncomp in brackets. */
@@ -176,6 +179,43 @@ int ati_rk_stage(ati_handle_t *h, int nk);
 /* nsteps full time steps: filter, nkrk stages, n += 1, timo += dt
  * (src/Main3D.f90:552-965).  Returns ATI_ENONFINITE if the state blew up. */
 int ati_step(ati_handle_t *h, int nsteps);
+
+/* ---- instrumentation (no counterpart in the reference) ------------------
+ * With profiling enabled every kernel launch of the handle is bracketed by
+ * CUDA events on the handle's stream and its device time is summed per
+ * kernel class (ATI_K_*); ati_profile_read synchronises and returns the sums
+ * in milliseconds with the launch counts.  ati_launch_count counts every
+ * kernel launch since creation, profiled or not. */
+#define ATI_K_DERIV_XI 0
+#define ATI_K_DERIV_ETA 1
+#define ATI_K_DERIV_ZETA 2
+#define ATI_K_FILTER_XI 3
+#define ATI_K_FILTER_ETA 4
+#define ATI_K_FILTER_ZETA 5
+#define ATI_K_MPIGO 6
+#define ATI_K_PRIM 7
+#define ATI_K_CFL 8
+#define ATI_K_GRAD 9
+#define ATI_K_STRESS 10
+#define ATI_K_FLUX 11
+#define ATI_K_DIV 12
+#define ATI_K_RK 13
+#define ATI_K_GCBC 14
+#define ATI_K_WALL_JUNCTION 15
+#define ATI_K_AVERAGE 16
+#define ATI_K_SCALAR 17
+#define ATI_K_COPY 18
+#define ATI_K_NSLOTS 19
+int ati_profile_enable(ati_handle_t *h, int enable);
+int ati_profile_read(ati_handle_t *h, int nslots, double *ms, int64_t *launches);
+int ati_launch_count(ati_handle_t *h, int64_t *count);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or events against the solver's. */
+void *ati_stream(ati_handle_t *h);
+/* FMA throughput of the current device (independent FMA chains, no memory
+ * traffic) in TFLOP/s, FP64 when fp64 != 0 else FP32: the compute roofline
+ * denominator of the FP64 path. */
+int ati_probe_fma_tflops(int fp64, double *tflops);
 
 /* Lift and drag of the wall blocks as clpost computes them
  * (src/rpt.f90:1017-1056), from the p and stresses of the last stage:

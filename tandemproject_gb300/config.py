@@ -14,6 +14,7 @@ import dataclasses
 MAX_BK = 8
 FP64 = 0
 MIXED = 1
+FP64_STRICT = 2
 
 
 class AtiConfig(ctypes.Structure):
@@ -150,6 +151,8 @@ class CaseConfig:
 
 PRESETS = {
     "naca0012_0p6m": CaseConfig(),
+    # a 228 K-point case whose CPU run takes seconds (smoke checks, quick benches)
+    "naca0012_0p2m": CaseConfig(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,)),
     # smgrid scales the near-wall spacing with resolution so that the quintic
     # grid lines of gridf stay monotone (no folded cells) at these sizes
     "naca0012_8p8m": CaseConfig(lxibk=(383, 383, 383), letbk=(119, 119), lzebk=(31,), smgrid=0.0025),

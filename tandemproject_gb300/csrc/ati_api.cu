@@ -1,0 +1,915 @@
+// ati_api.cu — C ABI (include/ati.h) over the sm_103a kernels.
+//
+// One handle = one aerofoil case = every block of the multi-block grid in one
+// GPU's HBM, with one CUDA stream.  The reference's MPI exchanges between
+// blocks (src/Subroutines3D.f90:47-56, src/Main3D.f90:799-813 and 901-925,
+// src/SingleTurbulence3D.f90:378-443) become reads of the neighbour block's
+// face buffers inside the kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ati.h"
+#include "ati_internal.h"
+#include "ati_kernels.h"
+#include "ati_scheme.h"
+
+using namespace ati;
+
+namespace {
+
+struct TaskRange {
+  int off = 0, n = 0, maxline = 0;
+};
+
+thread_local std::string g_create_err;
+
+}  // namespace
+
+struct ati_handle {
+  ati_config_t cfg{};
+  int nb = 0;
+  std::vector<BlockDev> blk;
+  SchemeHost sh{};
+  int64_t N = 0, F = 0, nfac = 0, nsbcc = 0, nwall = 0;
+  cudaStream_t st = nullptr;
+  char *arena = nullptr;
+  size_t arena_bytes = 0;
+  Ctx ctx{};
+  BlockDev *dblk = nullptr;
+  Scheme *dsc = nullptr;
+  Scalars *dscal = nullptr;
+  FaceTask *dtasks = nullptr;
+  std::vector<FaceTask> htasks;
+  TaskRange tl_mpigo, tl_gcbc, tl_gcbc_dir[4], tl_wall, tl_pack, tl_avg_dir[4], tl_force, tl_all;
+  JunctionDev *djn = nullptr;
+  int njct = 0, jnk = 0;
+  double *area = nullptr, *wnor = nullptr, *dforce = nullptr, *dspg = nullptr;
+  int64_t *dwoff = nullptr;
+  int maxlines[4] = {0, 0, 0, 0};
+  std::vector<int> grid_set;
+  bool inited = false;
+  int64_t n_host = 0;
+  std::string err;
+  // instrumentation
+  int64_t launches = 0;
+  bool profiling = false;
+  struct Ev {
+    cudaEvent_t a, b;
+    int cls;
+  };
+  std::vector<Ev> ev_used, ev_free;
+  double prof_ms[ATI_K_NSLOTS] = {0};
+  int64_t prof_n[ATI_K_NSLOTS] = {0};
+  int cur_cls = -1;
+  cudaEvent_t cur_a = nullptr;
+};
+
+// every launch site is wrapped in prof_begin/prof_end; without profiling
+// this only counts launches
+static void prof_begin(ati_handle *h, int cls) {
+  h->launches++;
+  if (!h->profiling) return;
+  ati_handle::Ev e;
+  if (!h->ev_free.empty()) {
+    e = h->ev_free.back();
+    h->ev_free.pop_back();
+  } else {
+    cudaEventCreate(&e.a);
+    cudaEventCreate(&e.b);
+  }
+  e.cls = cls;
+  cudaEventRecord(e.a, h->st);
+  h->ev_used.push_back(e);
+}
+static void prof_end(ati_handle *h) {
+  if (!h->profiling || h->ev_used.empty()) return;
+  cudaEventRecord(h->ev_used.back().b, h->st);
+}
+static void prof_drain(ati_handle *h) {
+  for (auto &e : h->ev_used) {
+    float ms = 0.f;
+    cudaEventSynchronize(e.b);
+    cudaEventElapsedTime(&ms, e.a, e.b);
+    h->prof_ms[e.cls] += ms;
+    h->prof_n[e.cls] += 1;
+    h->ev_free.push_back(e);
+  }
+  h->ev_used.clear();
+}
+#define PROF(h, cls, launch) \
+  do {                        \
+    prof_begin(h, cls);       \
+    launch;                   \
+    prof_end(h);              \
+  } while (0)
+
+static int fail(ati_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  else g_create_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                      \
+  do {                                                                                \
+    cudaError_t e_ = (call);                                                          \
+    if (e_ != cudaSuccess) return fail(h, ATI_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CKL()                                                                         \
+  do {                                                                                \
+    cudaError_t e_ = cudaGetLastError();                                              \
+    if (e_ != cudaSuccess) return fail(h, ATI_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+static const FaceTask *tp(const ati_handle *h, const TaskRange &r) { return h->dtasks + r.off; }
+
+// The two builds of the kernels: fused time steps use fast (FMA contraction)
+// unless the case asks for ATI_FP64_STRICT; set-up and the granular calls
+// always use strict, so they reproduce the reference's rounding.
+struct Ops {
+  decltype(&fast::launch_sweep) sweep;
+  decltype(&fast::launch_mpigo) mpigo;
+  decltype(&fast::launch_pointwise) pointwise;
+  decltype(&fast::launch_face) face;
+  decltype(&fast::launch_junction) junction;
+  decltype(&fast::launch_scalar) scalar;
+  decltype(&fast::launch_forces) forces;
+};
+static const Ops kFast = {fast::launch_sweep, fast::launch_mpigo, fast::launch_pointwise, fast::launch_face,
+                          fast::launch_junction, fast::launch_scalar, fast::launch_forces};
+static const Ops kStrict = {strict::launch_sweep, strict::launch_mpigo, strict::launch_pointwise, strict::launch_face,
+                            strict::launch_junction, strict::launch_scalar, strict::launch_forces};
+static const Ops &fused_ops(const ati_handle *h) { return h->cfg.precision == ATI_FP64_STRICT ? kStrict : kFast; }
+
+static void ijk_host(const BlockDev &B, int nn, int &i1, int &i2, int &i3) {
+  if (nn == 1) { i1 = B.lxi; i2 = B.let; i3 = B.lze; }
+  else if (nn == 2) { i1 = B.let; i2 = B.lze; i3 = B.lxi; }
+  else { i1 = B.lze; i2 = B.lxi; i3 = B.let; }
+}
+
+// ---- set-up kernels -----------------------------------------------------
+namespace {
+
+__device__ __forceinline__ int64_t sidx3(int lxi, int let, int i, int j, int k, int nn) {
+  if (nn == 1) return ((int64_t)k * (let + 1) + j) * (lxi + 1) + i;
+  if (nn == 2) return ((int64_t)j * (let + 1) + i) * (lxi + 1) + k;
+  return ((int64_t)i * (let + 1) + k) * (lxi + 1) + j;
+}
+
+__device__ __forceinline__ void sface(const BlockDev &B, int nn, int ip, int jk, int &i, int &j, int &k) {
+  int a1, a2;
+  if (nn == 1) { a1 = B.lxi; a2 = B.let; }
+  else if (nn == 2) { a1 = B.let; a2 = B.lze; }
+  else { a1 = B.lze; a2 = B.lxi; }
+  j = jk % (a2 + 1);
+  k = jk / (a2 + 1);
+  i = ip * a1;
+}
+
+// face unit normals (src/Main3D.f90:429-439)
+__global__ void k_cm(Ctx c, const FaceTask *tasks) {
+  const FaceTask T = tasks[blockIdx.y];
+  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk >= T.nline) return;
+  const BlockDev &B = c.blk[T.b];
+  int i, j, k;
+  sface(B, T.nn, T.ip, jk, i, j, k);
+  const int64_t g = B.off + sidx3(B.lxi, B.let, i, j, k, T.nn), N = c.N, nbs = T.nline;
+  const double *mt = T.nn == 1 ? c.xim : (T.nn == 2 ? c.etm : c.zem);
+  const double y = c.yaco[g];
+  const double r1 = y * mt[g], r2 = y * mt[g + N], r3 = y * mt[g + 2 * N];
+  const double f = 1.0 / sqrt(r1 * r1 + r2 * r2 + r3 * r3);
+  double *cm = c.cm + B.face_off[T.nn] * 6;
+  cm[jk + nbs * (0 + 3 * T.ip)] = f * r1;
+  cm[jk + nbs * (1 + 3 * T.ip)] = f * r2;
+  cm[jk + nbs * (2 + 3 * T.ip)] = f * r3;
+}
+
+// GCBC weights (src/Main3D.f90:460-480): visit counts, then weights
+__global__ void k_sbcc_count(Ctx c, const FaceTask *tasks, double *cnt) {
+  const FaceTask T = tasks[blockIdx.y];
+  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk >= T.nline) return;
+  const BlockDev &B = c.blk[T.b];
+  int i, j, k;
+  sface(B, T.nn, T.ip, jk, i, j, k);
+  const int iq = 1 - 2 * T.ip;
+  for (int ii = 0; ii <= MBCI; ii++) atomicAdd(&cnt[B.off + sidx3(B.lxi, B.let, i + iq * ii, j, k, T.nn)], 1.0);
+}
+
+__global__ void k_sbcc_weight(Ctx c, const FaceTask *tasks, const double *cnt, double *sbcc, double s1, double s2,
+                              double s3) {
+  const FaceTask T = tasks[blockIdx.y];
+  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk >= T.nline) return;
+  const BlockDev &B = c.blk[T.b];
+  int i, j, k;
+  sface(B, T.nn, T.ip, jk, i, j, k);
+  const int iq = 1 - 2 * T.ip;
+  const double res = 1.0 / c.yaco[B.off + sidx3(B.lxi, B.let, i, j, k, T.nn)];
+  const double sb[4] = {0.0, s1, s2, s3};
+  for (int ii = 0; ii <= MBCI; ii++) {
+    const double w = ii == 0 ? res : res * sb[ii];
+    sbcc[T.sbcc_off + (int64_t)jk * (MBCI + 1) + ii] = w / cnt[B.off + sidx3(B.lxi, B.let, i + iq * ii, j, k, T.nn)];
+  }
+}
+
+// sponge coefficients (spongeup, src/SingleTurbulence3D.f90:209-249); spg per
+// block: [0..2] nsz(0,:)*szr(0,:), [3..5] szp(0,:), [6..8] nsz(1,:)*szr(1,:), [9..11] szp(1,:)
+__global__ void k_sponge(Ctx c, const double *spg, double szco, double domlen, double pi) {
+  const BlockDev &B = c.blk[blockIdx.y];
+  const double *P = spg + 12 * blockIdx.y;
+  const int64_t N = c.N;
+  const double ra1 = 0.25, ra2 = pi / (2.0 * domlen);
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < B.npts; l += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t g = B.off + l;
+    double r[3];
+    for (int q = 0; q < 3; q++) {
+      const double x = c.ss[g + q * N];
+      r[q] = P[q] * fmax(P[3 + q] - x, 0.0) + P[6 + q] * fmax(x - P[9 + q], 0.0);
+    }
+    const double sig = szco * (1.0 - 0.125 * (1.0 + cos(pi * r[0])) * (1.0 + cos(pi * r[1])) * (1.0 + cos(pi * r[2])));
+    const double lam = ra1 + 0.5 * (1.0 - ra1) * (1.0 + cos(ra2 * (fmin(c.ss[g], domlen) + domlen)));
+    if (sig > 0.0) {
+      const double res = 1.0 / c.yaco[g];
+      c.asz[g] = res * sig * lam;
+      c.bsz[g] = res * c.sc->hamm1 * sig;
+    } else {
+      c.asz[g] = 0.0;
+      c.bsz[g] = 0.0;
+    }
+  }
+}
+
+// wall area and normals (wallArea/walldir, src/rpt.f90:774-864), list order
+// ll = k*(lxi+1) + i of the wall row j
+__global__ void k_wall_geom(Ctx c, const FaceTask *tasks, const int64_t *woff, double *area, double *wnor, int bcw) {
+  const FaceTask T = tasks[blockIdx.y];
+  const BlockDev &B = c.blk[T.b];
+  const int64_t nw = T.nline, N = c.N;
+  const int64_t ll = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (ll >= nw) return;
+  const int k = (int)(ll / (B.lxi + 1)), i = (int)(ll % (B.lxi + 1));
+  const int j = T.ip * B.let;
+  const double coef = T.ip == 0 ? 1.0 : -1.0;
+  const int64_t g = B.off + ((int64_t)k * (B.let + 1) + j) * (B.lxi + 1) + i;
+  const double a1 = c.qo[g], a3 = c.qo[g + 2 * N], b1 = c.qa[g], b3 = c.qa[g + 2 * N], d1 = c.de[g], d3 = c.de[g + 2 * N];
+  const double g11 = a1 * a1 + b1 * b1 + d1 * d1, g33 = a3 * a3 + b3 * b3 + d3 * d3, g13 = a1 * a3 + b1 * b3 + d1 * d3;
+  double ar = sqrt(g11 * g33 - g13 * g13);
+  if (i == 0) ar = ar * 0.5;
+  else if (i == B.lxi) ar = ar * 0.5;
+  if (k == 0) ar = ar * 0.5;
+  else if (k == B.lze) ar = ar * 0.5;
+  const int64_t o = woff[blockIdx.y];
+  area[o + ll] = ar;
+  const double e1 = c.etm[g], e2 = c.etm[g + N], e3 = c.etm[g + 2 * N];
+  const double tmp = coef / sqrt(e1 * e1 + e2 * e2 + e3 * e3);
+  wnor[3 * o + ll] = e1 * tmp;
+  wnor[3 * o + nw + ll] = e2 * tmp;
+  wnor[3 * o + 2 * nw + ll] = e3 * tmp;
+  (void)bcw;
+}
+
+// initial condition of initialo (src/SingleTurbulence3D.f90:203)
+__global__ void k_ic(Ctx c) {
+  const int64_t N = c.N;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    c.qa[g] = c.sc->rhooo;
+    c.qa[g + N] = 0.0;
+    c.qa[g + 2 * N] = 0.0;
+    c.qa[g + 3 * N] = 0.0;
+    c.qa[g + 4 * N] = c.sc->hamm1 * c.sc->poo;
+  }
+}
+
+}  // namespace
+
+// ---- topology: domdcomp (src/SingleTurbulence3D.f90:121-164), npc = 1 ---------
+static void topology(const ati_config_t &cfg, int mb, BlockDev &B, int nbcs[4], int nbce[4]) {
+  const int bkx = cfg.bkx, bky = cfg.bky, mbk = cfg.bkx * cfg.bky * cfg.bkz - 1;
+  const int bcw = 20 + 5 * cfg.nviscous, bcinout = 10, bcperiod = 45, bcinter = 30;
+  int ms[4], me[4];
+  const int ll = mb % bkx;
+  if (ll == 0) { ms[1] = mb + (bkx - 1); me[1] = mb + 1; nbcs[1] = bcinout; nbce[1] = bcinter; }
+  else if (ll == bkx - 1) { ms[1] = mb - 1; me[1] = mb - (bkx - 1); nbcs[1] = bcinter; nbce[1] = bcinout; }
+  else { ms[1] = mb - 1; me[1] = mb + 1; nbcs[1] = bcinter; nbce[1] = bcinter; }
+  if (mb < bkx) { ms[2] = mb + bkx * (bky - 1); me[2] = mb + bkx; nbcs[2] = bcinout; nbce[2] = bcinter; }
+  else if (mb > mbk - bkx) { ms[2] = mb - bkx; me[2] = mb - bkx * (bky - 1); nbcs[2] = bcinter; nbce[2] = bcinout; }
+  else { ms[2] = mb - bkx; me[2] = mb + bkx; nbcs[2] = bcinter; nbce[2] = bcinter; }
+  nbcs[3] = bcperiod; nbce[3] = bcperiod; ms[3] = mb; me[3] = mb;
+  if (mb == 1) nbce[2] = bcw;
+  if (mb == 4) nbcs[2] = bcw;
+  for (int nn = 1; nn <= 3; nn++) {
+    B.nbc[0][nn] = nbcs[nn]; B.nbc[1][nn] = nbce[nn];
+    B.ncd[0][nn] = ms[nn]; B.ncd[1][nn] = me[nn];
+    for (int ip = 0; ip <= 1; ip++) {
+      const int np = B.nbc[ip][nn];
+      B.ndf[ip][nn] = (np == 35 || np == 40 || np == 45) ? 1 : 0;
+    }
+  }
+}
+
+static bool is_gcbc(int np) { return np == 10 || np == 20 || np == 25 || np == 30; }
+static bool is_wall(int np) { return np == 20 || np == 25; }
+static bool is_avg(int np) { return np == 30 || np == 35 || np == 45; }
+
+// ---- lifetime --------------------------------------------------------------
+extern "C" int ati_abi_version(void) { return ATI_ABI_VERSION; }
+
+extern "C" const char *ati_last_error(const ati_handle_t *h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<double> &facf, std::vector<double> &spg) {
+  const ati_config_t &cfg = h->cfg;
+  int64_t off = 0, face = 0, fac = 0;
+  spg.assign((size_t)12 * h->nb, 0.0);
+  for (int mb = 0; mb < h->nb; mb++) {
+    BlockDev &B = h->blk[mb];
+    std::memset(&B, 0, sizeof(B));
+    const int i = mb % cfg.bkx, j = (mb / cfg.bkx) % cfg.bky, k = mb / (cfg.bkx * cfg.bky);
+    B.lxi = cfg.lxibk[i]; B.let = cfg.letbk[j]; B.lze = cfg.lzebk[k];
+    if (B.lxi < 6 || B.let < 6 || B.lze < 12) return fail(h, ATI_EINVAL, "block sizes: lxi, let >= 6 and lze >= 12 required");
+    int nbcs[4], nbce[4];
+    topology(cfg, mb, B, nbcs, nbce);
+    B.off = off;
+    B.npts = (int64_t)(B.lxi + 1) * (B.let + 1) * (B.lze + 1);
+    off += B.npts;
+    for (int nn = 1; nn <= 3; nn++) {
+      int a1, a2, a3;
+      ijk_host(B, nn, a1, a2, a3);
+      B.nbsize[nn] = (a2 + 1) * (a3 + 1);
+      B.face_off[nn] = face;
+      face += B.nbsize[nn];
+      B.fac_off[nn] = fac;
+      fac += a1 + 1;
+      h->maxlines[nn] = std::max(h->maxlines[nn], B.nbsize[nn]);
+    }
+    // sponge set-up constants (spongeup, src/SingleTurbulence3D.f90:211-222);
+    // the literal 0.7e0 is default (single) precision in the reference
+    const double p7 = (double)0.7f, dl = cfg.domlen;
+    double szr[2][4] = {{0, 1 / cfg.szth1, 1 / cfg.szth2, 0}, {0, 1 / (cfg.szth1 + cfg.szxt), 1 / cfg.szth2, 0}};
+    double szp[2][4] = {{0, -p7 * dl + cfg.szth1, -p7 * dl + cfg.szth2, 0},
+                        {0, dl - cfg.szth1, dl + cfg.szxt - cfg.szth2, 0}};
+    for (int nn = 1; nn <= 3; nn++) {
+      const double n0 = nbcs[nn] == 10 ? 1.0 : 0.0, n1 = nbce[nn] == 10 ? 1.0 : 0.0;
+      spg[12 * mb + (nn - 1)] = n0 * szr[0][nn];
+      spg[12 * mb + 3 + (nn - 1)] = szp[0][nn];
+      spg[12 * mb + 6 + (nn - 1)] = n1 * szr[1][nn];
+      spg[12 * mb + 9 + (nn - 1)] = szp[1][nn];
+    }
+  }
+  h->N = off;
+  h->F = face;
+  h->nfac = fac;
+  facd.assign((size_t)fac * 5, 0.0);
+  facf.assign((size_t)fac * 5, 0.0);
+  for (int mb = 0; mb < h->nb; mb++) {
+    const BlockDev &B = h->blk[mb];
+    for (int nn = 1; nn <= 3; nn++) {
+      int a1, a2, a3;
+      ijk_host(B, nn, a1, a2, a3);
+      const int ns = B.ndf[0][nn], ne = B.ndf[1][nn];
+      penta_factors(h->sh.albed[ns], h->sh.albed[ne], 0.5862704032801503, 0.09549533555017055, a1 + 1,
+                    &facd[(size_t)B.fac_off[nn] * 5]);
+      penta_factors(h->sh.albef[ns], h->sh.albef[ne], h->sh.alphf, h->sh.betf, a1 + 1, &facf[(size_t)B.fac_off[nn] * 5]);
+    }
+  }
+  // face task lists
+  auto &T = h->htasks;
+  T.clear();
+  auto add = [&](TaskRange &r, auto pred) {
+    r.off = (int)T.size();
+    for (int mb = 0; mb < h->nb; mb++)
+      for (int nn = 1; nn <= 3; nn++)
+        for (int ip = 0; ip <= 1; ip++) {
+          const BlockDev &B = h->blk[mb];
+          if (!pred(B, nn, ip)) continue;
+          FaceTask t{};
+          t.b = mb; t.nn = nn; t.ip = ip; t.bc = B.nbc[ip][nn]; t.nb_b = B.ncd[ip][nn];
+          t.nline = B.nbsize[nn]; t.sbcc_off = -1; t.wall_off = -1;
+          T.push_back(t);
+          r.maxline = std::max(r.maxline, t.nline);
+        }
+    r.n = (int)T.size() - r.off;
+  };
+  add(h->tl_mpigo, [](const BlockDev &B, int nn, int ip) { return B.ndf[ip][nn] == 1; });
+  add(h->tl_gcbc, [](const BlockDev &B, int nn, int ip) { return is_gcbc(B.nbc[ip][nn]); });
+  for (int d = 1; d <= 3; d++)
+    add(h->tl_gcbc_dir[d], [d](const BlockDev &B, int nn, int ip) { return nn == d && is_gcbc(B.nbc[ip][nn]); });
+  add(h->tl_wall, [](const BlockDev &B, int nn, int ip) { return is_wall(B.nbc[ip][nn]); });
+  add(h->tl_pack, [](const BlockDev &B, int nn, int ip) { return is_avg(B.nbc[ip][nn]); });
+  for (int d = 1; d <= 3; d++)
+    add(h->tl_avg_dir[d], [d](const BlockDev &B, int nn, int ip) { return nn == d && is_avg(B.nbc[ip][nn]); });
+  add(h->tl_all, [](const BlockDev &, int, int) { return true; });
+  const int bcw = 20 + 5 * cfg.nviscous;
+  add(h->tl_force, [bcw](const BlockDev &B, int nn, int ip) {
+    if (nn != 2) return false;
+    if (ip == 0) return B.nbc[0][2] == bcw;
+    return B.nbc[0][2] != bcw && B.nbc[1][2] == bcw;
+  });
+  // GCBC weight and wall offsets, keyed by (block, nn, ip)
+  std::vector<int64_t> sb_off((size_t)h->nb * 8, -1), w_off((size_t)h->nb * 8, -1);
+  int64_t ns = 0, nw = 0;
+  for (int mb = 0; mb < h->nb; mb++)
+    for (int nn = 1; nn <= 3; nn++)
+      for (int ip = 0; ip <= 1; ip++) {
+        const BlockDev &B = h->blk[mb];
+        const int np = B.nbc[ip][nn];
+        if (is_gcbc(np)) { sb_off[mb * 8 + nn * 2 + ip] = ns; ns += (int64_t)B.nbsize[nn] * (MBCI + 1); }
+        if (is_wall(np)) { w_off[mb * 8 + nn * 2 + ip] = nw; nw += B.nbsize[nn]; }
+      }
+  for (auto &t : T) {
+    t.sbcc_off = sb_off[t.b * 8 + t.nn * 2 + t.ip];
+    t.wall_off = w_off[t.b * 8 + t.nn * 2 + t.ip];
+  }
+  h->nsbcc = ns;
+  h->nwall = nw;
+  return ATI_OK;
+}
+
+extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
+  ati_handle *h = nullptr;
+  if (!cfg || !out) return fail(h, ATI_EINVAL, "null argument");
+  *out = nullptr;
+  if (cfg->bkx != 3 || cfg->bky != 2 || cfg->bkz != 1)
+    return fail(h, ATI_EINVAL, "the aerofoil H-grid topology has bkx=3, bky=2, bkz=1 blocks");
+  if (cfg->nkrk < 1 || cfg->nkrk > 8) return fail(h, ATI_EINVAL, "nkrk must be 1..8");
+  if (cfg->precision != ATI_FP64 && cfg->precision != ATI_FP64_STRICT)
+    return fail(h, ATI_EINVAL, "precision: ATI_FP64 or ATI_FP64_STRICT (the mixed path is not built into this handle)");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(h, ATI_ECUDA, "no CUDA device: this library has no CPU fallback");
+  h = new ati_handle();
+  h->cfg = *cfg;
+  h->nb = cfg->bkx * cfg->bky * cfg->bkz;
+  h->blk.resize(h->nb);
+  h->grid_set.assign(h->nb, 0);
+  build_scheme(*cfg, h->sh);
+  std::vector<double> facd, facf, spg;
+  int rc = build_tables(h, facd, facf, spg);
+  if (rc) {
+    g_create_err = h->err;
+    delete h;
+    return rc;
+  }
+  // arena: fields, face buffers, tables
+  const int64_t N = h->N, F = h->F;
+  const int nplanes = 5 + 5 + 5 + 3 + 3 + 3 + 3 + 3 + 1 + 1 + 9 + 1 + 1 + 1;
+  size_t bytes = 0;
+  auto take = [&](size_t n) {
+    size_t o = bytes;
+    bytes += (n * sizeof(double) + 255) & ~(size_t)255;
+    return o;
+  };
+  const size_t o_f = take((size_t)nplanes * N), o_drva = take((size_t)10 * F), o_drvb = take((size_t)10 * F),
+               o_recv = take((size_t)6 * F), o_cm = take((size_t)6 * F), o_facd = take(facd.size()),
+               o_facf = take(facf.size()), o_sbcc = take((size_t)std::max<int64_t>(h->nsbcc, 1)),
+               o_rpex = take((size_t)std::max<int64_t>(h->nwall, 1)), o_area = take((size_t)std::max<int64_t>(h->nwall, 1)),
+               o_wnor = take((size_t)3 * std::max<int64_t>(h->nwall, 1)), o_frc = take(64), o_spg = take(spg.size()),
+               o_blk = take((sizeof(BlockDev) * h->nb + 7) / 8), o_sc = take((sizeof(Scheme) + 7) / 8),
+               o_scal = take((sizeof(Scalars) + 7) / 8), o_task = take((sizeof(FaceTask) * h->htasks.size() + 7) / 8),
+               o_jn = take((sizeof(JunctionDev) * 4 + 7) / 8), o_woff = take(16);
+  cudaError_t e = cudaMalloc(&h->arena, bytes);
+  if (e != cudaSuccess) {
+    g_create_err = std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e);
+    delete h;
+    return ATI_ENOMEM;
+  }
+  h->arena_bytes = bytes;
+  auto D = [&](size_t o) { return (double *)(h->arena + o); };
+  Ctx &c = h->ctx;
+  double *f = D(o_f);
+  c.N = N;
+  c.qa = f; f += 5 * N; c.qo = f; f += 5 * N; c.de = f; f += 5 * N; c.rr = f; f += 3 * N; c.ss = f; f += 3 * N;
+  c.xim = f; f += 3 * N; c.etm = f; f += 3 * N; c.zem = f; f += 3 * N; c.p = f; f += N; c.yaco = f; f += N;
+  c.tau = f; f += 9 * N; c.asz = f; f += N; c.bsz = f; f += N; c.fw = f; f += N;
+  c.drva = D(o_drva); c.drvb = D(o_drvb); c.recv = D(o_recv); c.cm = D(o_cm);
+  c.facd = D(o_facd); c.facf = D(o_facf);
+  c.sbcc = D(o_sbcc); c.rpex = D(o_rpex);
+  h->area = D(o_area); h->wnor = D(o_wnor); h->dforce = D(o_frc); h->dspg = D(o_spg);
+  h->dblk = (BlockDev *)(h->arena + o_blk);
+  h->dsc = (Scheme *)(h->arena + o_sc);
+  h->dscal = (Scalars *)(h->arena + o_scal);
+  h->dtasks = (FaceTask *)(h->arena + o_task);
+  h->djn = (JunctionDev *)(h->arena + o_jn);
+  h->dwoff = (int64_t *)(h->arena + o_woff);
+  c.blk = h->dblk; c.sc = h->dsc; c.scal = h->dscal;
+  // junctions (src/SingleTurbulence3D.f90:386-398), bkx = 3, bky = 2
+  std::vector<JunctionDev> jn;
+  for (int nn = 0; nn <= (cfg->bkx - 1) * (cfg->bky - 1) - 1; nn++) {
+    const int njct = nn + nn / (cfg->bkx - 1);
+    const int mm[4] = {njct, njct + 1, njct + cfg->bkx, njct + cfg->bkx + 1};
+    const int cip[4] = {1, 0, 1, 0}, cjp[4] = {1, 1, 0, 0};
+    JunctionDev J{};
+    for (int q = 0; q < 4; q++) {
+      const BlockDev &B = h->blk[mm[q]];
+      const int i = cip[q] * B.lxi, j = cjp[q] * B.let;
+      J.base[q] = B.off + (int64_t)j * (B.lxi + 1) + i;
+      J.kstr[q] = (int64_t)(B.lxi + 1) * (B.let + 1);
+    }
+    J.nk = h->blk[mm[0]].lze + 1;
+    J.pa = (1 - nn) == 1 ? 2 : 1;
+    J.pb = (1 - nn) == 1 ? 4 : 3;
+    jn.push_back(J);
+    h->jnk = std::max(h->jnk, J.nk);
+  }
+  h->njct = (int)jn.size();
+  std::vector<int64_t> woff;
+  for (int q = 0; q < h->tl_force.n; q++) woff.push_back(h->htasks[h->tl_force.off + q].wall_off);
+  e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->arena, 0, bytes, h->st);
+  auto up = [&](void *dst, const void *src, size_t n) {
+    if (e == cudaSuccess && n) e = cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, h->st);
+  };
+  up(const_cast<double *>(c.facd), facd.data(), facd.size() * 8);
+  up(const_cast<double *>(c.facf), facf.data(), facf.size() * 8);
+  up(h->dspg, spg.data(), spg.size() * 8);
+  up(h->dblk, h->blk.data(), sizeof(BlockDev) * h->nb);
+  up(h->dsc, &h->sh.s, sizeof(Scheme));
+  up(h->dtasks, h->htasks.data(), sizeof(FaceTask) * h->htasks.size());
+  up(h->djn, jn.data(), sizeof(JunctionDev) * jn.size());
+  up(h->dwoff, woff.data(), sizeof(int64_t) * woff.size());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) {
+    g_create_err = std::string("set-up copy: ") + cudaGetErrorString(e);
+    cudaFree(h->arena);
+    delete h;
+    return ATI_ECUDA;
+  }
+  *out = h;
+  return ATI_OK;
+}
+
+extern "C" int ati_destroy(ati_handle_t *h) {
+  if (!h) return ATI_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  prof_drain(h);
+  for (auto &e : h->ev_free) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  if (h->arena) cudaFree(h->arena);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return ATI_OK;
+}
+
+extern "C" int ati_synchronize(ati_handle_t *h) {
+  if (!h) return ATI_EINVAL;
+  CK(cudaStreamSynchronize(h->st));
+  return ATI_OK;
+}
+
+extern "C" int ati_block_dims(ati_handle_t *h, int blk, int32_t dims[3], int64_t *npts) {
+  if (!h || blk < 0 || blk >= h->nb || !dims) return fail(h, ATI_EINVAL, "ati_block_dims: bad argument");
+  dims[0] = h->blk[blk].lxi; dims[1] = h->blk[blk].let; dims[2] = h->blk[blk].lze;
+  if (npts) *npts = h->blk[blk].npts;
+  return ATI_OK;
+}
+
+// ---- field copies ----------------------------------------------------------
+static double *field_base(ati_handle *h, int field, int &ncomp) {
+  Ctx &c = h->ctx;
+  switch (field) {
+    case ATI_F_QA: ncomp = 5; return c.qa;
+    case ATI_F_QO: ncomp = 5; return c.qo;
+    case ATI_F_DE: ncomp = 5; return c.de;
+    case ATI_F_RR: ncomp = 3; return c.rr;
+    case ATI_F_SS: ncomp = 3; return c.ss;
+    case ATI_F_XIM: ncomp = 3; return c.xim;
+    case ATI_F_ETM: ncomp = 3; return c.etm;
+    case ATI_F_ZEM: ncomp = 3; return c.zem;
+    case ATI_F_P: ncomp = 1; return c.p;
+    case ATI_F_YACO: ncomp = 1; return c.yaco;
+    case ATI_F_STRESS: ncomp = 9; return c.tau;
+    case ATI_F_SPONGE: ncomp = 2; return c.asz;  // asz and bsz are adjacent planes
+    default: ncomp = 0; return nullptr;
+  }
+}
+
+static int copy_field(ati_handle *h, int blk, int field, double *host, bool to_dev) {
+  if (!h || blk < 0 || blk >= h->nb || !host) return fail(h, ATI_EINVAL, "field copy: bad argument");
+  int nc = 0;
+  double *base = field_base(h, field, nc);
+  if (!base) return fail(h, ATI_EINVAL, "unknown field id");
+  const BlockDev &B = h->blk[blk];
+  const size_t w = (size_t)B.npts * sizeof(double), dp = (size_t)h->N * sizeof(double);
+  if (to_dev) {
+    CK(cudaMemcpy2DAsync(base + B.off, dp, host, w, w, nc, cudaMemcpyHostToDevice, h->st));
+  } else {
+    CK(cudaMemcpy2DAsync(host, w, base + B.off, dp, w, nc, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return ATI_OK;
+}
+
+extern "C" int ati_set_field(ati_handle_t *h, int blk, int field, const double *v) {
+  return copy_field(h, blk, field, const_cast<double *>(v), true);
+}
+extern "C" int ati_get_field(ati_handle_t *h, int blk, int field, double *v) { return copy_field(h, blk, field, v, false); }
+extern "C" int ati_set_state(ati_handle_t *h, int blk, const double *q) {
+  return copy_field(h, blk, ATI_F_QA, const_cast<double *>(q), true);
+}
+extern "C" int ati_get_state(ati_handle_t *h, int blk, double *q) { return copy_field(h, blk, ATI_F_QA, q, false); }
+
+extern "C" int ati_get_face(ati_handle_t *h, int blk, int which, int nn, double *v) {
+  if (!h || blk < 0 || blk >= h->nb || nn < 1 || nn > 3 || !v) return fail(h, ATI_EINVAL, "ati_get_face: bad argument");
+  const BlockDev &B = h->blk[blk];
+  const double *src;
+  int nc;
+  switch (which) {
+    case ATI_FACE_DRVA: src = h->ctx.drva; nc = 10; break;
+    case ATI_FACE_DRVB: src = h->ctx.drvb; nc = 10; break;
+    case ATI_FACE_RECV: src = h->ctx.recv; nc = 6; break;
+    case ATI_FACE_CM: src = h->ctx.cm; nc = 6; break;
+    default: return fail(h, ATI_EINVAL, "unknown face buffer");
+  }
+  CK(cudaMemcpyAsync(v, src + B.face_off[nn] * nc, sizeof(double) * nc * B.nbsize[nn], cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return ATI_OK;
+}
+
+extern "C" int ati_get_time(ati_handle_t *h, ati_time_t *t) {
+  if (!h || !t) return fail(h, ATI_EINVAL, "ati_get_time: bad argument");
+  Scalars s;
+  CK(cudaMemcpyAsync(&s, h->dscal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  t->n = s.n; t->ndt = s.ndt; t->dt = s.dt; t->dts = s.dts; t->dte = s.dte; t->timo = s.timo;
+  return ATI_OK;
+}
+
+extern "C" int ati_set_time(ati_handle_t *h, const ati_time_t *t) {
+  if (!h || !t) return fail(h, ATI_EINVAL, "ati_set_time: bad argument");
+  Scalars s;
+  CK(cudaMemcpyAsync(&s, h->dscal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  s.n = t->n; s.ndt = t->ndt; s.dt = t->dt; s.dts = t->dts; s.dte = t->dte; s.timo = t->timo;
+  CK(cudaMemcpyAsync(h->dscal, &s, sizeof(s), cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->n_host = t->n;
+  return ATI_OK;
+}
+
+extern "C" int ati_set_grid(ati_handle_t *h, int blk, const double *xyz) {
+  int rc = copy_field(h, blk, ATI_F_SS, const_cast<double *>(xyz), true);
+  if (rc == ATI_OK) h->grid_set[blk] = 1;
+  return rc;
+}
+
+// ---- granular calls ----------------------------------------------------------
+static int mpigo_src(ati_handle *h, const Ops &o, int nt, int n45, const double *s1, const double *s2,
+                     const double *s3) {
+  if (h->tl_mpigo.n == 0) return ATI_OK;
+  PROF(h, ATI_K_MPIGO, o.mpigo(h->ctx, h->st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, nt, n45, s1, s2, s3));
+  CKL();
+  return ATI_OK;
+}
+
+static int sweep(ati_handle *h, const Ops &o, int nn, bool filt, const double *in, double *out, int m) {
+  PROF(h, (filt ? ATI_K_FILTER_XI : ATI_K_DERIV_XI) + nn - 1,
+       o.sweep(h->ctx, h->st, nn, filt, in, out, m, h->nb, h->maxlines[nn]));
+  CKL();
+  return ATI_OK;
+}
+
+extern "C" int ati_mpigo(ati_handle_t *h, int nt, int nrt, int n45) {
+  if (!h || nt < 0 || nt > 1 || nrt < 0 || nrt > 1 || n45 < 0 || n45 > 1) return fail(h, ATI_EINVAL, "ati_mpigo: bad selector");
+  const int64_t N = h->N;
+  const double *r = h->ctx.rr;
+  // nz = (1-nrt)*(nn-1)+1 (src/Subroutines3D.f90:23)
+  if (nrt == 1) return mpigo_src(h, kStrict, nt, n45, r, r, r);
+  return mpigo_src(h, kStrict, nt, n45, r, r + N, r + 2 * N);
+}
+
+extern "C" int ati_deriv(ati_handle_t *h, int nn, int nz, int m) {
+  if (!h || nn < 1 || nn > 3 || nz < 1 || nz > 3 || m < 1 || m > 5) return fail(h, ATI_EINVAL, "ati_deriv: bad selector");
+  const int64_t N = h->N;
+  return sweep(h, kStrict, nn, false, h->ctx.rr + (nz - 1) * N, h->ctx.rr + (nn - 1) * N, m);
+}
+
+extern "C" int ati_filte(ati_handle_t *h, int nn, int nz) {
+  if (!h || nn < 1 || nn > 3 || nz < 1 || nz > 3) return fail(h, ATI_EINVAL, "ati_filte: bad selector");
+  const int64_t N = h->N;
+  return sweep(h, kStrict, nn, true, h->ctx.rr + (nz - 1) * N, h->ctx.rr + (nz - 1) * N, 0);
+}
+
+// ---- set-up: metrics, normals, GCBC weights, sponge, wall, IC ---------------
+extern "C" int ati_init(ati_handle_t *h) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
+  for (int b = 0; b < h->nb; b++)
+    if (!h->grid_set[b]) return fail(h, ATI_ESTATE, "ati_init: grid of block " + std::to_string(b) + " not set");
+  Ctx &c = h->ctx;
+  const int64_t N = h->N;
+  // coordinate derivatives (src/Main3D.f90:365-375)
+  double *dst[3] = {c.qo, c.qa, c.de};
+  for (int m = 1; m <= 3; m++) {
+    CK(cudaMemcpyAsync(c.rr, c.ss + (m - 1) * N, sizeof(double) * N, cudaMemcpyDeviceToDevice, h->st));
+    int rc = ati_mpigo(h, 0, 1, 1);
+    if (!rc) rc = ati_deriv(h, 3, 1, m);
+    if (!rc) rc = ati_deriv(h, 2, 1, m);
+    if (!rc) rc = ati_deriv(h, 1, 1, m);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(dst[m - 1], c.rr, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, h->st));
+  }
+  kStrict.pointwise(c, h->st, PW_METRICS, 0, nullptr, nullptr, nullptr);
+  CKL();
+  // wall area and normals (from the coordinate derivatives still in qo/qa/de)
+  if (h->tl_force.n) {
+    k_wall_geom<<<dim3((h->tl_force.maxline + 127) / 128, h->tl_force.n), 128, 0, h->st>>>(
+        c, tp(h, h->tl_force), h->dwoff, h->area, h->wnor, 20 + 5 * h->cfg.nviscous);
+    CKL();
+  }
+  // face normals
+  k_cm<<<dim3((h->tl_all.maxline + 127) / 128, h->tl_all.n), 128, 0, h->st>>>(c, tp(h, h->tl_all));
+  CKL();
+  // GCBC weights: visit counts in the fw scratch plane
+  CK(cudaMemsetAsync(c.fw, 0, sizeof(double) * N, h->st));
+  if (h->tl_gcbc.n) {
+    dim3 g((h->tl_gcbc.maxline + 127) / 128, h->tl_gcbc.n);
+    k_sbcc_count<<<g, 128, 0, h->st>>>(c, tp(h, h->tl_gcbc), c.fw);
+    k_sbcc_weight<<<g, 128, 0, h->st>>>(c, tp(h, h->tl_gcbc), c.fw, const_cast<double *>(c.sbcc), h->sh.sbci[1],
+                                        h->sh.sbci[2], h->sh.sbci[3]);
+    CKL();
+  }
+  // sponge (the grid coordinates are still in ss)
+  k_sponge<<<dim3(64, h->nb), 256, 0, h->st>>>(c, h->dspg, h->cfg.szco, h->cfg.domlen, std::acos(-1.0));
+  CKL();
+  // initial condition and time scalars (src/Main3D.f90:520-522)
+  k_ic<<<256, 256, 0, h->st>>>(c);
+  CKL();
+  CK(cudaMemsetAsync(h->dscal, 0, sizeof(Scalars), h->st));
+  kStrict.scalar(c, h->st, SC_INIT, 0);
+  CKL();
+  CK(cudaStreamSynchronize(h->st));
+  h->n_host = 0;
+  h->inited = true;
+  return ATI_OK;
+}
+
+// ---- fused calls ----------------------------------------------------------------
+static int filter_step(ati_handle *h) {
+  Ctx &c = h->ctx;
+  const Ops &o = fused_ops(h);
+  const int64_t N = h->N;
+  for (int m = 1; m <= 5; m++) {
+    double *q = c.qa + (m - 1) * N;
+    int rc = mpigo_src(h, o, 1, 0, q, q, q);
+    for (int nn = 1; nn <= 3 && !rc; nn++) rc = sweep(h, o, nn, true, q, q, 0);
+    if (rc) return rc;
+  }
+  prof_begin(h, ATI_K_COPY);
+  cudaError_t e = cudaMemcpyAsync(c.qo, c.qa, sizeof(double) * 5 * N, cudaMemcpyDeviceToDevice, h->st);
+  prof_end(h);
+  CK(e);
+  return ATI_OK;
+}
+
+static int rk_stage(ati_handle *h, int nk) {
+  Ctx &c = h->ctx;
+  cudaStream_t st = h->st;
+  const Ops &o = fused_ops(h);
+  const int64_t N = h->N;
+  int rc = 0;
+#define PWX(cls, which, ...) PROF(h, cls, o.pointwise(c, st, which, __VA_ARGS__))
+#define FKX(cls, which, tasks, n, ml) \
+  do {                                 \
+    if ((n) > 0) PROF(h, cls, o.face(c, st, which, tasks, n, ml)); \
+  } while (0)
+  PROF(h, ATI_K_SCALAR, o.scalar(c, st, SC_MOVEF_A, nk));
+  PWX(ATI_K_PRIM, PW_PRIM, 0, nullptr, nullptr, nullptr);
+  if (nk == 1) {
+    if (h->n_host % 10 == 1) {
+      if (h->cfg.dto < 0) {
+        PROF(h, ATI_K_SCALAR, o.scalar(c, st, SC_CFL_RESET, nk));
+        PWX(ATI_K_CFL, PW_CFL, 0, nullptr, nullptr, nullptr);
+      }
+      PROF(h, ATI_K_SCALAR, o.scalar(c, st, SC_DT_NEW, nk));
+    }
+    PROF(h, ATI_K_SCALAR, o.scalar(c, st, SC_DT, nk));
+  }
+  CKL();
+  if (h->cfg.nviscous == 1) {
+    double *t = c.tau;
+    double *outs[4][3] = {{t, t + 8 * N, t + 5 * N},            // txx, hzz, tzx
+                          {t + 3 * N, t + N, t + 6 * N},        // txy, tyy, hxx
+                          {t + 7 * N, t + 4 * N, t + 2 * N},    // hyy, tyz, tzz
+                          {c.ss, c.ss + N, c.ss + 2 * N}};      // temperature gradient
+    for (int m = 2; m <= 5; m++) {
+      const double *src = c.de + (m - 1) * N;
+      if ((rc = mpigo_src(h, o, 0, 0, src, src, src))) return rc;
+      if ((rc = sweep(h, o, 3, false, src, c.rr + 2 * N, m))) return rc;
+      if ((rc = sweep(h, o, 2, false, src, c.rr + N, m))) return rc;
+      if ((rc = sweep(h, o, 1, false, src, c.rr, m))) return rc;
+      PWX(ATI_K_GRAD, PW_GRAD, m, outs[m - 2][0], outs[m - 2][1], outs[m - 2][2]);
+    }
+    PWX(ATI_K_STRESS, PW_STRESS, 0, nullptr, nullptr, nullptr);
+  }
+  PWX(ATI_K_FLUX, PW_FLUXPREP, 0, nullptr, nullptr, nullptr);
+  CKL();
+  for (int m = 1; m <= 5; m++) {
+    PWX(ATI_K_FLUX, PW_FLUX, m, nullptr, nullptr, nullptr);
+    if ((rc = mpigo_src(h, o, 0, 0, c.rr, c.rr + N, c.rr + 2 * N))) return rc;
+    for (int nn = 1; nn <= 3; nn++)
+      if ((rc = sweep(h, o, nn, false, c.rr + (nn - 1) * N, c.rr + (nn - 1) * N, m))) return rc;
+    PWX(ATI_K_DIV, PW_DIV, m, nullptr, nullptr, nullptr);
+  }
+  FKX(ATI_K_GCBC, FK_GCBC_PREP, tp(h, h->tl_gcbc), h->tl_gcbc.n, h->tl_gcbc.maxline);
+  for (int d = 1; d <= 3; d++)
+    FKX(ATI_K_GCBC, FK_GCBC_APPLY, tp(h, h->tl_gcbc_dir[d]), h->tl_gcbc_dir[d].n, h->tl_gcbc_dir[d].maxline);
+  PROF(h, ATI_K_SCALAR, o.scalar(c, st, SC_MOVEF_B, nk));
+  PWX(ATI_K_RK, PW_RK, 0, nullptr, nullptr, nullptr);
+  FKX(ATI_K_WALL_JUNCTION, FK_WALL, tp(h, h->tl_wall), h->tl_wall.n, h->tl_wall.maxline);
+  PROF(h, ATI_K_WALL_JUNCTION, o.junction(c, st, h->djn, h->njct, h->jnk));
+  FKX(ATI_K_AVERAGE, FK_PACK, tp(h, h->tl_pack), h->tl_pack.n, h->tl_pack.maxline);
+  for (int d = 1; d <= 3; d++)
+    FKX(ATI_K_AVERAGE, FK_AVG, tp(h, h->tl_avg_dir[d]), h->tl_avg_dir[d].n, h->tl_avg_dir[d].maxline);
+  CKL();
+  return ATI_OK;
+#undef PWX
+#undef FKX
+}
+
+static int check_flag(ati_handle *h) {
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, &h->dscal->flag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (flag) return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state (flag " +
+                                               std::to_string(flag) + ")");
+  return ATI_OK;
+}
+
+extern "C" int ati_filter_step(ati_handle_t *h) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  return filter_step(h);
+}
+
+extern "C" int ati_rk_stage(ati_handle_t *h, int nk) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  if (nk < 1 || nk > h->cfg.nkrk) return fail(h, ATI_EINVAL, "ati_rk_stage: nk out of range");
+  return rk_stage(h, nk);
+}
+
+extern "C" int ati_step(ati_handle_t *h, int nsteps) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  if (nsteps < 0) return fail(h, ATI_EINVAL, "nsteps < 0");
+  for (int s = 0; s < nsteps; s++) {
+    int rc = filter_step(h);
+    for (int nk = 1; nk <= h->cfg.nkrk && !rc; nk++) rc = rk_stage(h, nk);
+    if (rc) return rc;
+    PROF(h, ATI_K_SCALAR, fused_ops(h).scalar(h->ctx, h->st, SC_ADVANCE, 0));
+    CKL();
+    h->n_host++;
+  }
+  return check_flag(h);
+}
+
+extern "C" int ati_forces(ati_handle_t *h, double out[2]) {
+  if (!h || !out) return fail(h, ATI_EINVAL, "ati_forces: bad argument");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  kStrict.forces(h->ctx, h->st, tp(h, h->tl_force), h->tl_force.n, h->area, h->wnor, h->dwoff, h->dforce);
+  CKL();
+  std::vector<double> part((size_t)2 * h->tl_force.n);
+  CK(cudaMemcpyAsync(part.data(), h->dforce, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const double dynp = 2.0 / (h->sh.s.amachoo * h->sh.s.amachoo * h->cfg.span);
+  out[0] = 0.0; out[1] = 0.0;
+  for (int q = 0; q < h->tl_force.n; q++) {  // blocks in rank order, as MPI_REDUCE over wcom
+    out[0] = out[0] + part[2 * q] * dynp;
+    out[1] = out[1] + part[2 * q + 1] * dynp;
+  }
+  return ATI_OK;
+}
+
+// ---- instrumentation ------------------------------------------------------------
+extern "C" int ati_profile_enable(ati_handle_t *h, int enable) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
+  CK(cudaStreamSynchronize(h->st));
+  prof_drain(h);
+  h->profiling = enable != 0;
+  for (int q = 0; q < ATI_K_NSLOTS; q++) { h->prof_ms[q] = 0.0; h->prof_n[q] = 0; }
+  return ATI_OK;
+}
+
+extern "C" int ati_profile_read(ati_handle_t *h, int nslots, double *ms, int64_t *launches) {
+  if (!h || nslots < 0 || (nslots > 0 && (!ms || !launches))) return fail(h, ATI_EINVAL, "ati_profile_read: bad argument");
+  CK(cudaStreamSynchronize(h->st));
+  prof_drain(h);
+  for (int q = 0; q < nslots && q < ATI_K_NSLOTS; q++) { ms[q] = h->prof_ms[q]; launches[q] = h->prof_n[q]; }
+  return ATI_OK;
+}
+
+extern "C" int ati_launch_count(ati_handle_t *h, int64_t *count) {
+  if (!h || !count) return fail(h, ATI_EINVAL, "ati_launch_count: bad argument");
+  *count = h->launches;
+  return ATI_OK;
+}
+
+extern "C" void *ati_stream(ati_handle_t *h) { return h ? (void *)h->st : nullptr; }

@@ -1,0 +1,252 @@
+"""Host-side mirror of the reference's call surface over the CUDA library.
+
+``Case`` owns one ``ati_handle_t`` (include/ati.h).  Its methods keep the
+reference's names and selector arguments:
+
+    mpigo(nt, nrt, n45)      src/Subroutines3D.f90:16-80
+    deriv(nn, nz, m)         src/Subroutines3D.f90:84-141
+    filte(nn, nz)            src/Subroutines3D.f90:145-206
+    filter_step()            src/Main3D.f90:555-561
+    rk_stage(nk)             src/Main3D.f90:567-958
+    step(nsteps)             src/Main3D.f90:552-965
+    forces()                 clpost, src/rpt.f90:1017-1056
+
+There is no CPU fallback: if libati.so cannot be loaded, or no CUDA device is
+present, construction raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .config import AtiTime, CaseConfig
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libati.so")
+
+ATI_OK, ATI_EINVAL, ATI_ENOMEM, ATI_ECUDA, ATI_ENONFINITE, ATI_ETIMEDOUT, ATI_ESTATE = range(7)
+F_QA, F_QO, F_DE, F_RR, F_SS, F_XIM, F_ETM, F_ZEM, F_P, F_YACO, F_STRESS, F_SPONGE = range(12)
+FACE_DRVA, FACE_DRVB, FACE_RECV, FACE_CM = range(4)
+NCOMP = {F_QA: 5, F_QO: 5, F_DE: 5, F_RR: 3, F_SS: 3, F_XIM: 3, F_ETM: 3, F_ZEM: 3, F_P: 1, F_YACO: 1,
+         F_STRESS: 9, F_SPONGE: 2}
+
+# every entry point declared in include/ati.h, with its ctypes signature
+_vp, _i32, _dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+SIGNATURES = {
+    "ati_abi_version": ([], ctypes.c_int),
+    "ati_create": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
+    "ati_destroy": ([_vp], ctypes.c_int),
+    "ati_last_error": ([_vp], ctypes.c_char_p),
+    "ati_synchronize": ([_vp], ctypes.c_int),
+    "ati_set_grid": ([_vp, _i32, _dp], ctypes.c_int),
+    "ati_init": ([_vp], ctypes.c_int),
+    "ati_set_state": ([_vp, _i32, _dp], ctypes.c_int),
+    "ati_get_state": ([_vp, _i32, _dp], ctypes.c_int),
+    "ati_set_field": ([_vp, _i32, _i32, _dp], ctypes.c_int),
+    "ati_get_field": ([_vp, _i32, _i32, _dp], ctypes.c_int),
+    "ati_get_face": ([_vp, _i32, _i32, _i32, _dp], ctypes.c_int),
+    "ati_get_time": ([_vp, _vp], ctypes.c_int),
+    "ati_set_time": ([_vp, _vp], ctypes.c_int),
+    "ati_block_dims": ([_vp, _i32, _vp, _vp], ctypes.c_int),
+    "ati_mpigo": ([_vp, _i32, _i32, _i32], ctypes.c_int),
+    "ati_deriv": ([_vp, _i32, _i32, _i32], ctypes.c_int),
+    "ati_filte": ([_vp, _i32, _i32], ctypes.c_int),
+    "ati_filter_step": ([_vp], ctypes.c_int),
+    "ati_rk_stage": ([_vp, _i32], ctypes.c_int),
+    "ati_step": ([_vp, _i32], ctypes.c_int),
+    "ati_forces": ([_vp, _dp], ctypes.c_int),
+    "ati_profile_enable": ([_vp, _i32], ctypes.c_int),
+    "ati_profile_read": ([_vp, _i32, _dp, _vp], ctypes.c_int),
+    "ati_launch_count": ([_vp, _vp], ctypes.c_int),
+    "ati_stream": ([_vp], ctypes.c_void_p),
+    "ati_probe_fma_tflops": ([_i32, _dp], ctypes.c_int),
+}
+
+KERNEL_CLASSES = ["deriv_xi", "deriv_eta", "deriv_zeta", "filter_xi", "filter_eta", "filter_zeta", "mpigo",
+                  "prim", "cfl", "grad", "stress", "flux", "div", "rk", "gcbc", "wall_junction", "average",
+                  "scalar", "copy"]
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load libati.so and bind every entry point; raise if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libati.so not built at {path}: run tandemproject_gb300.build.build() "
+                           "(there is no CPU fallback)")
+    L = ctypes.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _dp_of(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class AtiError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"status {code}: {msg}")
+        self.code = code
+
+
+class Case:
+    """One aerofoil case resident on the GPU (all blocks in one handle)."""
+
+    def __init__(self, cfg: CaseConfig, lib_path=LIB_PATH):
+        self.L = load_library(lib_path)
+        self.cfg = cfg
+        self._c = cfg.to_c()
+        h = ctypes.c_void_p()
+        rc = self.L.ati_create(ctypes.byref(self._c), ctypes.byref(h))
+        if rc:
+            raise AtiError(rc, self.L.ati_last_error(None).decode())
+        self.h = h
+        self.dims = []
+        for mb in range(cfg.nblocks):
+            d = (ctypes.c_int32 * 3)()
+            n = ctypes.c_int64()
+            self._chk(self.L.ati_block_dims(self.h, mb, d, ctypes.byref(n)))
+            self.dims.append((d[0], d[1], d[2], n.value))
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ati_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc:
+            raise AtiError(rc, self.L.ati_last_error(self.h).decode())
+        return rc
+
+    def npts(self, mb):
+        return self.dims[mb][3]
+
+    # -- set-up
+    def set_grid(self, mb, xyz):
+        a = np.ascontiguousarray(xyz, dtype=np.float64)
+        assert a.size == 3 * self.npts(mb)
+        self._chk(self.L.ati_set_grid(self.h, mb, _dp_of(a)))
+
+    def init(self):
+        self._chk(self.L.ati_init(self.h))
+
+    # -- copies
+    def get_field(self, mb, fid):
+        out = np.empty(NCOMP[fid] * self.npts(mb))
+        self._chk(self.L.ati_get_field(self.h, mb, fid, _dp_of(out)))
+        return out.reshape(NCOMP[fid], -1)
+
+    def set_field(self, mb, fid, v):
+        a = np.ascontiguousarray(v, dtype=np.float64).ravel()
+        assert a.size == NCOMP[fid] * self.npts(mb)
+        self._chk(self.L.ati_set_field(self.h, mb, fid, _dp_of(a)))
+
+    def get_state(self, mb, out=None):
+        if out is None:
+            out = np.empty(5 * self.npts(mb))
+        self._chk(self.L.ati_get_state(self.h, mb, _dp_of(out)))
+        return out.reshape(5, -1)
+
+    def set_state(self, mb, q):
+        a = np.ascontiguousarray(q, dtype=np.float64)
+        self._chk(self.L.ati_set_state(self.h, mb, _dp_of(a)))
+
+    def get_face(self, mb, which, nn):
+        lxi, let, lze, _ = self.dims[mb]
+        nbs = {1: (let + 1) * (lze + 1), 2: (lze + 1) * (lxi + 1), 3: (lxi + 1) * (let + 1)}[nn]
+        nc = 10 if which in (FACE_DRVA, FACE_DRVB) else 6
+        out = np.empty(nc * nbs)
+        self._chk(self.L.ati_get_face(self.h, mb, which, nn, _dp_of(out)))
+        return out.reshape(-1, nbs)
+
+    def get_time(self):
+        t = AtiTime()
+        self._chk(self.L.ati_get_time(self.h, ctypes.byref(t)))
+        return t.as_tuple()
+
+    def set_time(self, tup):
+        t = AtiTime(*tup)
+        self._chk(self.L.ati_set_time(self.h, ctypes.byref(t)))
+
+    # -- the reference's procedures
+    def mpigo(self, nt, nrt, n45):
+        self._chk(self.L.ati_mpigo(self.h, nt, nrt, n45))
+
+    def deriv(self, nn, nz, m):
+        self._chk(self.L.ati_deriv(self.h, nn, nz, m))
+
+    def filte(self, nn, nz):
+        self._chk(self.L.ati_filte(self.h, nn, nz))
+
+    def filter_step(self):
+        self._chk(self.L.ati_filter_step(self.h))
+
+    def rk_stage(self, nk):
+        self._chk(self.L.ati_rk_stage(self.h, nk))
+
+    def step(self, nsteps=1):
+        return self._chk(self.L.ati_step(self.h, nsteps))
+
+    def synchronize(self):
+        self._chk(self.L.ati_synchronize(self.h))
+
+    def profile(self, enable=True):
+        """Bracket every launch with CUDA events on the case's stream."""
+        self._chk(self.L.ati_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{kernel class: (milliseconds, launches)} since profiling was enabled."""
+        n = len(KERNEL_CLASSES)
+        ms = np.zeros(n)
+        cnt = (ctypes.c_int64 * n)()
+        self._chk(self.L.ati_profile_read(self.h, n, _dp_of(ms), cnt))
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(KERNEL_CLASSES)}
+
+    def launch_count(self):
+        v = ctypes.c_int64()
+        self._chk(self.L.ati_launch_count(self.h, ctypes.byref(v)))
+        return v.value
+
+    def stream(self):
+        """The case's cudaStream_t as an integer handle."""
+        return self.L.ati_stream(self.h)
+
+    def forces(self):
+        out = np.zeros(2)
+        self._chk(self.L.ati_forces(self.h, _dp_of(out)))
+        return out
+
+
+def probe_fma_tflops(fp64=True):
+    """Measured FMA throughput of this GPU (TFLOP/s)."""
+    L = load_library()
+    v = ctypes.c_double()
+    rc = L.ati_probe_fma_tflops(1 if fp64 else 0, ctypes.byref(v))
+    if rc:
+        raise AtiError(rc, "ati_probe_fma_tflops failed")
+    return v.value
+
+
+def setup_case(cfg: CaseConfig, grid=None, cls=Case):
+    """Create a case, upload the aerofoil grid and run the set-up."""
+    from .grid import aerofoil_grid
+    c = cls(cfg)
+    g = aerofoil_grid(cfg) if grid is None else grid
+    for mb in range(cfg.nblocks):
+        c.set_grid(mb, g[mb])
+    c.init()
+    return c
