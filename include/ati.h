@@ -217,6 +217,33 @@ void *ati_stream(ati_handle_t *h);
  * denominator of the FP64 path. */
 int ati_probe_fma_tflops(int fp64, double *tflops);
 
+/* ---- allocation-free derivative (no counterpart in the reference) -------
+ * For callers that must not allocate GPU memory when they call in: codes
+ * that give all device memory to their own pool at start-up, or time loops
+ * that may not allocate once running (an allocation can stall the whole
+ * device or fail late).  Computes the compact first derivative of nlines
+ * contiguous lines of len points each, in -> out (both caller-owned device
+ * arrays, line t at offset t*len), with the one-sided boundary rows at both
+ * ends -- the result ati_deriv gives along xi on blocks whose xi faces are
+ * boundaries or interfaces, bit for bit -- asynchronously on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream).
+ *  - Allocates and frees nothing.  Its scratch (LU factors and the
+ *    forward-elimination values) is one static device array of
+ *    5*ATI_NOALLOC_MAX_LEN + ATI_NOALLOC_MAX_POINTS doubles (about 16 MB),
+ *    reserved on every GPU that loads this library until the process exits.
+ *  - Rejects len outside 7..ATI_NOALLOC_MAX_LEN and nlines*len above
+ *    ATI_NOALLOC_MAX_POINTS with ATI_EINVAL (text in ati_last_error(NULL)).
+ *  - The first call on each device looks up the scratch array's device
+ *    address (cudaGetSymbolAddress) with that device current; make that
+ *    first call before any stream capture.
+ *  - All calls share the one scratch array and it keeps the previous call's
+ *    contents; every value a call reads was written by the same call, so
+ *    nothing needs clearing, but calls that overlap on the GPU (different
+ *    streams, no ordering between them) race on it and must not be issued. */
+#define ATI_NOALLOC_MAX_POINTS 2000000
+#define ATI_NOALLOC_MAX_LEN 4096
+int ati_deriv_lines_noalloc(const double *in, double *out, int64_t nlines, int32_t len, void *stream);
+
 /* Lift and drag of the wall blocks as clpost computes them
  * (src/rpt.f90:1017-1056), from the p and stresses of the last stage:
  * out[0] = force coefficient along x, out[1] = along y. */

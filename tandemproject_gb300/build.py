@@ -27,6 +27,7 @@ SOURCES = [
     ("ati_api.cu", "ati_api.o", ["-fmad=false"]),
     ("ati_scheme.cpp", "ati_scheme.o", []),
     ("ati_probe.cu", "ati_probe.o", []),
+    ("ati_noalloc.cu", "ati_noalloc.o", ["-fmad=false"]),
 ]
 
 

@@ -109,6 +109,9 @@ static void prof_drain(ati_handle *h) {
     prof_end(h);              \
   } while (0)
 
+// error text for calls that have no handle (ati_last_error(NULL))
+void ati_set_thread_error(const char *msg) { g_create_err = msg ? msg : ""; }
+
 static int fail(ati_handle *h, int code, const std::string &msg) {
   if (h) h->err = msg;
   else g_create_err = msg;

@@ -60,6 +60,7 @@ SIGNATURES = {
     "ati_launch_count": ([_vp, _vp], ctypes.c_int),
     "ati_stream": ([_vp], ctypes.c_void_p),
     "ati_probe_fma_tflops": ([_i32, _dp], ctypes.c_int),
+    "ati_deriv_lines_noalloc": ([_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp], ctypes.c_int),
 }
 
 KERNEL_CLASSES = ["deriv_xi", "deriv_eta", "deriv_zeta", "filter_xi", "filter_eta", "filter_zeta", "mpigo",
