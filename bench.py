@@ -42,8 +42,10 @@ L2_BYTES = 129 * 2 ** 20
 # one output plane written; flops of the 7-point RHS + forward + backward pass)
 SWEEP_BYTES = {"deriv": 16, "filter": 16}
 SWEEP_FLOPS = {"deriv": 17, "filter": 22}
-# canonical FP64 bytes per grid-point-stage of the whole stage (141 words)
+# canonical bytes per grid-point-stage of the whole stage: 141 FP64 words, or
+# the mixed data flow with FP32 intermediates and FP64 state/metrics
 STAGE_BYTES_FP64 = 1128
+STAGE_BYTES_MIXED = 728
 
 
 def dist_env():
@@ -173,6 +175,7 @@ def main():
     ap.add_argument("--preset", default="naca0012_8p8m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-mixed", dest="mixed", action="store_false")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -233,6 +236,51 @@ def main():
         t_dev = float(tt.item())
     value = npts * cfg.nkrk * args.steps * ws / t_dev
 
+    # the mixed-precision path on the same workload, from the same start
+    from tandemproject_gb300.config import MIXED
+    mixed = None
+    if args.mixed:
+        cm = Case(cfg.replace(precision=MIXED))
+        for mb in range(cfg.nblocks):
+            cm.set_grid(mb, grid[mb])
+        cm.init()
+        cm.step(args.warmup)
+        barrier()
+        sm = torch.cuda.ExternalStream(cm.stream())
+        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        m0.record(sm)
+        cm.step(args.steps)
+        m1.record(sm)
+        barrier()
+        t_mix = m0.elapsed_time(m1) / 1e3
+        if dist is not None:
+            tt = torch.tensor([t_mix], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t_mix = float(tt.item())
+        num = np.zeros(5)
+        den = np.zeros(5)
+        for mb in range(cfg.nblocks):
+            qd, qm = case.get_state(mb), cm.get_state(mb)
+            num += np.sum((qm - qd) ** 2, axis=1)
+            den += np.sum(qd ** 2, axis=1)
+        den[1:4] = den[1:4].sum()
+        cm.profile(True)
+        cm.step(2)
+        mprof = cm.profile_read()
+        cm.profile(False)
+        cm.close()
+        mtot = sum(v[0] for v in mprof.values())
+        mixed = {"value": npts * cfg.nkrk * args.steps * ws / t_mix, "ms_per_step": t_mix / args.steps * 1e3,
+                 "dtype": "f32 line solves/filters/fluxes, f64 metrics, Jacobian and RK state",
+                 "speedup_vs_fp64": (npts * cfg.nkrk * args.steps * ws / t_mix) / value,
+                 "rel_l2_vs_fp64_after_steps": {"steps": args.warmup + args.steps,
+                                                "rho": float(np.sqrt(num[0] / den[0])),
+                                                "momentum": float(np.sqrt(num[1:4].sum() / den[1])),
+                                                "rhoE": float(np.sqrt(num[4] / den[4]))},
+                 "stage_hbm_frac_728B": STAGE_BYTES_MIXED * (npts * cfg.nkrk * args.steps / t_mix) / 1e9
+                 / measured_peaks()[0],
+                 "kernel_share": {k: round(v[0] / mtot, 4) for k, v in mprof.items() if v[1]}}
+
     # end to end through the C ABI: pinned host state in, step, state out
     host = [torch.empty(5 * case.npts(mb), dtype=torch.float64, pin_memory=True) for mb in range(cfg.nblocks)]
     hnp = [h.numpy() for h in host]
@@ -290,6 +338,8 @@ def main():
                        "points": npts, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "l2": "no flush: the state alone (5 x 8 B x points) exceeds the 129 MB L2"},
             "e2e": e2e, "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches}
+    if mixed is not None:
+        line["mixed"] = mixed
     case.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cfg, grid)

@@ -195,17 +195,16 @@ int ati_step(ati_handle_t *h, int nsteps);
 #define ATI_K_MPIGO 6
 #define ATI_K_PRIM 7
 #define ATI_K_CFL 8
-#define ATI_K_GRAD 9
-#define ATI_K_STRESS 10
-#define ATI_K_FLUX 11
-#define ATI_K_DIV 12
-#define ATI_K_RK 13
-#define ATI_K_GCBC 14
-#define ATI_K_WALL_JUNCTION 15
-#define ATI_K_AVERAGE 16
-#define ATI_K_SCALAR 17
-#define ATI_K_COPY 18
-#define ATI_K_NSLOTS 19
+#define ATI_K_VISC 9
+#define ATI_K_FLUX 10
+#define ATI_K_DIV 11
+#define ATI_K_RK 12
+#define ATI_K_GCBC 13
+#define ATI_K_WALL_JUNCTION 14
+#define ATI_K_AVERAGE 15
+#define ATI_K_SCALAR 16
+#define ATI_K_NSLOTS 17
+/* Profiling replaces the CUDA-graph replay of ati_step by eager launches. */
 int ati_profile_enable(ati_handle_t *h, int enable);
 int ati_profile_read(ati_handle_t *h, int nslots, double *ms, int64_t *launches);
 int ati_launch_count(ati_handle_t *h, int64_t *count);

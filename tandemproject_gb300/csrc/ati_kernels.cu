@@ -1,9 +1,11 @@
-// ati_kernels.cu — sm_103a kernels of the ATI3D per-RK-stage hot path (FP64).
+// ati_kernels.cu — sm_103a kernels of the ATI3D per-RK-stage hot path.
 //
 // Each kernel restates one loop nest of the reference (cited per kernel) over
-// all blocks of the case at once.  This file is compiled twice: into
-// namespace ati::fast with FMA contraction (the fused time step) and into
-// ati::strict with -fmad=false, where every operation rounds as the
+// all blocks of the case at once.  The kernels are templated on the type of
+// the stage intermediates (double: the FP64 path, float: the mixed path; the
+// state qa/qo stays double) and keep the reference's operation order.  This
+// file is compiled twice: into namespace ati::fast with FMA contraction and
+// into ati::strict with -fmad=false, where every operation rounds as the
 // reference's Fortran expressions do (set-up and the granular calls, which
 // then agree with the CPU restatement bit for bit).
 #include <cuda_runtime.h>
@@ -35,17 +37,171 @@ __device__ __forceinline__ void ijk_of(const BlockDev &B, int nn, int &i1, int &
 }
 
 // ---------------------------------------------------------------------------
-// Compact derivative / filter line sweeps: deriv (src/Subroutines3D.f90:84-141)
-// and filte (src/Subroutines3D.f90:145-206).
-//
-// One thread owns one line.  For eta and zeta lines consecutive threads own
-// consecutive xi positions, so every load and store of a warp is one
-// contiguous 256-byte row; xi lines are contiguous per thread and are served
-// from L1.  The six boundary right-hand sides are built first from the
-// original values, so the sweep may run in place (deriv(1,1,m), filte).
-// Forward-elimination values go to the scratch plane fw at the same point
-// index; the back substitution reads them back.
+// Compact derivative / filter of one line: deriv (src/Subroutines3D.f90:84-141)
+// and filte (src/Subroutines3D.f90:145-206).  ld(i) gives the original value at
+// position i, fw holds the forward-elimination values, put(i, v) receives the
+// derivative (or the filter correction) at i.  The six boundary rows and the
+// first window are read before anything is stored, so fw may alias the input
+// (in-place solve in shared memory).
 // ---------------------------------------------------------------------------
+template <bool FILT, typename TC, class Src>
+__device__ __forceinline__ void line_ends(const Coef<TC> &C, int L, int ns, int ne, const TC *rcv, int64_t nbs, int jk,
+                                          const Src &ld, TC &sbs0, TC &sbs1, TC &sbs2, TC &sbe0, TC &sbe1,
+                                          TC &sbe2) {
+  const TC two = (TC)2;
+  if (!FILT) {
+    const TC aa = C.aa, ab = C.ab, ac = C.ac;
+    if (ns == 0) {
+      const TC w0 = ld(0), w1 = ld(1), w2 = ld(2), w3 = ld(3), w4 = ld(4), w5 = ld(5), w6 = ld(6);
+      const TC *a = C.abc[0];
+      sbs0 = a[0] * (w1 - w0) + a[1] * (w2 - w0) + a[2] * (w3 - w0) + a[3] * (w4 - w0) + a[4] * (w5 - w0) + a[5] * (w6 - w0);
+      a = C.abc[1];
+      sbs1 = a[0] * (w0 - w1) + a[1] * (w2 - w1) + a[2] * (w3 - w1) + a[3] * (w4 - w1) + a[4] * (w5 - w1) + a[5] * (w6 - w1);
+      a = C.abc[2];
+      sbs2 = a[0] * (w0 - w2) + a[1] * (w1 - w2) + a[2] * (w3 - w2) + a[3] * (w4 - w2) + a[4] * (w5 - w2) + a[5] * (w6 - w2);
+    } else {
+      TC s0 = 0, s1 = 0;
+#pragma unroll
+      for (int q = 0; q <= LMD; q++) {
+        const TC v = ld(q);
+        s0 += C.pbci[0][0][q] * v;
+        s1 += C.pbci[0][1][q] * v;
+      }
+      sbs0 = s0 + rcv[jk + nbs * 0];
+      sbs1 = s1 + rcv[jk + nbs * 1];
+      sbs2 = aa * (ld(3) - ld(1)) + ab * (ld(4) - ld(0)) + ac * (ld(5) - rcv[jk + nbs * 2]);
+    }
+    if (ne == 0) {
+      const TC w0 = ld(L - 1), w1 = ld(L - 2), w2 = ld(L - 3), w3 = ld(L - 4), w4 = ld(L - 5), w5 = ld(L - 6),
+               w6 = ld(L - 7);
+      const TC *a = C.abc[0];
+      sbe0 = a[0] * (w0 - w1) + a[1] * (w0 - w2) + a[2] * (w0 - w3) + a[3] * (w0 - w4) + a[4] * (w0 - w5) + a[5] * (w0 - w6);
+      a = C.abc[1];
+      sbe1 = a[0] * (w1 - w0) + a[1] * (w1 - w2) + a[2] * (w1 - w3) + a[3] * (w1 - w4) + a[4] * (w1 - w5) + a[5] * (w1 - w6);
+      a = C.abc[2];
+      sbe2 = a[0] * (w2 - w0) + a[1] * (w2 - w1) + a[2] * (w2 - w3) + a[3] * (w2 - w4) + a[4] * (w2 - w5) + a[5] * (w2 - w6);
+    } else {
+      TC s0 = 0, s1 = 0;
+#pragma unroll
+      for (int q = 0; q <= LMD; q++) {
+        const TC v = ld(L - 1 - q);
+        s0 += C.pbci[0][0][q] * v;
+        s1 += C.pbci[0][1][q] * v;
+      }
+      sbe0 = -s0 - rcv[jk + nbs * 3];
+      sbe1 = -s1 - rcv[jk + nbs * 4];
+      sbe2 = aa * (ld(L - 2) - ld(L - 4)) + ab * (ld(L - 1) - ld(L - 5)) + ac * (rcv[jk + nbs * 5] - ld(L - 6));
+    }
+  } else {
+    const TC fa = C.fa, fb = C.fb, fc = C.fc;
+    if (ns == 0) {
+      const TC w0 = ld(0), w1 = ld(1), w2 = ld(2), w3 = ld(3), w4 = ld(4), w5 = ld(5);
+      const TC ra0 = two * w0, ra1 = two * w1, ra2 = two * w2;
+      const TC res = C.fex[1] * (w1 - w0) + C.fex[2] * (w2 - w0) + C.fex[3] * (w3 - w0);
+      const TC rv1 = w0 - res * C.ffx[1], rv2 = w0 - res * C.ffx[2], rv3 = w0 - res * C.ffx[3];
+      sbs0 = C.fam[0] * (rv1 + w1 - ra0) + C.fbm[0] * (rv2 + w2 - ra0) + C.fcm[0] * (rv3 + w3 - ra0);
+      sbs1 = C.fam[1] * (w0 + w2 - ra1) + C.fbm[1] * (rv1 + w3 - ra1) + C.fcm[1] * (rv2 + w4 - ra1);
+      sbs2 = C.fam[2] * (w1 + w3 - ra2) + C.fbm[2] * (w0 + w4 - ra2) + C.fcm[2] * (rv1 + w5 - ra2);
+    } else {
+      TC s0 = 0, s1 = 0;
+#pragma unroll
+      for (int q = 0; q <= LMF; q++) {
+        const TC v = ld(q);
+        s0 += C.pbci[1][0][q] * v;
+        s1 += C.pbci[1][1][q] * v;
+      }
+      const TC ra2 = two * ld(2);
+      sbs0 = s0 + rcv[jk + nbs * 0];
+      sbs1 = s1 + rcv[jk + nbs * 1];
+      sbs2 = fa * (ld(1) + ld(3) - ra2) + fb * (ld(0) + ld(4) - ra2) + fc * (rcv[jk + nbs * 2] + ld(5) - ra2);
+    }
+    if (ne == 0) {
+      const TC w0 = ld(L - 1), w1 = ld(L - 2), w2 = ld(L - 3), w3 = ld(L - 4), w4 = ld(L - 5), w5 = ld(L - 6);
+      const TC ra0 = two * w0, ra1 = two * w1, ra2 = two * w2;
+      const TC res = C.fex[1] * (w0 - w1) + C.fex[2] * (w0 - w2) + C.fex[3] * (w0 - w3);
+      const TC rv1 = w0 + res * C.ffx[1], rv2 = w0 + res * C.ffx[2], rv3 = w0 + res * C.ffx[3];
+      sbe0 = C.fam[0] * (w1 + rv1 - ra0) + C.fbm[0] * (w2 + rv2 - ra0) + C.fcm[0] * (w3 + rv3 - ra0);
+      sbe1 = C.fam[1] * (w2 + w0 - ra1) + C.fbm[1] * (w3 + rv1 - ra1) + C.fcm[1] * (w4 + rv2 - ra1);
+      sbe2 = C.fam[2] * (w3 + w1 - ra2) + C.fbm[2] * (w4 + w0 - ra2) + C.fcm[2] * (w5 + rv1 - ra2);
+    } else {
+      TC s0 = 0, s1 = 0;
+#pragma unroll
+      for (int q = 0; q <= LMF; q++) {
+        const TC v = ld(L - 1 - q);
+        s0 += C.pbci[1][0][q] * v;
+        s1 += C.pbci[1][1][q] * v;
+      }
+      const TC ra2 = two * ld(L - 3);
+      sbe0 = s0 + rcv[jk + nbs * 3];
+      sbe1 = s1 + rcv[jk + nbs * 4];
+      sbe2 = fa * (ld(L - 4) + ld(L - 2) - ra2) + fb * (ld(L - 5) + ld(L - 1) - ra2) +
+             fc * (ld(L - 6) + rcv[jk + nbs * 5] - ra2);
+    }
+  }
+}
+
+// right-hand side of interior row i from the window a0..a6 = ld(i-3..i+3)
+template <bool FILT, typename TC>
+__device__ __forceinline__ TC interior_rhs(const Coef<TC> &C, TC a0, TC a1, TC a2, TC a3, TC a4, TC a5, TC a6) {
+  if (!FILT) return C.aa * (a4 - a2) + C.ab * (a5 - a1) + C.ac * (a6 - a0);
+  const TC res = (TC)2 * a3;
+  return C.fa * (a2 + a4 - res) + C.fb * (a1 + a5 - res) + C.fc * (a0 + a6 - res);
+}
+
+template <bool FILT, typename TC, class Src, class Fw, class Sink>
+__device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int L, int ns, int ne, const TC *rcv,
+                                           int64_t nbs, int jk, const Src &ld, Fw &fw, Sink &put, TC &first,
+                                           TC &last) {
+  TC sbs0, sbs1, sbs2, sbe0, sbe1, sbe2;
+  line_ends<FILT, TC>(C, L, ns, ne, rcv, nbs, jk, ld, sbs0, sbs1, sbs2, sbe0, sbe1, sbe2);
+  // the first window is read before any forward value is stored
+  TC a0 = ld(0), a1 = ld(1), a2 = ld(2), a3 = ld(3), a4 = ld(4), a5 = ld(5);
+  // forward elimination (src/Subroutines3D.f90:124-128 / 190-194)
+  TC f2 = sbs0;
+  TC f1 = sbs1 - fac[1 * 5 + 1] * f2;
+  fw.st(0, f2);
+  fw.st(1, f1);
+  {
+    const TC v = sbs2 - fac[2 * 5 + 0] * f2 - fac[2 * 5 + 1] * f1;
+    fw.st(2, v);
+    f2 = f1; f1 = v;
+  }
+  for (int i = 3; i <= L - 4; i++) {
+    const TC a6 = ld(i + 3);
+    const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
+    const TC v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    fw.st(i, v);
+    f2 = f1; f1 = v;
+    a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
+  }
+  {
+    int i = L - 3;
+    TC v = sbe2 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    fw.st(i, v);
+    f2 = f1; f1 = v;
+    i = L - 2;
+    v = sbe1 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    fw.st(i, v);
+    f2 = f1; f1 = v;
+    i = L - 1;
+    v = sbe0 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    f2 = f1; f1 = v;  // f1 = fw(L-1), f2 = fw(L-2)
+  }
+  // back substitution (src/Subroutines3D.f90:129-136 / 195-202)
+  TC b0 = fac[(L - 1) * 5 + 2] * f1;
+  TC b1 = fac[(L - 2) * 5 + 2] * f2 - fac[(L - 2) * 5 + 3] * b0;
+  last = b0;
+  put(L - 1, b0);
+  put(L - 2, b1);
+  for (int i = L - 3; i >= 0; i--) {
+    const TC v = fac[i * 5 + 2] * fw.ld(i) - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
+    put(i, v);
+    b0 = b1; b1 = v;
+  }
+  first = b1;
+}
+
+// line geometry of direction NN: base point, stride, face index, length
 template <int NN>
 __device__ __forceinline__ bool line_geom(const BlockDev &B, int t, int64_t &base, int64_t &stride, int &jk, int &L) {
   const int nx = B.lxi + 1, ny = B.let + 1, nz = B.lze + 1;
@@ -63,259 +219,301 @@ __device__ __forceinline__ bool line_geom(const BlockDev &B, int t, int64_t &bas
   return true;
 }
 
-template <int NN, bool FILT>
-__global__ void __launch_bounds__(128) k_sweep(Ctx c, const double *in, double *out, int m) {
-  const BlockDev &B = c.blk[blockIdx.y];
+template <typename TI, typename TC>
+struct GlobalSrc {
+  const TI *p;
+  int64_t s;
+  __device__ __forceinline__ TC operator()(int i) const { return (TC)p[(int64_t)i * s]; }
+};
+template <typename TC>
+struct GlobalFw {
+  TC *p;
+  int64_t s;
+  __device__ __forceinline__ void st(int i, TC v) { p[(int64_t)i * s] = v; }
+  __device__ __forceinline__ TC ld(int i) const { return p[(int64_t)i * s]; }
+};
+template <bool FILT, typename TI, typename TO, typename TC>
+struct GlobalSink {
+  const TI *in;
+  TO *out, *out2;
+  int64_t s;
+  __device__ __forceinline__ void operator()(int i, TC v) {
+    const int64_t o = (int64_t)i * s;
+    TO r;
+    if (FILT) r = (TO)(in[o] + (TI)v);  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+    else r = (TO)v;
+    out[o] = r;
+    if (out2) out2[o] = r;
+  }
+};
+
+template <typename TI, typename TO, typename TC>
+struct SweepArgs {
+  const BlockDev *blk;
+  const Coef<TC> *cf;
+  const TC *fac;
+  SweepIO<TI, TO> io;
+  TC *fw;
+  int64_t fw_fs;
+  const TC *recv;
+  int64_t recv_fs;
+  TC *drva;
+};
+
+// eta and zeta lines: one thread per line; consecutive threads own consecutive xi positions, so each
+// warp access of an eta or zeta sweep is one contiguous row
+template <int NN, bool FILT, typename TI, typename TO, typename TC>
+__global__ void __launch_bounds__(128) k_sweep_g(SweepArgs<TI, TO, TC> a) {
+  const BlockDev &B = a.blk[blockIdx.y];
+  const int f = blockIdx.z;
   int64_t base, stride;
   int jk, L;
   if (!line_geom<NN>(B, blockIdx.x * blockDim.x + threadIdx.x, base, stride, jk, L)) return;
-  const Scheme &S = *c.sc;
+  const Coef<TC> &C = *a.cf;
   const int ns = B.ndf[0][NN], ne = B.ndf[1][NN];
   const int64_t nbs = B.nbsize[NN];
-  const double *recv = c.recv + B.face_off[NN] * 6;
-  const double *fac = (FILT ? c.facf : c.facd) + B.fac_off[NN] * 5;
-  const double *pin = in + base;
-  double *fw = c.fw + base;
-#define LD(i) pin[(int64_t)(i) * stride]
-  double sbs0, sbs1, sbs2, sbe0, sbe1, sbe2;
-  if (!FILT) {
-    const double aa = S.aa, ab = S.ab, ac = S.ac;
-    if (ns == 0) {
-      const double w0 = LD(0), w1 = LD(1), w2 = LD(2), w3 = LD(3), w4 = LD(4), w5 = LD(5), w6 = LD(6);
-      const double *a = S.abc[0];
-      sbs0 = a[0] * (w1 - w0) + a[1] * (w2 - w0) + a[2] * (w3 - w0) + a[3] * (w4 - w0) + a[4] * (w5 - w0) + a[5] * (w6 - w0);
-      a = S.abc[1];
-      sbs1 = a[0] * (w0 - w1) + a[1] * (w2 - w1) + a[2] * (w3 - w1) + a[3] * (w4 - w1) + a[4] * (w5 - w1) + a[5] * (w6 - w1);
-      a = S.abc[2];
-      sbs2 = a[0] * (w0 - w2) + a[1] * (w1 - w2) + a[2] * (w3 - w2) + a[3] * (w4 - w2) + a[4] * (w5 - w2) + a[5] * (w6 - w2);
-    } else {
-      double s0 = 0, s1 = 0;
-#pragma unroll
-      for (int q = 0; q <= LMD; q++) {
-        const double v = LD(q);
-        s0 += S.pbci[0][0][q] * v;
-        s1 += S.pbci[0][1][q] * v;
-      }
-      sbs0 = s0 + recv[jk + nbs * 0];
-      sbs1 = s1 + recv[jk + nbs * 1];
-      sbs2 = aa * (LD(3) - LD(1)) + ab * (LD(4) - LD(0)) + ac * (LD(5) - recv[jk + nbs * 2]);
-    }
-    if (ne == 0) {
-      const double w0 = LD(L - 1), w1 = LD(L - 2), w2 = LD(L - 3), w3 = LD(L - 4), w4 = LD(L - 5), w5 = LD(L - 6),
-                   w6 = LD(L - 7);
-      const double *a = S.abc[0];
-      sbe0 = a[0] * (w0 - w1) + a[1] * (w0 - w2) + a[2] * (w0 - w3) + a[3] * (w0 - w4) + a[4] * (w0 - w5) + a[5] * (w0 - w6);
-      a = S.abc[1];
-      sbe1 = a[0] * (w1 - w0) + a[1] * (w1 - w2) + a[2] * (w1 - w3) + a[3] * (w1 - w4) + a[4] * (w1 - w5) + a[5] * (w1 - w6);
-      a = S.abc[2];
-      sbe2 = a[0] * (w2 - w0) + a[1] * (w2 - w1) + a[2] * (w2 - w3) + a[3] * (w2 - w4) + a[4] * (w2 - w5) + a[5] * (w2 - w6);
-    } else {
-      double s0 = 0, s1 = 0;
-#pragma unroll
-      for (int q = 0; q <= LMD; q++) {
-        const double v = LD(L - 1 - q);
-        s0 += S.pbci[0][0][q] * v;
-        s1 += S.pbci[0][1][q] * v;
-      }
-      sbe0 = -s0 - recv[jk + nbs * 3];
-      sbe1 = -s1 - recv[jk + nbs * 4];
-      sbe2 = aa * (LD(L - 2) - LD(L - 4)) + ab * (LD(L - 1) - LD(L - 5)) + ac * (recv[jk + nbs * 5] - LD(L - 6));
-    }
-  } else {
-    const double fa = S.fa, fb = S.fb, fc = S.fc;
-    if (ns == 0) {
-      const double w0 = LD(0), w1 = LD(1), w2 = LD(2), w3 = LD(3), w4 = LD(4), w5 = LD(5);
-      const double ra0 = 2.0 * w0, ra1 = 2.0 * w1, ra2 = 2.0 * w2;
-      const double res = S.fex[1] * (w1 - w0) + S.fex[2] * (w2 - w0) + S.fex[3] * (w3 - w0);
-      const double rv1 = w0 - res * S.ffx[1], rv2 = w0 - res * S.ffx[2], rv3 = w0 - res * S.ffx[3];
-      sbs0 = S.fam[0] * (rv1 + w1 - ra0) + S.fbm[0] * (rv2 + w2 - ra0) + S.fcm[0] * (rv3 + w3 - ra0);
-      sbs1 = S.fam[1] * (w0 + w2 - ra1) + S.fbm[1] * (rv1 + w3 - ra1) + S.fcm[1] * (rv2 + w4 - ra1);
-      sbs2 = S.fam[2] * (w1 + w3 - ra2) + S.fbm[2] * (w0 + w4 - ra2) + S.fcm[2] * (rv1 + w5 - ra2);
-    } else {
-      double s0 = 0, s1 = 0;
-#pragma unroll
-      for (int q = 0; q <= LMF; q++) {
-        const double v = LD(q);
-        s0 += S.pbci[1][0][q] * v;
-        s1 += S.pbci[1][1][q] * v;
-      }
-      const double ra2 = 2.0 * LD(2);
-      sbs0 = s0 + recv[jk + nbs * 0];
-      sbs1 = s1 + recv[jk + nbs * 1];
-      sbs2 = fa * (LD(1) + LD(3) - ra2) + fb * (LD(0) + LD(4) - ra2) + fc * (recv[jk + nbs * 2] + LD(5) - ra2);
-    }
-    if (ne == 0) {
-      const double w0 = LD(L - 1), w1 = LD(L - 2), w2 = LD(L - 3), w3 = LD(L - 4), w4 = LD(L - 5), w5 = LD(L - 6);
-      const double ra0 = 2.0 * w0, ra1 = 2.0 * w1, ra2 = 2.0 * w2;
-      const double res = S.fex[1] * (w0 - w1) + S.fex[2] * (w0 - w2) + S.fex[3] * (w0 - w3);
-      const double rv1 = w0 + res * S.ffx[1], rv2 = w0 + res * S.ffx[2], rv3 = w0 + res * S.ffx[3];
-      sbe0 = S.fam[0] * (w1 + rv1 - ra0) + S.fbm[0] * (w2 + rv2 - ra0) + S.fcm[0] * (w3 + rv3 - ra0);
-      sbe1 = S.fam[1] * (w2 + w0 - ra1) + S.fbm[1] * (w3 + rv1 - ra1) + S.fcm[1] * (w4 + rv2 - ra1);
-      sbe2 = S.fam[2] * (w3 + w1 - ra2) + S.fbm[2] * (w4 + w0 - ra2) + S.fcm[2] * (w5 + rv1 - ra2);
-    } else {
-      double s0 = 0, s1 = 0;
-#pragma unroll
-      for (int q = 0; q <= LMF; q++) {
-        const double v = LD(L - 1 - q);
-        s0 += S.pbci[1][0][q] * v;
-        s1 += S.pbci[1][1][q] * v;
-      }
-      const double ra2 = 2.0 * LD(L - 3);
-      sbe0 = s0 + recv[jk + nbs * 3];
-      sbe1 = s1 + recv[jk + nbs * 4];
-      sbe2 = fa * (LD(L - 4) + LD(L - 2) - ra2) + fb * (LD(L - 5) + LD(L - 1) - ra2) +
-             fc * (LD(L - 6) + recv[jk + nbs * 5] - ra2);
-    }
+  const TC *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
+  const TC *fac = a.fac + B.fac_off[NN] * 5;
+  const TI *pin = a.io.in + f * a.io.in_fs + base;
+  GlobalSrc<TI, TC> ld{pin, stride};
+  GlobalFw<TC> fw{a.fw + f * a.fw_fs + base, stride};
+  TO *o2 = a.io.out2 ? a.io.out2 + f * a.io.out_fs + base : nullptr;
+  GlobalSink<FILT, TI, TO, TC> put{pin, a.io.out + f * a.io.out_fs + base, o2, stride};
+  TC first, last;
+  solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
+  if (!FILT && a.io.drva) {
+    TC *d = a.drva + B.face_off[NN] * 10;
+    const int m = a.io.m0 + f;
+    d[jk + nbs * ((m - 1) + 5 * 0)] = first;  // drva(jk,m,0) = sb(is)
+    d[jk + nbs * ((m - 1) + 5 * 1)] = last;   // drva(jk,m,1) = sb(ie)
   }
-  // forward elimination (src/Subroutines3D.f90:124-128 / 190-194)
-  double f2 = sbs0;
-  double f1 = sbs1 - fac[1 * 5 + 1] * f2;
-  fw[0] = f2;
-  fw[stride] = f1;
-  {
-    const double v = sbs2 - fac[2 * 5 + 0] * f2 - fac[2 * 5 + 1] * f1;
-    fw[2 * stride] = v;
+}
+
+// xi lines, chunked through shared memory.  A CTA owns XC_NL consecutive xi
+// lines of one block and one field (one thread per line) and streams them in
+// chunks of XC_C points: each chunk is loaded with coalesced reads into a
+// transposed tile [point][line], every thread advances its own recurrence
+// through the chunk, and the tile goes back to global memory coalesced.  The
+// forward pass writes fw(i) at position i+3 of the scratch plane (the point
+// whose load completed row i); the backward pass reads those chunks in reverse
+// and writes the result of row i at position i.  The six boundary rows use
+// direct loads of the line ends, and the last three forward values stay in
+// registers.  The tile is small (XC_C x XC_NL words), so many CTAs share an SM.
+constexpr int XC_NL = 64;
+constexpr int XC_C = 32;
+
+template <bool FILT, typename TI, typename TO, typename TC>
+__global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
+  __shared__ TC tile[XC_C][XC_NL + 1];
+  const BlockDev &B = a.blk[blockIdx.y];
+  const int f = blockIdx.z;
+  const int L = B.lxi + 1, nline = (B.let + 1) * (B.lze + 1);
+  const int t0 = blockIdx.x * XC_NL;
+  if (t0 >= nline) return;  // uniform over the CTA
+  const int nl = min(XC_NL, nline - t0);
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  constexpr int NW = XC_NL / 32;
+  const bool act = t < nl;
+  const int64_t off = B.off + (int64_t)t0 * L;
+  const TI *in = a.io.in + f * a.io.in_fs + off;
+  TC *fwg = a.fw + f * a.fw_fs + off;
+  TO *out = a.io.out + f * a.io.out_fs + off;
+  TO *out2 = a.io.out2 ? a.io.out2 + f * a.io.out_fs + off : nullptr;
+  const Coef<TC> &C = *a.cf;
+  const TC *fac = a.fac + B.fac_off[1] * 5;
+  const int jk = t0 + t;
+  const int64_t nbs = B.nbsize[1];
+
+  // boundary rows and the first window from the line itself
+  TC sbs0 = 0, sbs1 = 0, sbs2 = 0, sbe0 = 0, sbe1 = 0, sbe2 = 0;
+  TC a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, f1 = 0, f2 = 0, w0 = 0, w1 = 0, w2 = 0;
+  if (act) {
+    const TC *rcv = a.recv + f * a.recv_fs + B.face_off[1] * 6;
+    GlobalSrc<TI, TC> ld{in + (int64_t)t * L, 1};
+    line_ends<FILT, TC>(C, L, B.ndf[0][1], B.ndf[1][1], rcv, nbs, jk, ld, sbs0, sbs1, sbs2, sbe0, sbe1, sbe2);
+    a0 = ld(0); a1 = ld(1); a2 = ld(2); a3 = ld(3); a4 = ld(4); a5 = ld(5);
+    f2 = sbs0;
+    f1 = sbs1 - fac[1 * 5 + 1] * f2;
+    w0 = f2; w1 = f1;
+    const TC v = sbs2 - fac[2 * 5 + 0] * f2 - fac[2 * 5 + 1] * f1;
+    w2 = v;
     f2 = f1; f1 = v;
   }
-  {
-    double a0 = LD(0), a1 = LD(1), a2 = LD(2), a3 = LD(3), a4 = LD(4), a5 = LD(5);
-    if (!FILT) {
-      const double aa = S.aa, ab = S.ab, ac = S.ac;
-      for (int i = 3; i <= L - 4; i++) {
-        const double a6 = LD(i + 3);
-        const double sb = aa * (a4 - a2) + ab * (a5 - a1) + ac * (a6 - a0);
-        const double v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
-        fw[(int64_t)i * stride] = v;
-        f2 = f1; f1 = v;
-        a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
+  // forward elimination, chunk by chunk
+  for (int c0 = 0; c0 < L; c0 += XC_C) {
+    const int cl = min(XC_C, L - c0);
+    __syncthreads();
+    if (lane < cl)
+      for (int ln = warp; ln < nl; ln += NW) tile[lane][ln] = (TC)in[(int64_t)ln * L + c0 + lane];
+    __syncthreads();
+    if (act) {
+      int s0 = 0;
+      if (c0 == 0) {  // fw(0..2) go to positions 3..5
+        tile[3][t] = w0; tile[4][t] = w1; tile[5][t] = w2;
+        s0 = 6;
       }
-    } else {
-      const double fa = S.fa, fb = S.fb, fc = S.fc;
-      for (int i = 3; i <= L - 4; i++) {
-        const double a6 = LD(i + 3);
-        const double res = 2.0 * a3;
-        const double sb = fa * (a2 + a4 - res) + fb * (a1 + a5 - res) + fc * (a0 + a6 - res);
-        const double v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
-        fw[(int64_t)i * stride] = v;
+      for (int s = s0; s < cl; s++) {
+        const int i = c0 + s - 3;
+        const TC a6 = tile[s][t];
+        const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
+        const TC v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+        tile[s][t] = v;
         f2 = f1; f1 = v;
         a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
       }
     }
+    __syncthreads();
+    if (lane < cl)
+      for (int ln = warp; ln < nl; ln += NW) fwg[(int64_t)ln * L + c0 + lane] = tile[lane][ln];
   }
-  {
+  // the last three rows and the first three results, in registers
+  TC b0 = 0, b1 = 0;
+  if (act) {
     int i = L - 3;
-    double v = sbe2 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
-    fw[(int64_t)i * stride] = v;
+    TC v = sbe2 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    const TC fwl3 = v;
     f2 = f1; f1 = v;
     i = L - 2;
     v = sbe1 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
-    fw[(int64_t)i * stride] = v;
     f2 = f1; f1 = v;
     i = L - 1;
     v = sbe0 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
-    f2 = f1; f1 = v;  // f1 = fw(L-1), f2 = fw(L-2)
+    f2 = f1; f1 = v;
+    b0 = fac[(L - 1) * 5 + 2] * f1;
+    b1 = fac[(L - 2) * 5 + 2] * f2 - fac[(L - 2) * 5 + 3] * b0;
+    const TC r3 = fac[(L - 3) * 5 + 2] * fwl3 - fac[(L - 3) * 5 + 3] * b1 - fac[(L - 3) * 5 + 4] * b0;
+    if (!FILT && a.io.drva) {
+      TC *d = a.drva + B.face_off[1] * 10;
+      d[jk + nbs * ((a.io.m0 + f - 1) + 5 * 1)] = b0;  // drva(jk,m,1) = sb(ie)
+    }
+    const int64_t o = (int64_t)t * L;
+    const TC rv[3] = {r3, b1, b0};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const int64_t p = o + L - 3 + q;
+      TO r;
+      if (FILT) r = (TO)(in[p] + (TI)rv[q]);  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+      else r = (TO)rv[q];
+      out[p] = r;
+      if (out2) out2[p] = r;
+    }
+    b0 = b1; b1 = r3;
   }
-  // back substitution (src/Subroutines3D.f90:129-136 / 195-202)
-  double *po = out + base;
-  double b0 = fac[(L - 1) * 5 + 2] * f1;
-  double b1 = fac[(L - 2) * 5 + 2] * f2 - fac[(L - 2) * 5 + 3] * b0;
-  const double last = b0;
-  if (FILT) {
-    po[(int64_t)(L - 1) * stride] = LD(L - 1) + b0;
-    po[(int64_t)(L - 2) * stride] = LD(L - 2) + b1;
-  } else {
-    po[(int64_t)(L - 1) * stride] = b0;
-    po[(int64_t)(L - 2) * stride] = b1;
+  // back substitution, chunks in reverse: position j holds fw(j-3)
+  const int clast = ((L - 1) / XC_C) * XC_C;
+  for (int c0 = clast; c0 >= 0; c0 -= XC_C) {
+    const int cl = min(XC_C, L - c0);
+    __syncthreads();
+    if (lane < cl)
+      for (int ln = warp; ln < nl; ln += NW) tile[lane][ln] = fwg[(int64_t)ln * L + c0 + lane];
+    __syncthreads();
+    if (act) {
+      const int se = c0 == 0 ? 3 : 0;
+      for (int s = cl - 1; s >= se; s--) {
+        const int i = c0 + s - 3;
+        const TC v = fac[i * 5 + 2] * tile[s][t] - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
+        tile[s][t] = v;
+        b0 = b1; b1 = v;
+      }
+    }
+    __syncthreads();
+    const int sw = c0 == 0 ? 3 : 0;
+    if (lane < cl && lane >= sw)
+      for (int ln = warp; ln < nl; ln += NW) {
+        const int64_t p = (int64_t)ln * L + c0 + lane - 3;
+        const TC v = tile[lane][ln];
+        TO r;
+        if (FILT) r = (TO)(in[p] + (TI)v);
+        else r = (TO)v;
+        out[p] = r;
+        if (out2) out2[p] = r;
+      }
   }
-  for (int i = L - 3; i >= 0; i--) {
-    const double v = fac[i * 5 + 2] * fw[(int64_t)i * stride] - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
-    if (FILT) po[(int64_t)i * stride] = LD(i) + v;
-    else po[(int64_t)i * stride] = v;
-    b0 = b1; b1 = v;
+  if (act && !FILT && a.io.drva) {
+    TC *d = a.drva + B.face_off[1] * 10;
+    d[jk + nbs * ((a.io.m0 + f - 1) + 5 * 0)] = b1;  // drva(jk,m,0) = sb(is)
   }
-  if (!FILT) {
-    double *drva = c.drva + B.face_off[NN] * 10;
-    drva[jk + nbs * ((m - 1) + 5 * 0)] = b1;  // sb(is)
-    drva[jk + nbs * ((m - 1) + 5 * 1)] = last;  // sb(ie)
-  }
-#undef LD
 }
 
 // ---------------------------------------------------------------------------
 // mpigo (src/Subroutines3D.f90:16-80): closure values of every face with
-// ndf = 1.  The thread of face (A, nn, ip), line jk, computes what the
+// ndf = 1.  The thread of face (A, nn, ip), line jk, field f computes what the
 // neighbour B sends from its face 1-ip (the reference's tag pairing) and
-// writes it straight into A's recv buffer; with n45 = 1 it adds A's own
-// boundary value times pbcot (periodic coordinate re-basing).
+// writes it into A's recv; with n45 = 1 it adds A's own boundary value times
+// pbcot (periodic coordinate re-basing).
 // ---------------------------------------------------------------------------
-__global__ void k_mpigo(Ctx c, const FaceTask *tasks, int nt, int n45, const double *src1, const double *src2,
-                        const double *src3) {
+template <typename TI, typename TC>
+__global__ void k_mpigo(const BlockDev *blk, const Coef<TC> *cf, const FaceTask *tasks, int nt, int n45,
+                        const TI *src1, const TI *src2, const TI *src3, int64_t fs, TC *recv, int64_t recv_fs) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const Scheme &S = *c.sc;
-  const BlockDev &A = c.blk[T.b];
-  const BlockDev &Bn = c.blk[T.nb_b];
+  const int fld = blockIdx.z;
+  const Coef<TC> &C = *cf;
+  const BlockDev &A = blk[T.b];
+  const BlockDev &Bn = blk[T.nb_b];
   const int nn = T.nn, ip = T.ip, ipp = 1 - ip;
-  const double *src = nn == 1 ? src1 : (nn == 2 ? src2 : src3);
+  const TI *src = (nn == 1 ? src1 : (nn == 2 ? src2 : src3)) + fld * fs;
   int a1, a2, a3, b1, b2, b3;
   ijk_of(A, nn, a1, a2, a3);
   ijk_of(Bn, nn, b1, b2, b3);
   const int j = jk % (a2 + 1), k = jk / (a2 + 1);
   const int bcB = Bn.nbc[ipp][nn];
   const int ii = bcB == 40 ? 0 : 1;
-  const double ra0 = bcB == 45 ? (double)n45 : 0.0;
+  const TC ra0 = bcB == 45 ? (TC)n45 : (TC)0;
   const int isB = ipp * b1, ieB = 1 - 2 * ipp;
   const int mp = nt == 0 ? LMD : LMF;
-  const double res = ra0 * src[Bn.off + idx3(Bn.lxi, Bn.let, isB, j, k, nn)];
-  double s0 = 0, s1 = 0, sap0 = 0;
+  const TC res = ra0 * (TC)src[Bn.off + idx3(Bn.lxi, Bn.let, isB, j, k, nn)];
+  TC s0 = 0, s1 = 0, sap0 = 0;
   for (int i = 0; i <= mp; i++) {
-    const double v = src[Bn.off + idx3(Bn.lxi, Bn.let, isB + ieB * (i + ii), j, k, nn)];
+    const TC v = (TC)src[Bn.off + idx3(Bn.lxi, Bn.let, isB + ieB * (i + ii), j, k, nn)];
     if (i == 0) sap0 = v;
-    s0 += S.pbco[nt][0][i] * v;
-    s1 += S.pbco[nt][1][i] * v;
+    s0 += C.pbco[nt][0][i] * v;
+    s1 += C.pbco[nt][1][i] * v;
   }
-  double r0 = s0 - res * S.pbcot[nt][0];
-  double r1 = s1 - res * S.pbcot[nt][1];
-  double r2 = sap0 - res;
+  TC r0 = s0 - res * C.pbcot[nt][0];
+  TC r1 = s1 - res * C.pbcot[nt][1];
+  TC r2 = sap0 - res;
   if (n45 == 1 && A.nbc[ip][nn] == 45) {
-    const double v = src[A.off + idx3(A.lxi, A.let, ip * a1, j, k, nn)];
-    r0 = r0 + v * S.pbcot[nt][0];
-    r1 = r1 + v * S.pbcot[nt][1];
+    const TC v = (TC)src[A.off + idx3(A.lxi, A.let, ip * a1, j, k, nn)];
+    r0 = r0 + v * C.pbcot[nt][0];
+    r1 = r1 + v * C.pbcot[nt][1];
     r2 = r2 + v;
   }
   const int64_t nbs = A.nbsize[nn];
-  double *recv = c.recv + A.face_off[nn] * 6;
-  recv[jk + nbs * (0 + 3 * ip)] = r0;
-  recv[jk + nbs * (1 + 3 * ip)] = r1;
-  recv[jk + nbs * (2 + 3 * ip)] = r2;
+  TC *rc = recv + fld * recv_fs + A.face_off[nn] * 6;
+  rc[jk + nbs * (0 + 3 * ip)] = r0;
+  rc[jk + nbs * (1 + 3 * ip)] = r1;
+  rc[jk + nbs * (2 + 3 * ip)] = r2;
 }
 
 // ---------------------------------------------------------------------------
-// Pointwise stage kernels (grid-stride over all points of all blocks).
+// pointwise stage kernels (grid-stride over all points of all blocks)
 // ---------------------------------------------------------------------------
-#define GRID_STRIDE(g, N) for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < (N); g += (int64_t)gridDim.x * blockDim.x)
+#define GRID_STRIDE(g, N) \
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < (N); g += (int64_t)gridDim.x * blockDim.x)
 
-// primitives, pressure, temperature, Sutherland viscosity (src/Main3D.f90:576-583);
-// de(:,1) holds mu afterwards when viscous (src/Main3D.f90:627).
-__global__ void k_prim(Ctx c) {
-  const Scheme &S = *c.sc;
-  const int64_t N = c.N;
+// primitives, pressure, temperature, Sutherland viscosity (src/Main3D.f90:576-583)
+template <typename R>
+__global__ void k_prim(Eng<R> e) {
+  const Scheme &S = *e.sc;
+  const int64_t N = e.N;
+  const R gamm1 = (R)S.gamm1, gam = (R)S.gam, srefp1dre = (R)S.srefp1dre, srefoo = (R)S.srefoo;
   int bad = 0;
   GRID_STRIDE(g, N) {
-    const double q1 = c.qa[g], q2 = c.qa[g + N], q3 = c.qa[g + 2 * N], q4 = c.qa[g + 3 * N], q5 = c.qa[g + 4 * N];
-    const double d1 = 1.0 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
-    const double pp = S.gamm1 * (q5 - 0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
-    const double d5 = S.gam * pp * d1;
-    // T^1.5 as T*sqrt(T): same value as pow(T,1.5) to ~1 ulp, far fewer FP64 instructions
-    const double mu = S.srefp1dre * (d5 * sqrt(d5)) / (d5 + S.srefoo);
-    c.de[g] = S.nviscous == 1 ? mu : d1;
-    c.de[g + N] = d2; c.de[g + 2 * N] = d3; c.de[g + 3 * N] = d4; c.de[g + 4 * N] = d5;
-    c.p[g] = pp;
-    c.ss[g] = mu;
-    if (!(q1 > 0.0) || !(pp > 0.0) || !(fabs(q5) < 1e300)) bad = 1;
+    const R q1 = (R)e.qa[g], q2 = (R)e.qa[g + N], q3 = (R)e.qa[g + 2 * N], q4 = (R)e.qa[g + 3 * N],
+            q5 = (R)e.qa[g + 4 * N];
+    const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
+    const R pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
+    const R d5 = gam * pp * d1;
+    // T^1.5 as T*sqrt(T): the value of pow(T,1.5) to ~1 ulp with far fewer instructions
+    const R mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
+    e.prim[g] = d2; e.prim[g + N] = d3; e.prim[g + 2 * N] = d4; e.prim[g + 3 * N] = d5;
+    e.p[g] = pp;
+    e.mu[g] = mu;
+    if (!(q1 > (R)0) || !(pp > (R)0) || !(fabs((double)e.qa[g + 4 * N]) < 1e300)) bad = 1;
   }
-  if (bad) atomicOr(&c.scal->flag, 1);
+  if (bad) atomicOr(&e.scal->flag, 1);
 }
 
 __device__ __forceinline__ void atomic_max_pos(unsigned long long *a, double v) {
@@ -323,216 +521,236 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long *a, double v) 
 }
 
 // CFL spectral radii, max over all points (src/Main3D.f90:590-602)
-__global__ void k_cfl(Ctx c) {
-  const int64_t N = c.N;
-  const double u1 = c.scal->umf[1], u2 = c.scal->umf[2], u3 = c.scal->umf[3];
-  double m1 = 0.0, m2 = 0.0;
+template <typename R>
+__global__ void k_cfl(Eng<R> e) {
+  const int64_t N = e.N;
+  const R u1 = (R)e.scal->umf[1], u2 = (R)e.scal->umf[2], u3 = (R)e.scal->umf[3];
+  R m1 = 0, m2 = 0;
   GRID_STRIDE(g, N) {
-    const double x1 = c.xim[g], x2 = c.xim[g + N], x3 = c.xim[g + 2 * N];
-    const double e1 = c.etm[g], e2 = c.etm[g + N], e3 = c.etm[g + 2 * N];
-    const double z1 = c.zem[g], z2 = c.zem[g + N], z3 = c.zem[g + 2 * N];
-    const double d2 = c.de[g + N] + u1, d3 = c.de[g + 2 * N] + u2, d4 = c.de[g + 3 * N] + u3;
-    const double r1 = x1 * x1 + x2 * x2 + x3 * x3 + e1 * e1 + e2 * e2 + e3 * e3 + z1 * z1 + z2 * z2 + z3 * z3;
-    const double r2 = fabs(x1 * d2 + x2 * d3 + x3 * d4) + fabs(e1 * d2 + e2 * d3 + e3 * d4) + fabs(z1 * d2 + z2 * d3 + z3 * d4);
-    const double s2 = fabs(c.yaco[g]);
-    const double v1 = (sqrt(c.de[g + 4 * N] * r1) + r2) * s2;
-    const double d1 = 1.0 / c.qa[g];
-    const double v2 = d1 * c.ss[g] * r1 * s2 * s2;
+    const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
+    const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
+    const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+    const R d2 = e.prim[g] + u1, d3 = e.prim[g + N] + u2, d4 = e.prim[g + 2 * N] + u3;
+    const R r1 = x1 * x1 + x2 * x2 + x3 * x3 + e1 * e1 + e2 * e2 + e3 * e3 + z1 * z1 + z2 * z2 + z3 * z3;
+    const R r2 = fabs(x1 * d2 + x2 * d3 + x3 * d4) + fabs(e1 * d2 + e2 * d3 + e3 * d4) + fabs(z1 * d2 + z2 * d3 + z3 * d4);
+    const R s2 = fabs(e.yaco[g]);
+    const R v1 = (sqrt(e.prim[g + 3 * N] * r1) + r2) * s2;
+    const R d1 = (R)1 / (R)e.qa[g];
+    const R v2 = d1 * e.mu[g] * r1 * s2 * s2;
     m1 = fmax(m1, v1);
     m2 = fmax(m2, v2);
-    if (v1 != v1 || v2 != v2) atomicOr(&c.scal->flag, 4);
+    if (v1 != v1 || v2 != v2) atomicOr(&e.scal->flag, 4);
   }
+  double dm1 = (double)m1, dm2 = (double)m2;
   for (int o = 16; o > 0; o >>= 1) {
-    m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-    m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
+    dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
   }
   __shared__ double s1[32], s2v[32];
   const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  if (ln == 0) { s1[w] = m1; s2v[w] = m2; }
+  if (ln == 0) { s1[w] = dm1; s2v[w] = dm2; }
   __syncthreads();
   if (w == 0) {
     const int nw = blockDim.x >> 5;
-    m1 = ln < nw ? s1[ln] : 0.0;
-    m2 = ln < nw ? s2v[ln] : 0.0;
+    dm1 = ln < nw ? s1[ln] : 0.0;
+    dm2 = ln < nw ? s2v[ln] : 0.0;
     for (int o = 16; o > 0; o >>= 1) {
-      m1 = fmax(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-      m2 = fmax(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+      dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
+      dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
     }
     if (ln == 0) {
-      atomic_max_pos(&c.scal->cflmax[0], m1);
-      atomic_max_pos(&c.scal->cflmax[1], m2);
+      atomic_max_pos(&e.scal->cflmax[0], dm1);
+      atomic_max_pos(&e.scal->cflmax[1], dm2);
     }
   }
 }
 
-// physical gradients of one primitive (src/Main3D.f90:631-651):
-// o1 = xim(:,1)*rr1 + etm(:,1)*rr2 + zem(:,1)*rr3, o2 with component 2, o3 with 3
-__global__ void k_grad(Ctx c, double *o1, double *o2, double *o3) {
-  const int64_t N = c.N;
+// physical gradients of u, v, w, T and the viscous stresses and heat fluxes
+// (src/Main3D.f90:631-692), from the twelve derivative planes dv
+template <typename R>
+__global__ void k_visc(Eng<R> e) {
+  const Scheme &S = *e.sc;
+  const int64_t N = e.N;
+  const R gp = (R)S.gamm1prndtli, tgp = (R)S.tgamm1prndtli, tt = (R)S.two_three;
+  const R sm1 = (R)S.smago1, sm2 = (R)S.smago2;
+  const R *dv = e.dv;
+  R *t = e.tau;
   GRID_STRIDE(g, N) {
-    const double r1 = c.rr[g], r2 = c.rr[g + N], r3 = c.rr[g + 2 * N];
-    o1[g] = c.xim[g] * r1 + c.etm[g] * r2 + c.zem[g] * r3;
-    o2[g] = c.xim[g + N] * r1 + c.etm[g + N] * r2 + c.zem[g + N] * r3;
-    o3[g] = c.xim[g + 2 * N] * r1 + c.etm[g + 2 * N] * r2 + c.zem[g + 2 * N] * r3;
-  }
-}
-
-// stresses and heat fluxes (src/Main3D.f90:653-692)
-__global__ void k_stress(Ctx c) {
-  const Scheme &S = *c.sc;
-  const int64_t N = c.N;
-  double *t = c.tau;
-  GRID_STRIDE(g, N) {
-    const double yac = c.yaco[g];
-    double r1 = c.de[g] * yac;
-    double r2 = S.gamm1prndtli * r1, r3 = 0.0, d5;
-    double txx = t[g], tyy = t[g + N], tzz = t[g + 2 * N];
-    const double txy = t[g + 3 * N], tyz = t[g + 4 * N], tzx = t[g + 5 * N];
-    const double hxx = t[g + 6 * N], hyy = t[g + 7 * N], hzz = t[g + 8 * N];
+    const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
+    const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
+    const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+    R c[4][3];
+#pragma unroll
+    for (int f = 0; f < 4; f++) {
+      const R r1 = dv[g + (f * 3 + 0) * N], r2 = dv[g + (f * 3 + 1) * N], r3 = dv[g + (f * 3 + 2) * N];
+      c[f][0] = x1 * r1 + e1 * r2 + z1 * r3;
+      c[f][1] = x2 * r1 + e2 * r2 + z2 * r3;
+      c[f][2] = x3 * r1 + e3 * r2 + z3 * r3;
+    }
+    // txx,hzz,tzx from u; txy,tyy,hxx from v; hyy,tyz,tzz from w; ss(:,1:3) from T
+    R txx = c[0][0], hzz = c[0][1], tzx = c[0][2];
+    R txy = c[1][0], tyy = c[1][1], hxx = c[1][2];
+    R hyy = c[2][0], tyz = c[2][1], tzz = c[2][2];
+    const R yac = e.yaco[g];
+    R r1 = e.mu[g] * yac;
+    R r2 = gp * r1, r3 = 0, d5;
     if (S.les == 1) {
-      const double d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
-                        (hxx + tyz) * (hxx + tyz);
-      const double varr = pow(-1.0 / yac, 1.5);
-      const double q1 = c.qa[g];
-      r3 = q1 * (S.smago1 * S.smago1) * varr * sqrt(2.0 * d1);
+      const R d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
+                   (hxx + tyz) * (hxx + tyz);
+      const R varr = (R)pow(-1.0 / (double)yac, 1.5);
+      const R q1 = (R)e.qa[g];
+      r3 = q1 * (sm1 * sm1) * varr * sqrt((R)2 * d1);
       r1 = r1 + r3 * yac;
-      r2 = r2 + S.tgamm1prndtli * r3 * yac;
-      r3 = S.two_three * (q1 * S.smago2 * varr * d1);
-      d5 = S.two_three * (txx + tyy + tzz);
-      txx = r1 * (2.0 * txx - d5) - r3;
-      tyy = r1 * (2.0 * tyy - d5) - r3;
-      tzz = r1 * (2.0 * tzz - d5) - r3;
+      r2 = r2 + tgp * r3 * yac;
+      r3 = tt * (q1 * sm2 * varr * d1);
+      d5 = tt * (txx + tyy + tzz);
+      txx = r1 * ((R)2 * txx - d5) - r3;
+      tyy = r1 * ((R)2 * tyy - d5) - r3;
+      tzz = r1 * ((R)2 * tzz - d5) - r3;
     } else {
-      d5 = S.two_three * (txx + tyy + tzz);
-      txx = r1 * (2.0 * txx - d5);
-      tyy = r1 * (2.0 * tyy - d5);
-      tzz = r1 * (2.0 * tzz - d5);
+      d5 = tt * (txx + tyy + tzz);
+      txx = r1 * ((R)2 * txx - d5);
+      tyy = r1 * ((R)2 * tyy - d5);
+      tzz = r1 * ((R)2 * tzz - d5);
     }
-    const double ntxy = r1 * (txy + hzz), ntyz = r1 * (tyz + hxx), ntzx = r1 * (tzx + hyy);
-    const double d2 = c.de[g + N], d3 = c.de[g + 2 * N], d4 = c.de[g + 3 * N];
+    const R ntxy = r1 * (txy + hzz), ntyz = r1 * (tyz + hxx), ntzx = r1 * (tzx + hyy);
+    const R d2 = e.prim[g], d3 = e.prim[g + N], d4 = e.prim[g + 2 * N];
     t[g] = txx; t[g + N] = tyy; t[g + 2 * N] = tzz;
     t[g + 3 * N] = ntxy; t[g + 4 * N] = ntyz; t[g + 5 * N] = ntzx;
-    t[g + 6 * N] = r2 * c.ss[g] + d2 * txx + d3 * ntxy + d4 * ntzx;
-    t[g + 7 * N] = r2 * c.ss[g + N] + d2 * ntxy + d3 * tyy + d4 * ntyz;
-    t[g + 8 * N] = r2 * c.ss[g + 2 * N] + d2 * ntzx + d3 * ntyz + d4 * tzz;
+    t[g + 6 * N] = r2 * c[3][0] + d2 * txx + d3 * ntxy + d4 * ntzx;
+    t[g + 7 * N] = r2 * c[3][1] + d2 * ntxy + d3 * tyy + d4 * ntyz;
+    t[g + 8 * N] = r2 * c[3][2] + d2 * ntzx + d3 * ntyz + d4 * tzz;
   }
 }
 
-// contravariant velocities (src/Main3D.f90:710-715)
-__global__ void k_fluxprep(Ctx c) {
-  const int64_t N = c.N;
-  const double u1 = c.scal->umf[1], u2 = c.scal->umf[2], u3 = c.scal->umf[3];
-  GRID_STRIDE(g, N) {
-    const double r1 = c.de[g + N] + u1, r2 = c.de[g + 2 * N] + u2, r3 = c.de[g + 3 * N] + u3;
-    c.ss[g] = c.xim[g] * r1 + c.xim[g + N] * r2 + c.xim[g + 2 * N] * r3;
-    c.ss[g + N] = c.etm[g] * r1 + c.etm[g + N] * r2 + c.etm[g + 2 * N] * r3;
-    c.ss[g + 2 * N] = c.zem[g] * r1 + c.zem[g + N] * r2 + c.zem[g + 2 * N] * r3;
-  }
-}
-
-// flux components of variable m in the three directions (src/Main3D.f90:718-766)
-__global__ void k_flux(Ctx c, int m) {
-  const Scheme &S = *c.sc;
-  const int64_t N = c.N;
-  const double u1 = c.scal->umf[1], u2 = c.scal->umf[2], u3 = c.scal->umf[3];
+// contravariant velocities and the fifteen flux components
+// (src/Main3D.f90:710-766): flx plane (m-1)*3 + (nn-1)
+template <typename R>
+__global__ void k_flux(Eng<R> e) {
+  const Scheme &S = *e.sc;
+  const int64_t N = e.N;
+  const R u1 = (R)e.scal->umf[1], u2 = (R)e.scal->umf[2], u3 = (R)e.scal->umf[3];
   const bool visc = S.nviscous == 1;
-  const double *t = c.tau;
+  const R *t = e.tau;
+  R *F = e.flx;
   GRID_STRIDE(g, N) {
-    const double s1 = c.ss[g], s2 = c.ss[g + N], s3 = c.ss[g + 2 * N];
-    double r1, r2, r3;
-    if (m == 1) {
-      const double q = c.qa[g];
-      r1 = q * s1; r2 = q * s2; r3 = q * s3;
-    } else if (m <= 4) {
-      const double q = c.qa[g + (m - 1) * N], pp = c.p[g];
-      r1 = q * s1 + c.xim[g + (m - 2) * N] * pp;
-      r2 = q * s2 + c.etm[g + (m - 2) * N] * pp;
-      r3 = q * s3 + c.zem[g + (m - 2) * N] * pp;
-      if (visc) {
-        double ta, tb, tc;
-        if (m == 2) { ta = t[g]; tb = t[g + 3 * N]; tc = t[g + 5 * N]; }
-        else if (m == 3) { ta = t[g + 3 * N]; tb = t[g + N]; tc = t[g + 4 * N]; }
-        else { ta = t[g + 5 * N]; tb = t[g + 4 * N]; tc = t[g + 2 * N]; }
-        r1 = r1 - c.xim[g] * ta - c.xim[g + N] * tb - c.xim[g + 2 * N] * tc;
-        r2 = r2 - c.etm[g] * ta - c.etm[g + N] * tb - c.etm[g + 2 * N] * tc;
-        r3 = r3 - c.zem[g] * ta - c.zem[g + N] * tb - c.zem[g + 2 * N] * tc;
-      }
-    } else {
-      const double pp = c.p[g];
-      const double d5 = c.qa[g + 4 * N] + pp;
-      const double x1 = c.xim[g], x2 = c.xim[g + N], x3 = c.xim[g + 2 * N];
-      const double e1 = c.etm[g], e2 = c.etm[g + N], e3 = c.etm[g + 2 * N];
-      const double z1 = c.zem[g], z2 = c.zem[g + N], z3 = c.zem[g + 2 * N];
-      r1 = d5 * s1 - pp * (u1 * x1 + u2 * x2 + u3 * x3);
-      r2 = d5 * s2 - pp * (u1 * e1 + u2 * e2 + u3 * e3);
-      r3 = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
-      if (visc) {
-        const double ha = t[g + 6 * N], hb = t[g + 7 * N], hc = t[g + 8 * N];
-        r1 = r1 - x1 * ha - x2 * hb - x3 * hc;
-        r2 = r2 - e1 * ha - e2 * hb - e3 * hc;
-        r3 = r3 - z1 * ha - z2 * hb - z3 * hc;
-      }
+    const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
+    const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
+    const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+    const R r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
+    const R s1 = x1 * r1 + x2 * r2 + x3 * r3;
+    const R s2 = e1 * r1 + e2 * r2 + e3 * r3;
+    const R s3 = z1 * r1 + z2 * r2 + z3 * r3;
+    const R pp = e.p[g];
+    {
+      const R q = (R)e.qa[g];
+      F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
     }
-    c.rr[g] = r1; c.rr[g + N] = r2; c.rr[g + 2 * N] = r3;
-  }
-}
-
-// divergence de(:,m) = rr1+rr2+rr3 (src/Main3D.f90:722...) plus the sponge
-// term of spongego (src/SingleTurbulence3D.f90:368-372) on sponge points
-__global__ void k_div(Ctx c, int m) {
-  const Scheme &S = *c.sc;
-  const int64_t N = c.N;
-  GRID_STRIDE(g, N) {
-    double d = c.rr[g] + c.rr[g + N] + c.rr[g + 2 * N];
-    const double as = c.asz[g], bs = c.bsz[g];
-    if (as != 0.0 || bs != 0.0) {
-      if (m == 1) d = d + as * (c.qa[g] - 1.0);
-      else if (m <= 4) d = d + as * (c.qa[g + (m - 1) * N] - 0.0);
-      else d = d + bs * (c.p[g] - S.ham * 1.0);
+    R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
+    if (visc) {
+      ta[0] = t[g]; tb[0] = t[g + 3 * N]; tc[0] = t[g + 5 * N];
+      ta[1] = t[g + 3 * N]; tb[1] = t[g + N]; tc[1] = t[g + 4 * N];
+      ta[2] = t[g + 5 * N]; tb[2] = t[g + 4 * N]; tc[2] = t[g + 2 * N];
     }
-    c.de[g + (m - 1) * N] = d;
-  }
-}
-
-// RK update (src/Main3D.f90:876-881)
-__global__ void k_rk(Ctx c) {
-  const int64_t N = c.N;
-  const double dtk = c.scal->dtk;
-  GRID_STRIDE(g, N) {
-    const double r1 = dtk * c.yaco[g];
+    const R xm[3] = {x1, x2, x3}, em[3] = {e1, e2, e3}, zm[3] = {z1, z2, z3};
 #pragma unroll
-    for (int q = 0; q < 5; q++) c.qa[g + q * N] = c.qo[g + q * N] - r1 * c.de[g + q * N];
+    for (int m = 2; m <= 4; m++) {
+      const R q = (R)e.qa[g + (m - 1) * N];
+      R a = q * s1 + xm[m - 2] * pp;
+      R b = q * s2 + em[m - 2] * pp;
+      R c = q * s3 + zm[m - 2] * pp;
+      if (visc) {
+        a = a - x1 * ta[m - 2] - x2 * tb[m - 2] - x3 * tc[m - 2];
+        b = b - e1 * ta[m - 2] - e2 * tb[m - 2] - e3 * tc[m - 2];
+        c = c - z1 * ta[m - 2] - z2 * tb[m - 2] - z3 * tc[m - 2];
+      }
+      F[g + ((m - 1) * 3 + 0) * N] = a;
+      F[g + ((m - 1) * 3 + 1) * N] = b;
+      F[g + ((m - 1) * 3 + 2) * N] = c;
+    }
+    {
+      const R d5 = (R)e.qa[g + 4 * N] + pp;
+      R a = d5 * s1 - pp * (u1 * x1 + u2 * x2 + u3 * x3);
+      R b = d5 * s2 - pp * (u1 * e1 + u2 * e2 + u3 * e3);
+      R c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
+      if (visc) {
+        const R ha = t[g + 6 * N], hb = t[g + 7 * N], hc = t[g + 8 * N];
+        a = a - x1 * ha - x2 * hb - x3 * hc;
+        b = b - e1 * ha - e2 * hb - e3 * hc;
+        c = c - z1 * ha - z2 * hb - z3 * hc;
+      }
+      F[g + 12 * N] = a; F[g + 13 * N] = b; F[g + 14 * N] = c;
+    }
+  }
+}
+
+// divergence de(:,m) = rr1+rr2+rr3 (src/Main3D.f90:722...) plus the sponge of
+// spongego (src/SingleTurbulence3D.f90:368-372) on sponge points
+template <typename R>
+__global__ void k_div(Eng<R> e) {
+  const Scheme &S = *e.sc;
+  const int64_t N = e.N;
+  const R ham = (R)S.ham;
+  const R *F = e.flx;
+  GRID_STRIDE(g, N) {
+    const R as = e.asz[g], bs = e.bsz[g];
+    const bool sponge = as != (R)0 || bs != (R)0;
+#pragma unroll
+    for (int m = 1; m <= 5; m++) {
+      R d = F[g + ((m - 1) * 3 + 0) * N] + F[g + ((m - 1) * 3 + 1) * N] + F[g + ((m - 1) * 3 + 2) * N];
+      if (sponge) {
+        if (m == 1) d = d + as * ((R)e.qa[g] - (R)1);
+        else if (m <= 4) d = d + as * ((R)e.qa[g + (m - 1) * N] - (R)0);
+        else d = d + bs * (e.p[g] - ham * (R)1);
+      }
+      e.de[g + (m - 1) * N] = d;
+    }
+  }
+}
+
+// RK update (src/Main3D.f90:876-881): FP64 state, FP64 Jacobian
+template <typename R>
+__global__ void k_rk(Eng<R> e) {
+  const int64_t N = e.N;
+  const double dtk = e.scal->dtk;
+  GRID_STRIDE(g, N) {
+    const double r1 = dtk * e.yacod[g];
+#pragma unroll
+    for (int q = 0; q < 5; q++) e.qa[g + q * N] = e.qo[g + q * N] - r1 * (double)e.de[g + q * N];
   }
 }
 
 // ---------------------------------------------------------------------------
 // characteristic boundary treatment: eleme, xtq2r, xtr2q
 // (src/Subroutines3D.f90:235-324) and the GCBC/GCIC loops of
-// src/Main3D.f90:780-869.
+// src/Main3D.f90:780-869
 // ---------------------------------------------------------------------------
+template <typename R>
 struct Elem {
-  double rhoi, ao, aoi, ve[3], hv2, vn, vs;
+  R rhoi, ao, aoi, ve[3], hv2, vn, vs;
 };
 
-__device__ __forceinline__ void eleme(const Scheme &S, const Ctx &c, int64_t g, const double cm[3], const double umf[4],
-                                      Elem &e) {
-  const int64_t N = c.N;
-  e.rhoi = 1.0 / c.qa[g];
-  e.ao = sqrt(S.gam * e.rhoi * c.p[g]);
-  e.aoi = 1.0 / e.ao;
-  e.ve[0] = e.rhoi * c.qa[g + N];
-  e.ve[1] = e.rhoi * c.qa[g + 2 * N];
-  e.ve[2] = e.rhoi * c.qa[g + 3 * N];
-  e.hv2 = 0.5 * (e.ve[0] * e.ve[0] + e.ve[1] * e.ve[1] + e.ve[2] * e.ve[2]);
-  e.vn = cm[0] * e.ve[0] + cm[1] * e.ve[1] + cm[2] * e.ve[2];
-  e.vs = cm[0] * umf[1] + cm[1] * umf[2] + cm[2] * umf[3];
+template <typename R>
+__device__ __forceinline__ void eleme(const Scheme &S, const Eng<R> &e, int64_t g, const R cm[3], const R umf[4],
+                                      Elem<R> &el) {
+  const int64_t N = e.N;
+  el.rhoi = (R)1 / (R)e.qa[g];
+  el.ao = sqrt((R)S.gam * el.rhoi * e.p[g]);
+  el.aoi = (R)1 / el.ao;
+  el.ve[0] = el.rhoi * (R)e.qa[g + N];
+  el.ve[1] = el.rhoi * (R)e.qa[g + 2 * N];
+  el.ve[2] = el.rhoi * (R)e.qa[g + 3 * N];
+  el.hv2 = (R)0.5 * (el.ve[0] * el.ve[0] + el.ve[1] * el.ve[1] + el.ve[2] * el.ve[2]);
+  el.vn = cm[0] * el.ve[0] + cm[1] * el.ve[1] + cm[2] * el.ve[2];
+  el.vs = cm[0] * umf[1] + cm[1] * umf[2] + cm[2] * umf[3];
 }
 
-__device__ __forceinline__ void xtq2r(const Scheme &S, const Elem &e, const double cm[3], double xt[5][5]) {
-  const double ho = S.gamm1 * e.aoi * e.aoi, bo = 1.0 - ho * e.hv2, co = e.aoi * e.vn;
-  const double dm0 = e.aoi * cm[0], dm1 = e.aoi * cm[1], dm2 = e.aoi * cm[2];
-  const double rv0 = ho * e.ve[0], rv1 = ho * e.ve[1], rv2 = ho * e.ve[2];
-  const double *ve = e.ve;
+template <typename R>
+__device__ __forceinline__ void xtq2r(const Scheme &S, const Elem<R> &el, const R cm[3], R xt[5][5]) {
+  const R ho = (R)S.gamm1 * el.aoi * el.aoi, bo = (R)1 - ho * el.hv2, co = el.aoi * el.vn;
+  const R dm0 = el.aoi * cm[0], dm1 = el.aoi * cm[1], dm2 = el.aoi * cm[2];
+  const R rv0 = ho * el.ve[0], rv1 = ho * el.ve[1], rv2 = ho * el.ve[2];
+  const R *ve = el.ve;
   xt[0][0] = bo * cm[0] + dm1 * ve[2] - dm2 * ve[1];
   xt[0][1] = cm[0] * rv0;
   xt[0][2] = cm[0] * rv1 + dm2;
@@ -548,243 +766,247 @@ __device__ __forceinline__ void xtq2r(const Scheme &S, const Elem &e, const doub
   xt[2][2] = cm[2] * rv1 - dm0;
   xt[2][3] = cm[2] * rv2;
   xt[2][4] = -ho * cm[2];
-  xt[3][0] = 1.0 - bo - co;
+  xt[3][0] = (R)1 - bo - co;
   xt[3][1] = dm0 - rv0;
   xt[3][2] = dm1 - rv1;
   xt[3][3] = dm2 - rv2;
   xt[3][4] = ho;
-  xt[4][0] = 1.0 - bo + co;
+  xt[4][0] = (R)1 - bo + co;
   xt[4][1] = -dm0 - rv0;
   xt[4][2] = -dm1 - rv1;
   xt[4][3] = -dm2 - rv2;
   xt[4][4] = ho;
 }
 
-__device__ __forceinline__ void xtr2q(const Scheme &S, const Elem &e, const double cm[3], double xt[5][5]) {
-  const double bo = e.hv2 + S.hamm1 * e.ao * e.ao, co = e.ao * e.vn;
-  const double dm0 = e.ao * cm[0], dm1 = e.ao * cm[1], dm2 = e.ao * cm[2];
-  const double *ve = e.ve;
-  xt[0][0] = cm[0]; xt[0][1] = cm[1]; xt[0][2] = cm[2]; xt[0][3] = 0.5; xt[0][4] = 0.5;
+template <typename R>
+__device__ __forceinline__ void xtr2q(const Scheme &S, const Elem<R> &el, const R cm[3], R xt[5][5]) {
+  const R bo = el.hv2 + (R)S.hamm1 * el.ao * el.ao, co = el.ao * el.vn;
+  const R dm0 = el.ao * cm[0], dm1 = el.ao * cm[1], dm2 = el.ao * cm[2];
+  const R *ve = el.ve;
+  const R h = (R)0.5;
+  xt[0][0] = cm[0]; xt[0][1] = cm[1]; xt[0][2] = cm[2]; xt[0][3] = h; xt[0][4] = h;
   xt[1][0] = cm[0] * ve[0];
   xt[1][1] = cm[1] * ve[0] - dm2;
   xt[1][2] = cm[2] * ve[0] + dm1;
-  xt[1][3] = 0.5 * (ve[0] + dm0);
+  xt[1][3] = h * (ve[0] + dm0);
   xt[1][4] = xt[1][3] - dm0;
   xt[2][0] = cm[0] * ve[1] + dm2;
   xt[2][1] = cm[1] * ve[1];
   xt[2][2] = cm[2] * ve[1] - dm0;
-  xt[2][3] = 0.5 * (ve[1] + dm1);
+  xt[2][3] = h * (ve[1] + dm1);
   xt[2][4] = xt[2][3] - dm1;
   xt[3][0] = cm[0] * ve[2] - dm1;
   xt[3][1] = cm[1] * ve[2] + dm0;
   xt[3][2] = cm[2] * ve[2];
-  xt[3][3] = 0.5 * (ve[2] + dm2);
+  xt[3][3] = h * (ve[2] + dm2);
   xt[3][4] = xt[3][3] - dm2;
-  xt[4][0] = e.hv2 * cm[0] + dm2 * ve[1] - dm1 * ve[2];
-  xt[4][1] = e.hv2 * cm[1] + dm0 * ve[2] - dm2 * ve[0];
-  xt[4][2] = e.hv2 * cm[2] + dm1 * ve[0] - dm0 * ve[1];
-  xt[4][3] = 0.5 * (bo + co);
+  xt[4][0] = el.hv2 * cm[0] + dm2 * ve[1] - dm1 * ve[2];
+  xt[4][1] = el.hv2 * cm[1] + dm0 * ve[2] - dm2 * ve[0];
+  xt[4][2] = el.hv2 * cm[2] + dm1 * ve[0] - dm0 * ve[1];
+  xt[4][3] = h * (bo + co);
   xt[4][4] = xt[4][3] - co;
 }
 
-__device__ __forceinline__ void face_point(const BlockDev &B, int nn, int ip, int jk, int &i, int &j, int &k, int &i1) {
+__device__ __forceinline__ void face_point(const BlockDev &B, int nn, int ip, int jk, int &i, int &j, int &k) {
   int a1, a2, a3;
   ijk_of(B, nn, a1, a2, a3);
   j = jk % (a2 + 1);
   k = jk / (a2 + 1);
   i = ip * a1;
-  i1 = a1;
 }
 
-// GCBC/GCIC preparation: drva = X * (J * (ra0*drva + ra1*de)) (src/Main3D.f90:780-795)
-__global__ void k_gcbc_prep(Ctx c, const FaceTask *tasks) {
+// drva = X * (J * (ra0*drva + ra1*de)) (src/Main3D.f90:780-795)
+template <typename R>
+__global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const Scheme &S = *c.sc;
-  const BlockDev &B = c.blk[T.b];
+  const Scheme &S = *e.sc;
+  const BlockDev &B = e.blk[T.b];
   const int nn = T.nn, ip = T.ip, np = T.bc;
-  int i, j, k, i1;
-  face_point(B, nn, ip, jk, i, j, k, i1);
-  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, nn), N = c.N, nbs = T.nline;
-  const double ra0 = (double)((20 - np) * (25 - np) * (30 - np) / 3000), ra1 = 1.0 - ra0;
-  double *drva = c.drva + B.face_off[nn] * 10;
-  const double *cmv = c.cm + B.face_off[nn] * 6;
-  const double cm[3] = {cmv[jk + nbs * (0 + 3 * ip)], cmv[jk + nbs * (1 + 3 * ip)], cmv[jk + nbs * (2 + 3 * ip)]};
-  double umf[4] = {0, c.scal->umf[1], c.scal->umf[2], c.scal->umf[3]};
-  Elem e;
-  eleme(S, c, g, cm, umf, e);
-  double xt[5][5];
-  xtq2r(S, e, cm, xt);
-  double v[5];
-  const double yac = c.yaco[g];
+  int i, j, k;
+  face_point(B, nn, ip, jk, i, j, k);
+  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, nn), N = e.N, nbs = T.nline;
+  const R ra0 = (R)((20 - np) * (25 - np) * (30 - np) / 3000), ra1 = (R)1 - ra0;
+  R *drva = e.drva + B.face_off[nn] * 10;
+  const R *cmv = e.cm + B.face_off[nn] * 6;
+  const R cm[3] = {cmv[jk + nbs * (0 + 3 * ip)], cmv[jk + nbs * (1 + 3 * ip)], cmv[jk + nbs * (2 + 3 * ip)]};
+  const R umf[4] = {0, (R)e.scal->umf[1], (R)e.scal->umf[2], (R)e.scal->umf[3]};
+  Elem<R> el;
+  eleme(S, e, g, cm, umf, el);
+  R xt[5][5];
+  xtq2r(S, el, cm, xt);
+  R v[5];
+  const R yac = e.yaco[g];
 #pragma unroll
-  for (int q = 0; q < 5; q++) v[q] = yac * (ra0 * drva[jk + nbs * (q + 5 * ip)] + ra1 * c.de[g + q * N]);
+  for (int q = 0; q < 5; q++) v[q] = yac * (ra0 * drva[jk + nbs * (q + 5 * ip)] + ra1 * e.de[g + q * N]);
 #pragma unroll
   for (int r = 0; r < 5; r++) {
-    double s = 0.0;
+    R s = 0;
 #pragma unroll
     for (int q = 0; q < 5; q++) s += xt[r][q] * v[q];
     drva[jk + nbs * (r + 5 * ip)] = s;
   }
 }
 
-// GCBC/GCIC application for the faces of one direction (src/Main3D.f90:817-869).
-// Launched once per direction in the reference's order so that edge points
-// touched by faces of two directions accumulate in the same order.
-__global__ void k_gcbc_apply(Ctx c, const FaceTask *tasks) {
+// GCBC/GCIC application for the faces of one direction (src/Main3D.f90:817-869),
+// launched once per direction in the reference's order so that edge points
+// touched by faces of two directions accumulate in the same order
+template <typename R>
+__global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const Scheme &S = *c.sc;
-  const BlockDev &B = c.blk[T.b];
+  const Scheme &S = *e.sc;
+  const BlockDev &B = e.blk[T.b];
   const int nn = T.nn, ip = T.ip, np = T.bc, iq = 1 - 2 * ip;
-  const double ra0 = (double)iq;
-  int i, j, k, i1;
-  face_point(B, nn, ip, jk, i, j, k, i1);
-  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, nn), N = c.N, nbs = T.nline;
-  const double *drva = c.drva + B.face_off[nn] * 10;
-  const double *cmv = c.cm + B.face_off[nn] * 6;
-  const double cm[3] = {cmv[jk + nbs * (0 + 3 * ip)], cmv[jk + nbs * (1 + 3 * ip)], cmv[jk + nbs * (2 + 3 * ip)]};
-  double umf[4] = {0, c.scal->umf[1], c.scal->umf[2], c.scal->umf[3]};
-  Elem e;
-  eleme(S, c, g, cm, umf, e);
-  double cha[5], d0[5];
+  const R ra0 = (R)iq;
+  int i, j, k;
+  face_point(B, nn, ip, jk, i, j, k);
+  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, nn), N = e.N, nbs = T.nline;
+  const R *drva = e.drva + B.face_off[nn] * 10;
+  const R *cmv = e.cm + B.face_off[nn] * 6;
+  const R cm[3] = {cmv[jk + nbs * (0 + 3 * ip)], cmv[jk + nbs * (1 + 3 * ip)], cmv[jk + nbs * (2 + 3 * ip)]};
+  const R umf[4] = {0, (R)e.scal->umf[1], (R)e.scal->umf[2], (R)e.scal->umf[3]};
+  Elem<R> el;
+  eleme(S, e, g, cm, umf, el);
+  R cha[5], d0[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) { d0[q] = drva[jk + nbs * (q + 5 * ip)]; cha[q] = d0[q]; }
   if (np == 10) {
-    if (ra0 * (e.vn + e.vs + e.ao) > 0.0) cha[3] = 0.0;
-    if (ra0 * (e.vn + e.vs - e.ao) > 0.0) cha[4] = 0.0;
+    if (ra0 * (el.vn + el.vs + el.ao) > (R)0) cha[3] = 0;
+    if (ra0 * (el.vn + el.vs - el.ao) > (R)0) cha[4] = 0;
   } else if (np == 20 || np == 25) {
-    if (c.rpex[T.wall_off + jk] == 0.0) {
-      const double s = cm[0] * c.scal->dudtmf[1] + cm[1] * c.scal->dudtmf[2] + cm[2] * c.scal->dudtmf[3];
-      cha[3 + ip] = cha[4 - ip] + 2.0 * ra0 * e.aoi * c.qa[g] * (s + 50.0 * (e.vn + e.vs));
+    if (e.rpex[T.wall_off + jk] == (R)0) {
+      const R s = cm[0] * (R)e.scal->dudtmf[1] + cm[1] * (R)e.scal->dudtmf[2] + cm[2] * (R)e.scal->dudtmf[3];
+      cha[3 + ip] = cha[4 - ip] + (R)2 * ra0 * el.aoi * (R)e.qa[g] * (s + (R)50 * (el.vn + el.vs));
     }
   } else {  // 30: characteristic interface, incoming waves from the neighbour
-    const BlockDev &Bn = c.blk[T.nb_b];
-    const double *nbr = c.drva + Bn.face_off[nn] * 10;
-    double *drvb = c.drvb + B.face_off[nn] * 10;
-    double dha[5];
+    const BlockDev &Bn = e.blk[T.nb_b];
+    const R *nbr = e.drva + Bn.face_off[nn] * 10;
+    R *drvb = e.drvb + B.face_off[nn] * 10;
+    R dha[5];
 #pragma unroll
     for (int q = 0; q < 5; q++) {
       dha[q] = nbr[jk + nbs * (q + 5 * (1 - ip))];
       drvb[jk + nbs * (q + 5 * ip)] = dha[q];
     }
-    if (ra0 * (e.vn + e.vs) > 0.0) { cha[0] = dha[0]; cha[1] = dha[1]; cha[2] = dha[2]; }
-    if (ra0 * (e.vn + e.vs + e.ao) > 0.0) cha[3] = dha[3];
-    if (ra0 * (e.vn + e.vs - e.ao) > 0.0) cha[4] = dha[4];
+    if (ra0 * (el.vn + el.vs) > (R)0) { cha[0] = dha[0]; cha[1] = dha[1]; cha[2] = dha[2]; }
+    if (ra0 * (el.vn + el.vs + el.ao) > (R)0) cha[3] = dha[3];
+    if (ra0 * (el.vn + el.vs - el.ao) > (R)0) cha[4] = dha[4];
   }
-  double xt[5][5];
-  xtr2q(S, e, cm, xt);
-  double dif[5], dh[5];
+  R xt[5][5];
+  xtr2q(S, el, cm, xt);
+  R dif[5], dh[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) dif[q] = cha[q] - d0[q];
 #pragma unroll
   for (int r = 0; r < 5; r++) {
-    double s = 0.0;
+    R s = 0;
 #pragma unroll
     for (int q = 0; q < 5; q++) s += xt[r][q] * dif[q];
     dh[r] = s;
   }
-  const double *w = c.sbcc + T.sbcc_off + (int64_t)jk * (MBCI + 1);
+  const R *w = e.sbcc + T.sbcc_off + (int64_t)jk * (MBCI + 1);
   for (int ii = 0; ii <= MBCI; ii++) {
     const int64_t g2 = B.off + idx3(B.lxi, B.let, i + iq * ii, j, k, nn);
-    const double wv = w[ii];
+    const R wv = w[ii];
 #pragma unroll
-    for (int q = 0; q < 5; q++) c.de[g2 + q * N] = c.de[g2 + q * N] + wv * dh[q];
+    for (int q = 0; q < 5; q++) e.de[g2 + q * N] = e.de[g2 + q * N] + wv * dh[q];
   }
 }
 
-// wall temperature and velocity (src/Main3D.f90:886-895)
-__global__ void k_wall(Ctx c, const FaceTask *tasks) {
+// wall temperature and velocity (src/Main3D.f90:886-895), FP64 state
+__global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const Scheme &S = *c.sc;
-  const BlockDev &B = c.blk[T.b];
-  int i, j, k, i1;
-  face_point(B, T.nn, T.ip, jk, i, j, k, i1);
-  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = c.N;
+  const Scheme &S = *e.sc;
+  const BlockDev &B = e.blk[T.b];
+  int i, j, k;
+  face_point(B, T.nn, T.ip, jk, i, j, k);
+  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = e.N;
   const double ra0 = S.ham * S.hamm1 * S.wtemp;
   const double ra1 = (double)((T.bc - 20) / 5);
-  const double rp = c.rpex[T.wall_off + jk];
+  const double rp = e.rpex[T.wall_off + jk];
   const double ra2 = 1.0 - rp, ra3 = 1.0 - ra1 * ra2;
-  const double fctr = (1.0 - ra3) * c.qa[g];
-  const double q2 = ra3 * c.qa[g + N] - fctr * c.scal->umf[1];
-  const double q3 = ra3 * c.qa[g + 2 * N] - fctr * c.scal->umf[2];
-  const double q4 = ra3 * c.qa[g + 3 * N] - fctr * c.scal->umf[3];
-  c.qa[g + N] = q2; c.qa[g + 2 * N] = q3; c.qa[g + 3 * N] = q4;
-  const double q1 = c.qa[g];
-  c.qa[g + 4 * N] = rp * c.qa[g + 4 * N] + ra2 * (ra0 * q1 + 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
+  const double fctr = (1.0 - ra3) * e.qa[g];
+  const double q2 = ra3 * e.qa[g + N] - fctr * e.scal->umf[1];
+  const double q3 = ra3 * e.qa[g + 2 * N] - fctr * e.scal->umf[2];
+  const double q4 = ra3 * e.qa[g + 3 * N] - fctr * e.scal->umf[3];
+  e.qa[g + N] = q2; e.qa[g + 2 * N] = q3; e.qa[g + 3 * N] = q4;
+  const double q1 = e.qa[g];
+  e.qa[g + 4 * N] = rp * e.qa[g + 4 * N] + ra2 * (ra0 * q1 + 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
 }
 
 // junction averaging of the corner lines shared by four blocks
 // (src/SingleTurbulence3D.f90:378-443)
-__global__ void k_junction(Ctx c, const JunctionDev *jn, int njct) {
+__global__ void k_junction(Eng<double> e, const JunctionDev *jn, int njct) {
   const int jx = blockIdx.y;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (jx >= njct) return;
   const JunctionDev J = jn[jx];
   if (k >= J.nk) return;
-  const int64_t N = c.N;
+  const int64_t N = e.N;
   int64_t g[4];
 #pragma unroll
   for (int q = 0; q < 4; q++) g[q] = J.base[q] + (int64_t)k * J.kstr[q];
   double avg[5];
 #pragma unroll
   for (int m = 0; m < 5; m++) {
-    const double d1 = c.qa[g[0] + m * N], d2 = c.qa[g[1] + m * N], d3 = c.qa[g[2] + m * N], d4 = c.qa[g[3] + m * N];
+    const double d1 = e.qa[g[0] + m * N], d2 = e.qa[g[1] + m * N], d3 = e.qa[g[2] + m * N], d4 = e.qa[g[3] + m * N];
     if (m == 0 || m == 4) avg[m] = 0.25 * (d1 + d2 + d3 + d4);
-    else avg[m] = 0.5 * (c.qa[g[J.pa - 1] + m * N] + c.qa[g[J.pb - 1] + m * N]);
+    else avg[m] = 0.5 * (e.qa[g[J.pa - 1] + m * N] + e.qa[g[J.pb - 1] + m * N]);
   }
 #pragma unroll
   for (int q = 0; q < 4; q++)
 #pragma unroll
-    for (int m = 0; m < 5; m++) c.qa[g[q] + m * N] = avg[m];
+    for (int m = 0; m < 5; m++) e.qa[g[q] + m * N] = avg[m];
 }
 
 // interface averaging: pack qa of every BC 30/35/45 face (src/Main3D.f90:908-914)
-__global__ void k_pack(Ctx c, const FaceTask *tasks) {
+// into the FP64 face buffer drva of the set-up engine
+__global__ void k_pack(Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const BlockDev &B = c.blk[T.b];
-  int i, j, k, i1;
-  face_point(B, T.nn, T.ip, jk, i, j, k, i1);
-  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = c.N, nbs = T.nline;
-  double *drva = c.drva + B.face_off[T.nn] * 10;
+  const BlockDev &B = e.blk[T.b];
+  int i, j, k;
+  face_point(B, T.nn, T.ip, jk, i, j, k);
+  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = e.N, nbs = T.nline;
+  double *drva = e.drva + B.face_off[T.nn] * 10;
 #pragma unroll
-  for (int q = 0; q < 5; q++) drva[jk + nbs * (q + 5 * T.ip)] = c.qa[g + q * N];
-  c.rr[g] = 1.0;
+  for (int q = 0; q < 5; q++) drva[jk + nbs * (q + 5 * T.ip)] = e.qa[g + q * N];
+  e.cnt[g] = 1.0;
 }
 
 // interface averaging of the faces of one direction (src/Main3D.f90:926-952)
-__global__ void k_avg(Ctx c, const FaceTask *tasks) {
+__global__ void k_avg(Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const BlockDev &B = c.blk[T.b];
-  const BlockDev &Bn = c.blk[T.nb_b];
-  int i, j, k, i1;
-  face_point(B, T.nn, T.ip, jk, i, j, k, i1);
-  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = c.N, nbs = T.nline;
-  const double *nbr = c.drva + Bn.face_off[T.nn] * 10;
-  double *drvb = c.drvb + B.face_off[T.nn] * 10;
-  const double cnt = c.rr[g] + 1.0;
-  c.rr[g] = cnt;
+  const BlockDev &B = e.blk[T.b];
+  const BlockDev &Bn = e.blk[T.nb_b];
+  int i, j, k;
+  face_point(B, T.nn, T.ip, jk, i, j, k);
+  const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = e.N, nbs = T.nline;
+  const double *nbr = e.drva + Bn.face_off[T.nn] * 10;
+  double *drvb = e.drvb + B.face_off[T.nn] * 10;
+  const double cnt = e.cnt[g] + 1.0;
+  e.cnt[g] = cnt;
   const double w = 1.0 / cnt;
-  c.rr[g + N] = w;
+  e.cnt[g + N] = w;
 #pragma unroll
   for (int q = 0; q < 5; q++) {
     const double dv = nbr[jk + nbs * (q + 5 * (1 - T.ip))];
     drvb[jk + nbs * (q + 5 * T.ip)] = dv;
-    c.qa[g + q * N] = w * ((cnt - 1.0) * c.qa[g + q * N] + dv);
+    e.qa[g + q * N] = w * ((cnt - 1.0) * e.qa[g + q * N] + dv);
   }
 }
 
 // ---------------------------------------------------------------------------
 // time-marching scalars: movef/pitch (src/Subroutineso.f90:192-259) and the
-// dt schedule (src/Main3D.f90:571-610, 873-874, 964-965), one thread.
+// dt schedule (src/Main3D.f90:571-610, 873-874, 964-965), one thread
 // ---------------------------------------------------------------------------
 __device__ void d_movef(const Scheme &S, Scalars &s, double dtko, double dtk) {
   if (S.nsmf == 0) {
@@ -819,9 +1041,9 @@ __device__ void d_movef(const Scheme &S, Scalars &s, double dtko, double dtk) {
   }
 }
 
-__global__ void k_scalar(Ctx c, int op, int nk) {
-  const Scheme &S = *c.sc;
-  Scalars &s = *c.scal;
+__global__ void k_scalar(const Scheme *sc, Scalars *scal, int op, int nk) {
+  const Scheme &S = *sc;
+  Scalars &s = *scal;
   const int nkrk = S.nkrk;
   if (op == SC_MOVEF_A) {
     const double dtko = s.dt * min(max(nk - 2, 0), 1) / (nkrk - nk + 3);
@@ -858,33 +1080,32 @@ __global__ void k_scalar(Ctx c, int op, int nk) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// metrics (src/Main3D.f90:378-413): non-conservative cross products and J
-// from the coordinate derivatives held in qo(1:3) (x), qa(1:3) (y), de(1:3) (z)
-// ---------------------------------------------------------------------------
-__global__ void k_metrics(Ctx c) {
-  const int64_t N = c.N;
+// metrics (src/Main3D.f90:378-413): non-conservative cross products and J from
+// the coordinate derivatives held in qo(1:3) (x), qa(1:3) (y), de(1:3) (z)
+__global__ void k_metrics(Eng<double> e, double *xim, double *etm, double *zem, double *yaco) {
+  const int64_t N = e.N;
   GRID_STRIDE(g, N) {
-    const double qo1 = c.qo[g], qo2 = c.qo[g + N], qo3 = c.qo[g + 2 * N];
-    const double qa1 = c.qa[g], qa2 = c.qa[g + N], qa3 = c.qa[g + 2 * N];
-    const double de1 = c.de[g], de2 = c.de[g + N], de3 = c.de[g + 2 * N];
+    const double qo1 = e.qo[g], qo2 = e.qo[g + N], qo3 = e.qo[g + 2 * N];
+    const double qa1 = e.qa[g], qa2 = e.qa[g + N], qa3 = e.qa[g + 2 * N];
+    const double de1 = e.de[g], de2 = e.de[g + N], de3 = e.de[g + 2 * N];
     const double x1 = qa2 * de3 - de2 * qa3, x2 = de2 * qo3 - qo2 * de3, x3 = qo2 * qa3 - qa2 * qo3;
     const double e1 = qa3 * de1 - de3 * qa1, e2 = de3 * qo1 - qo3 * de1, e3 = qo3 * qa1 - qa3 * qo1;
     const double z1 = qa1 * de2 - de1 * qa2, z2 = de1 * qo2 - qo1 * de2, z3 = qo1 * qa2 - qa1 * qo2;
-    c.xim[g] = x1; c.xim[g + N] = x2; c.xim[g + 2 * N] = x3;
-    c.etm[g] = e1; c.etm[g + N] = e2; c.etm[g + 2 * N] = e3;
-    c.zem[g] = z1; c.zem[g + N] = z2; c.zem[g + 2 * N] = z3;
-    c.yaco[g] = 3.0 / (qo1 * x1 + qo2 * e1 + qo3 * z1 + qa1 * x2 + qa2 * e2 + qa3 * z2 + de1 * x3 + de2 * e3 + de3 * z3);
+    xim[g] = x1; xim[g + N] = x2; xim[g + 2 * N] = x3;
+    etm[g] = e1; etm[g + N] = e2; etm[g + 2 * N] = e3;
+    zem[g] = z1; zem[g + N] = z2; zem[g + 2 * N] = z3;
+    yaco[g] = 3.0 / (qo1 * x1 + qo2 * e1 + qo3 * z1 + qa1 * x2 + qa2 * e2 + qa3 * z2 + de1 * x3 + de2 * e3 + de3 * z3);
   }
 }
 
 // clpost wall integrals (src/rpt.f90:1017-1056), one CTA per wall face,
-// deterministic tree sum; out[face*2 + dir]
-__global__ void k_forces(Ctx c, const FaceTask *tasks, const double *area, const double *wnor, const int64_t *woff,
-                         double *out) {
+// fixed-order tree sum; out[face*2 + dir]
+template <typename R>
+__global__ void k_forces(Eng<R> e, const FaceTask *tasks, const double *area, const double *wnor,
+                         const int64_t *woff, double *out) {
   const FaceTask T = tasks[blockIdx.x];
-  const BlockDev &B = c.blk[T.b];
-  const int64_t N = c.N, nw = T.nline;
+  const BlockDev &B = e.blk[T.b];
+  const int64_t N = e.N, nw = T.nline;
   const double *ar = area + woff[blockIdx.x], *wn = wnor + 3 * woff[blockIdx.x];
   double acc[2] = {0.0, 0.0};
   for (int64_t ll = threadIdx.x; ll < nw; ll += blockDim.x) {
@@ -894,12 +1115,12 @@ __global__ void k_forces(Ctx c, const FaceTask *tasks, const double *area, const
     const int64_t g = B.off + ((int64_t)kk * (B.let + 1) + jw) * (B.lxi + 1) + ii;
     const double w1 = wn[ll], w2 = wn[ll + nw], w3 = wn[ll + 2 * nw];
     for (int dir = 0; dir < 2; dir++) {
-      double v = c.p[g] * (dir == 0 ? w1 : w2) * ar[ll];
-      if (c.sc->nviscous == 1) {
-        const double *t = c.tau;
+      double v = (double)e.p[g] * (dir == 0 ? w1 : w2) * ar[ll];
+      if (e.sc->nviscous == 1) {
+        const R *t = e.tau;
         double tw;
-        if (dir == 0) tw = c.qa[g] * (t[g] * w1 + t[g + 3 * N] * w2 + t[g + 5 * N] * w3);
-        else tw = c.qa[g] * (t[g + 3 * N] * w1 + t[g + N] * w2 + t[g + 4 * N] * w3);
+        if (dir == 0) tw = e.qa[g] * ((double)t[g] * w1 + (double)t[g + 3 * N] * w2 + (double)t[g + 5 * N] * w3);
+        else tw = e.qa[g] * ((double)t[g + 3 * N] * w1 + (double)t[g + N] * w2 + (double)t[g + 4 * N] * w3);
         v += tw * ar[ll];
       }
       acc[dir] += v;
@@ -925,26 +1146,69 @@ __global__ void k_forces(Ctx c, const FaceTask *tasks, const double *area, const
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_sweep(const Ctx &c, cudaStream_t st, int nn, bool filt, const double *in, double *out, int m, int nblocks,
-                  int maxlines) {
+template <typename TI, typename TO, typename TC>
+static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const SweepIO<TI, TO> &io, int nblocks,
+                    int maxlines, int maxlen) {
+  (void)maxlen;
+  SweepArgs<TI, TO, TC> a;
+  a.blk = e.blk;
+  a.cf = e.cf;
+  a.fac = filt ? e.facf : e.facd;
+  a.io = io;
+  a.fw = e.fw;
+  a.fw_fs = e.N;
+  a.recv = e.recv;
+  a.recv_fs = e.F * 6;
+  a.drva = e.drva;
+  if (nn == 1) {
+    dim3 grid((maxlines + XC_NL - 1) / XC_NL, nblocks, io.nf);
+    if (filt) k_sweep_xc<true, TI, TO, TC><<<grid, XC_NL, 0, st>>>(a);
+    else k_sweep_xc<false, TI, TO, TC><<<grid, XC_NL, 0, st>>>(a);
+    return;
+  }
   const int tpb = 128;
-  dim3 grid((maxlines + tpb - 1) / tpb, nblocks);
+  dim3 grid((maxlines + tpb - 1) / tpb, nblocks, io.nf);
   if (!filt) {
-    if (nn == 1) k_sweep<1, false><<<grid, tpb, 0, st>>>(c, in, out, m);
-    else if (nn == 2) k_sweep<2, false><<<grid, tpb, 0, st>>>(c, in, out, m);
-    else k_sweep<3, false><<<grid, tpb, 0, st>>>(c, in, out, m);
+    if (nn == 2) k_sweep_g<2, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
+    else k_sweep_g<3, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
   } else {
-    if (nn == 1) k_sweep<1, true><<<grid, tpb, 0, st>>>(c, in, out, m);
-    else if (nn == 2) k_sweep<2, true><<<grid, tpb, 0, st>>>(c, in, out, m);
-    else k_sweep<3, true><<<grid, tpb, 0, st>>>(c, in, out, m);
+    if (nn == 2) k_sweep_g<2, true, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
+    else k_sweep_g<3, true, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
   }
 }
 
-void launch_mpigo(const Ctx &c, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
-                  const double *s1, const double *s2, const double *s3) {
-  if (ntask == 0) return;
+void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,
+               int nblocks, int maxlines, int maxlen) {
+  sweep_t<double, double, double>(e, st, nn, filt, io, nblocks, maxlines, maxlen);
+}
+void sweep_fff(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io,
+               int nblocks, int maxlines, int maxlen) {
+  sweep_t<float, float, float>(e, st, nn, filt, io, nblocks, maxlines, maxlen);
+}
+void sweep_ddf(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,
+               int nblocks, int maxlines, int maxlen) {
+  sweep_t<double, double, float>(e, st, nn, filt, io, nblocks, maxlines, maxlen);
+}
+
+template <typename TI, typename TC>
+static void mpigo_t(const Eng<TC> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
+                    const TI *s1, const TI *s2, const TI *s3, int64_t fs, int nf) {
+  if (ntask == 0 || nf == 0) return;
   const int tpb = 128;
-  k_mpigo<<<dim3((maxline + tpb - 1) / tpb, ntask), tpb, 0, st>>>(c, tasks, nt, n45, s1, s2, s3);
+  k_mpigo<TI, TC><<<dim3((maxline + tpb - 1) / tpb, ntask, nf), tpb, 0, st>>>(e.blk, e.cf, tasks, nt, n45, s1, s2, s3,
+                                                                              fs, e.recv, e.F * 6);
+}
+void mpigo_ddd(const Eng<double> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
+               const double *s1, const double *s2, const double *s3, int64_t fs, int nf) {
+  mpigo_t<double, double>(e, st, tasks, ntask, maxline, nt, n45, s1, s2, s3, fs, nf);
+}
+void mpigo_fff(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
+               const float *s1, const float *s2, const float *s3, int64_t fs, int nf) {
+  mpigo_t<float, float>(e, st, tasks, ntask, maxline, nt, n45, s1, s2, s3, fs, nf);
+}
+void mpigo_ddf(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
+               const double *s1, const double *s2, const double *s3, int64_t fs, int nf) {
+  mpigo_t<double, float>(e, st, tasks, ntask, maxline, nt, n45, s1, s2, s3, fs, nf);
 }
 
 static int pw_grid(int64_t N) {
@@ -953,46 +1217,67 @@ static int pw_grid(int64_t N) {
   return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
-void launch_pointwise(const Ctx &c, cudaStream_t st, int which, int m, double *o1, double *o2, double *o3) {
-  const int g = pw_grid(c.N), t = 256;
+template <typename R>
+static void pointwise_t(const Eng<R> &e, cudaStream_t st, int which) {
+  const int g = pw_grid(e.N), t = 256;
   switch (which) {
-    case PW_PRIM: k_prim<<<g, t, 0, st>>>(c); break;
-    case PW_CFL: k_cfl<<<g, t, 0, st>>>(c); break;
-    case PW_GRAD: k_grad<<<g, t, 0, st>>>(c, o1, o2, o3); break;
-    case PW_STRESS: k_stress<<<g, t, 0, st>>>(c); break;
-    case PW_FLUXPREP: k_fluxprep<<<g, t, 0, st>>>(c); break;
-    case PW_FLUX: k_flux<<<g, t, 0, st>>>(c, m); break;
-    case PW_DIV: k_div<<<g, t, 0, st>>>(c, m); break;
-    case PW_RK: k_rk<<<g, t, 0, st>>>(c); break;
-    case PW_METRICS: k_metrics<<<g, t, 0, st>>>(c); break;
+    case PW_PRIM: k_prim<R><<<g, t, 0, st>>>(e); break;
+    case PW_CFL: k_cfl<R><<<g, t, 0, st>>>(e); break;
+    case PW_VISC: k_visc<R><<<g, t, 0, st>>>(e); break;
+    case PW_FLUX: k_flux<R><<<g, t, 0, st>>>(e); break;
+    case PW_DIV: k_div<R><<<g, t, 0, st>>>(e); break;
+    case PW_RK: k_rk<R><<<g, t, 0, st>>>(e); break;
   }
 }
+void pointwise_d(const Eng<double> &e, cudaStream_t st, int which) { pointwise_t<double>(e, st, which); }
+void pointwise_f(const Eng<float> &e, cudaStream_t st, int which) { pointwise_t<float>(e, st, which); }
 
-void launch_face(const Ctx &c, cudaStream_t st, int which, const FaceTask *tasks, int ntask, int maxline) {
+void face_d(const Eng<double> &e, cudaStream_t st, int which, const FaceTask *tasks, int ntask, int maxline) {
   if (ntask == 0) return;
   const int tpb = 128;
   dim3 grid((maxline + tpb - 1) / tpb, ntask);
   switch (which) {
-    case FK_GCBC_PREP: k_gcbc_prep<<<grid, tpb, 0, st>>>(c, tasks); break;
-    case FK_GCBC_APPLY: k_gcbc_apply<<<grid, tpb, 0, st>>>(c, tasks); break;
-    case FK_WALL: k_wall<<<grid, tpb, 0, st>>>(c, tasks); break;
-    case FK_PACK: k_pack<<<grid, tpb, 0, st>>>(c, tasks); break;
-    case FK_AVG: k_avg<<<grid, tpb, 0, st>>>(c, tasks); break;
+    case FK_GCBC_PREP: k_gcbc_prep<double><<<grid, tpb, 0, st>>>(e, tasks); break;
+    case FK_GCBC_APPLY: k_gcbc_apply<double><<<grid, tpb, 0, st>>>(e, tasks); break;
+    case FK_WALL: k_wall<<<grid, tpb, 0, st>>>(e, tasks); break;
+    case FK_PACK: k_pack<<<grid, tpb, 0, st>>>(e, tasks); break;
+    case FK_AVG: k_avg<<<grid, tpb, 0, st>>>(e, tasks); break;
+  }
+}
+void face_f(const Eng<float> &e, cudaStream_t st, int which, const FaceTask *tasks, int ntask, int maxline) {
+  if (ntask == 0) return;
+  const int tpb = 128;
+  dim3 grid((maxline + tpb - 1) / tpb, ntask);
+  switch (which) {
+    case FK_GCBC_PREP: k_gcbc_prep<float><<<grid, tpb, 0, st>>>(e, tasks); break;
+    case FK_GCBC_APPLY: k_gcbc_apply<float><<<grid, tpb, 0, st>>>(e, tasks); break;
+    default: break;  // wall, pack and averaging act on the FP64 state: face_d
   }
 }
 
-void launch_junction(const Ctx &c, cudaStream_t st, const JunctionDev *jn, int njct, int nk) {
+void junction(const Eng<double> &e, cudaStream_t st, const JunctionDev *jn, int njct, int nk) {
   if (njct == 0) return;
   const int tpb = 64;
-  k_junction<<<dim3((nk + tpb - 1) / tpb, njct), tpb, 0, st>>>(c, jn, njct);
+  k_junction<<<dim3((nk + tpb - 1) / tpb, njct), tpb, 0, st>>>(e, jn, njct);
 }
 
-void launch_scalar(const Ctx &c, cudaStream_t st, int op, int nk) { k_scalar<<<1, 1, 0, st>>>(c, op, nk); }
+void scalar(const Eng<double> &e, cudaStream_t st, int op, int nk) { k_scalar<<<1, 1, 0, st>>>(e.sc, e.scal, op, nk); }
 
-void launch_forces(const Ctx &c, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area,
-                   const double *wnor, const int64_t *woff, double *out) {
+void metrics(const Eng<double> &e, cudaStream_t st, const double *xyz) {
+  (void)xyz;
+  k_metrics<<<pw_grid(e.N), 256, 0, st>>>(e, const_cast<double *>(e.xim), const_cast<double *>(e.etm),
+                                           const_cast<double *>(e.zem), const_cast<double *>(e.yaco));
+}
+
+void forces_d(const Eng<double> &e, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area,
+              const double *wnor, const int64_t *woff, double *out) {
   if (ntask == 0) return;
-  k_forces<<<ntask, 256, 0, st>>>(c, tasks, area, wnor, woff, out);
+  k_forces<double><<<ntask, 256, 0, st>>>(e, tasks, area, wnor, woff, out);
+}
+void forces_f(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area,
+              const double *wnor, const int64_t *woff, double *out) {
+  if (ntask == 0) return;
+  k_forces<float><<<ntask, 256, 0, st>>>(e, tasks, area, wnor, woff, out);
 }
 
 }  // namespace ATI_KNS

@@ -1,4 +1,9 @@
-// ati_kernels.h — kernel launch interface shared by the C-ABI layer.
+// ati_kernels.h — launch interface of the stage engine shared by the C-ABI layer.
+//
+// The engine is templated on R, the type of the stage intermediates
+// (primitives, gradients, stresses, fluxes, right-hand side): double for the
+// FP64 path, float for the mixed path.  The conservative state qa/qo and the
+// Jacobian used by the RK update are always double.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -6,35 +11,92 @@
 
 namespace ati {
 
-// Device pointers of one case, passed to every kernel by value.
-struct Ctx {
-  const BlockDev *blk;
-  const Scheme *sc;
-  Scalars *scal;
-  int64_t N;  // points of all blocks
-  double *qa, *qo, *de, *rr, *ss, *xim, *etm, *zem, *p, *yaco, *tau, *asz, *bsz, *fw;
-  double *drva, *drvb, *recv, *cm;
-  const double *facd, *facf, *sbcc, *rpex;
+// scheme coefficients in compute precision T (cast from Scheme on the host)
+template <typename T>
+struct Coef {
+  T abc[3][6];
+  T pbci[2][2][12];
+  T pbco[2][2][12];
+  T pbcot[2][2];
+  T fam[3], fbm[3], fcm[3];
+  T fa, fb, fc;
+  T fex[4], ffx[4];
+  T aa, ab, ac;
 };
 
-enum { PW_PRIM, PW_CFL, PW_GRAD, PW_STRESS, PW_FLUXPREP, PW_FLUX, PW_DIV, PW_RK, PW_METRICS };
+// Device pointers of one case for intermediates of type R, passed by value.
+template <typename R>
+struct Eng {
+  const BlockDev *blk;
+  const Scheme *sc;
+  const Coef<R> *cf;
+  Scalars *scal;
+  int64_t N;            // points of all blocks
+  double *qa, *qo;      // state (5 planes each), FP64
+  const double *yacod;  // Jacobian, FP64 (RK update)
+  double *cnt;          // visit counts of the interface averaging (2 planes), FP64
+  R *de;                // right-hand side (5 planes)
+  R *prim;              // u, v, w, T (4 planes)
+  R *mu, *p;            // Sutherland viscosity, pressure
+  R *dv;                // d(u,v,w,T)/d(xi,eta,zeta): plane f*3 + (nn-1)
+  R *tau;               // txx,tyy,tzz,txy,tyz,tzx,hxx,hyy,hzz
+  R *flx;               // fluxes: plane (m-1)*3 + (nn-1)
+  R *fw;                // forward-elimination scratch, one plane per field in flight
+  const R *xim, *etm, *zem, *yaco;
+  const R *asz, *bsz;
+  R *drva, *drvb, *recv;
+  const R *cm;
+  const R *facd, *facf, *sbcc, *rpex;
+  int64_t F;            // face index count (face buffers of one field: 6*F for recv)
+};
+
+enum { PW_PRIM, PW_CFL, PW_VISC, PW_FLUX, PW_DIV, PW_RK };
 enum { FK_GCBC_PREP, FK_GCBC_APPLY, FK_WALL, FK_PACK, FK_AVG };
 enum { SC_MOVEF_A, SC_CFL_RESET, SC_DT_NEW, SC_DT, SC_MOVEF_B, SC_ADVANCE, SC_INIT };
 
+// One line sweep over every block: nf fields, field f reads in + f*in_fs and
+// writes out + f*out_fs (out2 + f*out_fs too when out2 is set); recv holds the
+// closure of field f at recv + f*6*F; a derivative writes its line-end values
+// to drva component m0 + f when drva is set.
+template <typename TI, typename TO>
+struct SweepIO {
+  const TI *in;
+  int64_t in_fs;
+  TO *out;
+  int64_t out_fs;
+  TO *out2;
+  int nf, m0;
+  bool drva;
+};
+
 // Launchers, declared once per arithmetic mode: ati::fast (FMA contraction)
-// and ati::strict (every operation rounded, -fmad=false).
-#define ATI_DECLARE_LAUNCHERS(NS) \
-  namespace NS { \
-  void launch_sweep(const Ctx &c, cudaStream_t st, int nn, bool filt, const double *in, double *out, int m, int nblocks, \
-                    int maxlines); \
-  void launch_mpigo(const Ctx &c, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45, \
-                    const double *s1, const double *s2, const double *s3); \
-  void launch_pointwise(const Ctx &c, cudaStream_t st, int which, int m, double *o1, double *o2, double *o3); \
-  void launch_face(const Ctx &c, cudaStream_t st, int which, const FaceTask *tasks, int ntask, int maxline); \
-  void launch_junction(const Ctx &c, cudaStream_t st, const JunctionDev *jn, int njct, int nk); \
-  void launch_scalar(const Ctx &c, cudaStream_t st, int op, int nk); \
-  void launch_forces(const Ctx &c, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area, \
-                     const double *wnor, const int64_t *woff, double *out); \
+// and ati::strict (every operation rounded, -fmad=false).  Sweep and closure
+// launchers exist for (in, out, compute) = (d,d,d), (f,f,f) and (d,d,f).
+#define ATI_DECLARE_LAUNCHERS(NS)                                                                                  \
+  namespace NS {                                                                                                   \
+  void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,      \
+                 int nblocks, int maxlines, int maxlen);                                                           \
+  void sweep_fff(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io,         \
+                 int nblocks, int maxlines, int maxlen);                                                           \
+  void sweep_ddf(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,       \
+                 int nblocks, int maxlines, int maxlen);                                                           \
+  void mpigo_ddd(const Eng<double> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,      \
+                 int n45, const double *s1, const double *s2, const double *s3, int64_t fs, int nf);              \
+  void mpigo_fff(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,       \
+                 int n45, const float *s1, const float *s2, const float *s3, int64_t fs, int nf);                 \
+  void mpigo_ddf(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,       \
+                 int n45, const double *s1, const double *s2, const double *s3, int64_t fs, int nf);              \
+  void pointwise_d(const Eng<double> &e, cudaStream_t st, int which);                                             \
+  void pointwise_f(const Eng<float> &e, cudaStream_t st, int which);                                              \
+  void face_d(const Eng<double> &e, cudaStream_t st, int which, const FaceTask *tasks, int ntask, int maxline);    \
+  void face_f(const Eng<float> &e, cudaStream_t st, int which, const FaceTask *tasks, int ntask, int maxline);     \
+  void junction(const Eng<double> &e, cudaStream_t st, const JunctionDev *jn, int njct, int nk);                   \
+  void scalar(const Eng<double> &e, cudaStream_t st, int op, int nk);                                             \
+  void metrics(const Eng<double> &e, cudaStream_t st, const double *xyz_d);                                       \
+  void forces_d(const Eng<double> &e, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area,       \
+                const double *wnor, const int64_t *woff, double *out);                                             \
+  void forces_f(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area,        \
+                const double *wnor, const int64_t *woff, double *out);                                             \
   }
 ATI_DECLARE_LAUNCHERS(fast)
 ATI_DECLARE_LAUNCHERS(strict)

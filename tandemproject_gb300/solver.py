@@ -64,8 +64,7 @@ SIGNATURES = {
 }
 
 KERNEL_CLASSES = ["deriv_xi", "deriv_eta", "deriv_zeta", "filter_xi", "filter_eta", "filter_zeta", "mpigo",
-                  "prim", "cfl", "grad", "stress", "flux", "div", "rk", "gcbc", "wall_junction", "average",
-                  "scalar", "copy"]
+                  "prim", "cfl", "visc", "flux", "div", "rk", "gcbc", "wall_junction", "average", "scalar"]
 
 _lib = None
 
