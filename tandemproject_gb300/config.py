@@ -5,6 +5,7 @@ read at src/SingleTurbulence3D.f90:39-62), mirrored as the C struct
 
 Presets name the workloads by what they are:
   naca0012_0p6m  NACA 0012, 6 blocks (91/201/91)x40x20 = 0.61 M points, FP64
+  naca0012_3p5m  NACA 0012, 6 blocks 256x96x24 = 3.54 M points, FP64 (profiler captures)
   naca0012_8p8m  NACA 0012, 6 blocks 384x120x32 = 8.85 M points, FP64
   naca0012_25m   NACA 0012, 6 blocks 640x200x32 = 24.6 M points, mixed
 """
@@ -156,6 +157,8 @@ PRESETS = {
     # smgrid scales the near-wall spacing with resolution so that the quintic
     # grid lines of gridf stay monotone (no folded cells) at these sizes
     "naca0012_8p8m": CaseConfig(lxibk=(383, 383, 383), letbk=(119, 119), lzebk=(31,), smgrid=0.0025),
+    # a 3.5 M-point case (2.4 GB FP64 arena, state larger than L2) for profiler captures
+    "naca0012_3p5m": CaseConfig(lxibk=(255, 255, 255), letbk=(95, 95), lzebk=(23,), smgrid=0.004),
     "naca0012_25m": CaseConfig(lxibk=(639, 639, 639), letbk=(199, 199), lzebk=(31,), smgrid=0.002,
                                precision=MIXED),
 }

@@ -288,9 +288,9 @@ __global__ void k_to_float(const double *src, float *dst, int64_t n) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     dst[g] = (float)src[g];
 }
-__global__ void k_to_double(const float *src, double *dst, int64_t n) {
+__global__ void k_to_double(const float *src, double *dst, int64_t n, double add) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
-    dst[g] = (double)src[g];
+    dst[g] = (double)src[g] + add;
 }
 
 }  // namespace
@@ -500,13 +500,14 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
                o_blk = take(sizeof(BlockDev) * h->nb), o_sc = take(sizeof(Scheme)), o_cfd = take(sizeof(Coef<double>)),
                o_scal = take(sizeof(Scalars)), o_task = take(sizeof(FaceTask) * h->htasks.size()),
                o_jn = take(sizeof(JunctionDev) * 4), o_woff = take(16 * sizeof(int64_t));
-  // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(5) xim etm zem(3) yaco asz bsz(1)
+  // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
-         o_frpex = 0, o_cff = 0;
-  const int np32 = 5 + 4 + 1 + 1 + 12 + 9 + 15 + 5 + 9 + 1 + 1 + 1;
+         o_frpex = 0, o_cff = 0, o_fdrvm = 0;
+  const int np32 = 5 + 4 + 1 + 1 + 12 + 9 + 15 + 5 + 9 + 1 + 1 + 1 + 3;
   if (h->mixed) {
     o_ff = take((size_t)np32 * N * F4);
     o_fdrva = take(10 * F * F4); o_fdrvb = take(10 * F * F4); o_frecv = take(30 * F * F4); o_fcm = take(6 * F * F4);
+    o_fdrvm = take(10 * F * F4);
     o_ffacd = take(facd.size() * F4); o_ffacf = take(facf.size() * F4);
     o_fsbcc = take(std::max<int64_t>(h->nsbcc, 1) * F4); o_frpex = take(std::max<int64_t>(h->nwall, 1) * F4);
     o_cff = take(sizeof(Coef<float>));
@@ -546,7 +547,8 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
     m.de = g; g += 5 * N; m.prim = g; g += 4 * N; m.mu = g; g += N; m.p = g; g += N; m.dv = g; g += 12 * N;
     m.tau = g; g += 9 * N; m.flx = g; g += 15 * N; m.fw = g; g += 5 * N;
     m.xim = g; g += 3 * N; m.etm = g; g += 3 * N; m.zem = g; g += 3 * N; m.yaco = g; g += N;
-    m.asz = g; g += N; m.bsz = g; g += N;
+    m.asz = g; g += N; m.bsz = g; g += N; m.gm = g; g += 3 * N;
+    m.drvm = Fp(o_fdrvm);
     m.drva = Fp(o_fdrva); m.drvb = Fp(o_fdrvb); m.recv = Fp(o_frecv); m.cm = Fp(o_fcm);
     m.facd = Fp(o_ffacd); m.facf = Fp(o_ffacf); m.sbcc = Fp(o_fsbcc); m.rpex = Fp(o_frpex);
   }
@@ -675,8 +677,9 @@ static int copy_field(ati_handle *h, int blk, int field, double *host, bool to_d
   if (to_dev) {
     CK(cudaMemcpy2DAsync(base + B.off, dp, host, w, w, nc, cudaMemcpyHostToDevice, h->st));
   } else {
-    if (f32) {  // widen the FP32 stage field into the FP64 array first
-      k_to_double<<<256, 256, 0, h->st>>>(f32, base, (int64_t)nc * h->N);
+    if (f32) {  // widen the FP32 stage field into the FP64 array first (the mixed pressure plane holds p - p_inf)
+      const double add = field == ATI_F_P ? h->sh.s.poo : 0.0;
+      k_to_double<<<256, 256, 0, h->st>>>(f32, base, (int64_t)nc * h->N, add);
       CKL();
     }
     CK(cudaMemcpy2DAsync(host, w, base + B.off, dp, w, nc, cudaMemcpyDeviceToHost, h->st));
@@ -832,6 +835,19 @@ extern "C" int ati_init(ati_handle_t *h) {
     if (!rc) rc = to_float(h, c.sbcc, m.sbcc, h->nsbcc);
     if (!rc) rc = to_float(h, c.rpex, m.rpex, h->nwall);
     if (rc) return rc;
+    // metric divergence and its line-end values, FP64, for the freestream part of the fluxes: the same closure and
+    // sweeps as the flux derivatives (n45 = 0), applied to xim/etm/zem; flx is free scratch here
+    strict::mpigo_ddd(c, h->st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, 0, 0, c.xim, c.etm, c.zem, N,
+                      3);
+    const double *mf[3] = {c.xim, c.etm, c.zem};
+    for (int nn = 1; nn <= 3; nn++) {
+      SweepIO<double, double> io{mf[nn - 1], N, c.flx + 3 * (nn - 1) * N, N, nullptr, 3, 1, true};
+      strict::sweep_ddd(c, h->st, nn, false, io, h->nb, h->maxlines[nn], h->maxlen[nn]);
+    }
+    strict::metric_divergence(c, h->st, c.flx, const_cast<float *>(m.gm));
+    CKL();
+    rc = to_float(h, c.drva, const_cast<float *>(m.drvm), 10 * h->F);
+    if (rc) return rc;
   }
   // initial condition and time scalars (src/Main3D.f90:520-522)
   k_ic<<<256, 256, 0, h->st>>>(c);
@@ -870,7 +886,7 @@ struct EngineCalls<double> {
     else fast::mpigo_ddd(e, st, t, n, ml, nt, 0, s1, s2, s3, fs, nf);
   }
   static void qmpigo(bool strict, const Eng<double> &e, cudaStream_t st, const FaceTask *t, int n, int ml,
-                     const double *q, int64_t fs) {
+                     const double *q, int64_t fs, const FieldOfs<double> &) {
     mpigo(strict, e, st, t, n, ml, 1, q, q, q, fs, 5);
   }
   static void pw(bool strict, const Eng<double> &e, cudaStream_t st, int which) {
@@ -898,8 +914,8 @@ struct EngineCalls<float> {
     fast::mpigo_fff(e, st, t, n, ml, nt, 0, s1, s2, s3, fs, nf);
   }
   static void qmpigo(bool, const Eng<float> &e, cudaStream_t st, const FaceTask *t, int n, int ml, const double *q,
-                     int64_t fs) {
-    fast::mpigo_ddf(e, st, t, n, ml, 1, 0, q, q, q, fs, 5);
+                     int64_t fs, const FieldOfs<double> &fo) {
+    fast::mpigo_ddf(e, st, t, n, ml, 1, 0, q, q, q, fs, 5, fo);
   }
   static void pw(bool, const Eng<float> &e, cudaStream_t st, int which) { fast::pointwise_f(e, st, which); }
   static void face(bool, const Eng<float> &e, cudaStream_t st, int which, const FaceTask *t, int n, int ml) {
@@ -914,9 +930,14 @@ static int filter_step_t(ati_handle *h, const Eng<R> &e) {
   const int64_t N = h->N;
   // per-step filter of the five variables in place on qa, then qo = qa
   // (src/Main3D.f90:555-561); the last sweep writes qo as well
-  PROF(h, ATI_K_MPIGO, C::qmpigo(strict, e, h->st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, h->ed.qa, N));
+  // the mixed path filters q - q_inf (rho_inf = 1, rhoE_inf = p_inf/(gamma-1)): the filter annihilates constants,
+  // and removing them before the FP32 rounding keeps the rounding relative to the deviation
+  FieldOfs<double> fo{};
+  if (Freestream<R>::on) { fo.v[0] = h->sh.s.rhooo; fo.v[4] = h->sh.s.hamm1 * h->sh.s.poo; }
+  PROF(h, ATI_K_MPIGO, C::qmpigo(strict, e, h->st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, h->ed.qa, N, fo));
   for (int nn = 1; nn <= 3; nn++) {
     SweepIO<double, double> io{h->ed.qa, N, h->ed.qa, N, nn == 3 ? h->ed.qo : nullptr, 5, 1, false};
+    for (int f = 0; f < 5; f++) io.ofs[f] = fo.v[f];
     PROF(h, ATI_K_FILTER_XI + nn - 1, C::qsweep(strict, e, h->st, nn, io, h->nb, h->maxlines[nn], h->maxlen[nn]));
   }
   CKL();

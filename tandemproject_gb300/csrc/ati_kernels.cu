@@ -12,6 +12,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #include "ati_kernels.h"
 
@@ -219,11 +220,19 @@ __device__ __forceinline__ bool line_geom(const BlockDev &B, int t, int64_t &bas
   return true;
 }
 
+// input conversion: a wider input loses its constant offset before rounding
+template <typename TI, typename TC>
+__device__ __forceinline__ TC cvt_in(TI v, TI ofs) {
+  if constexpr (std::is_same<TI, TC>::value) return v;
+  else return (TC)(v - ofs);
+}
+
 template <typename TI, typename TC>
 struct GlobalSrc {
   const TI *p;
   int64_t s;
-  __device__ __forceinline__ TC operator()(int i) const { return (TC)p[(int64_t)i * s]; }
+  TI ofs;
+  __device__ __forceinline__ TC operator()(int i) const { return cvt_in<TI, TC>(p[(int64_t)i * s], ofs); }
 };
 template <typename TC>
 struct GlobalFw {
@@ -275,7 +284,7 @@ __global__ void __launch_bounds__(128) k_sweep_g(SweepArgs<TI, TO, TC> a) {
   const TC *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
   const TC *fac = a.fac + B.fac_off[NN] * 5;
   const TI *pin = a.io.in + f * a.io.in_fs + base;
-  GlobalSrc<TI, TC> ld{pin, stride};
+  GlobalSrc<TI, TC> ld{pin, stride, a.io.ofs[f]};
   GlobalFw<TC> fw{a.fw + f * a.fw_fs + base, stride};
   TO *o2 = a.io.out2 ? a.io.out2 + f * a.io.out_fs + base : nullptr;
   GlobalSink<FILT, TI, TO, TC> put{pin, a.io.out + f * a.io.out_fs + base, o2, stride};
@@ -329,7 +338,7 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
   TC a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, f1 = 0, f2 = 0, w0 = 0, w1 = 0, w2 = 0;
   if (act) {
     const TC *rcv = a.recv + f * a.recv_fs + B.face_off[1] * 6;
-    GlobalSrc<TI, TC> ld{in + (int64_t)t * L, 1};
+    GlobalSrc<TI, TC> ld{in + (int64_t)t * L, 1, a.io.ofs[f]};
     line_ends<FILT, TC>(C, L, B.ndf[0][1], B.ndf[1][1], rcv, nbs, jk, ld, sbs0, sbs1, sbs2, sbe0, sbe1, sbe2);
     a0 = ld(0); a1 = ld(1); a2 = ld(2); a3 = ld(3); a4 = ld(4); a5 = ld(5);
     f2 = sbs0;
@@ -340,11 +349,12 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
     f2 = f1; f1 = v;
   }
   // forward elimination, chunk by chunk
+  const TI ofs = a.io.ofs[f];
   for (int c0 = 0; c0 < L; c0 += XC_C) {
     const int cl = min(XC_C, L - c0);
     __syncthreads();
     if (lane < cl)
-      for (int ln = warp; ln < nl; ln += NW) tile[lane][ln] = (TC)in[(int64_t)ln * L + c0 + lane];
+      for (int ln = warp; ln < nl; ln += NW) tile[lane][ln] = cvt_in<TI, TC>(in[(int64_t)ln * L + c0 + lane], ofs);
     __syncthreads();
     if (act) {
       int s0 = 0;
@@ -444,7 +454,8 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
 // ---------------------------------------------------------------------------
 template <typename TI, typename TC>
 __global__ void k_mpigo(const BlockDev *blk, const Coef<TC> *cf, const FaceTask *tasks, int nt, int n45,
-                        const TI *src1, const TI *src2, const TI *src3, int64_t fs, TC *recv, int64_t recv_fs) {
+                        const TI *src1, const TI *src2, const TI *src3, int64_t fs, TC *recv, int64_t recv_fs,
+                        FieldOfs<TI> fo) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
@@ -463,10 +474,11 @@ __global__ void k_mpigo(const BlockDev *blk, const Coef<TC> *cf, const FaceTask 
   const TC ra0 = bcB == 45 ? (TC)n45 : (TC)0;
   const int isB = ipp * b1, ieB = 1 - 2 * ipp;
   const int mp = nt == 0 ? LMD : LMF;
-  const TC res = ra0 * (TC)src[Bn.off + idx3(Bn.lxi, Bn.let, isB, j, k, nn)];
+  const TI ofs = fo.v[fld];
+  const TC res = ra0 * cvt_in<TI, TC>(src[Bn.off + idx3(Bn.lxi, Bn.let, isB, j, k, nn)], ofs);
   TC s0 = 0, s1 = 0, sap0 = 0;
   for (int i = 0; i <= mp; i++) {
-    const TC v = (TC)src[Bn.off + idx3(Bn.lxi, Bn.let, isB + ieB * (i + ii), j, k, nn)];
+    const TC v = cvt_in<TI, TC>(src[Bn.off + idx3(Bn.lxi, Bn.let, isB + ieB * (i + ii), j, k, nn)], ofs);
     if (i == 0) sap0 = v;
     s0 += C.pbco[nt][0][i] * v;
     s1 += C.pbco[nt][1][i] * v;
@@ -475,7 +487,7 @@ __global__ void k_mpigo(const BlockDev *blk, const Coef<TC> *cf, const FaceTask 
   TC r1 = s1 - res * C.pbcot[nt][1];
   TC r2 = sap0 - res;
   if (n45 == 1 && A.nbc[ip][nn] == 45) {
-    const TC v = (TC)src[A.off + idx3(A.lxi, A.let, ip * a1, j, k, nn)];
+    const TC v = cvt_in<TI, TC>(src[A.off + idx3(A.lxi, A.let, ip * a1, j, k, nn)], ofs);
     r0 = r0 + v * C.pbcot[nt][0];
     r1 = r1 + v * C.pbcot[nt][1];
     r2 = r2 + v;
@@ -500,18 +512,28 @@ __global__ void k_prim(Eng<R> e) {
   const int64_t N = e.N;
   const R gamm1 = (R)S.gamm1, gam = (R)S.gam, srefp1dre = (R)S.srefp1dre, srefoo = (R)S.srefoo;
   int bad = 0;
+  const double rhoE_inf = S.hamm1 * S.poo;
   GRID_STRIDE(g, N) {
-    const R q1 = (R)e.qa[g], q2 = (R)e.qa[g + N], q3 = (R)e.qa[g + 2 * N], q4 = (R)e.qa[g + 3 * N],
-            q5 = (R)e.qa[g + 4 * N];
+    const R q1 = (R)e.qa[g], q2 = (R)e.qa[g + N], q3 = (R)e.qa[g + 2 * N], q4 = (R)e.qa[g + 3 * N];
     const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
-    const R pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
-    const R d5 = gam * pp * d1;
+    R pp, d5;
+    if constexpr (Freestream<R>::on) {
+      // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
+      const R re = (R)(e.qa[g + 4 * N] - rhoE_inf);
+      pp = gamm1 * (re - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
+      d5 = gam * ((R)S.poo + pp) * d1;
+    } else {
+      const R q5 = (R)e.qa[g + 4 * N];
+      pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
+      d5 = gam * pp * d1;
+    }
     // T^1.5 as T*sqrt(T): the value of pow(T,1.5) to ~1 ulp with far fewer instructions
     const R mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
     e.prim[g] = d2; e.prim[g + N] = d3; e.prim[g + 2 * N] = d4; e.prim[g + 3 * N] = d5;
     e.p[g] = pp;
     e.mu[g] = mu;
-    if (!(q1 > (R)0) || !(pp > (R)0) || !(fabs((double)e.qa[g + 4 * N]) < 1e300)) bad = 1;
+    const R pabs = Freestream<R>::on ? (R)S.poo + pp : pp;
+    if (!(q1 > (R)0) || !(pabs > (R)0) || !(fabs((double)e.qa[g + 4 * N]) < 1e300)) bad = 1;
   }
   if (bad) atomicOr(&e.scal->flag, 1);
 }
@@ -637,12 +659,25 @@ __global__ void k_flux(Eng<R> e) {
     const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
     const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
     const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
-    const R r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
-    const R s1 = x1 * r1 + x2 * r2 + x3 * r3;
-    const R s2 = e1 * r1 + e2 * r2 + e3 * r3;
-    const R s3 = z1 * r1 + z2 * r2 + z3 * r3;
     const R pp = e.p[g];
-    {
+    R s1, s2, s3;
+    // freestream split: contravariant velocities of u and of umf apart
+    R su1 = 0, su2 = 0, su3 = 0, sm1 = 0, sm2 = 0, sm3 = 0;
+    if constexpr (Freestream<R>::on) {
+      const R r1 = e.prim[g], r2 = e.prim[g + N], r3 = e.prim[g + 2 * N];
+      su1 = x1 * r1 + x2 * r2 + x3 * r3; sm1 = x1 * u1 + x2 * u2 + x3 * u3;
+      su2 = e1 * r1 + e2 * r2 + e3 * r3; sm2 = e1 * u1 + e2 * u2 + e3 * u3;
+      su3 = z1 * r1 + z2 * r2 + z3 * r3; sm3 = z1 * u1 + z2 * u2 + z3 * u3;
+      s1 = su1 + sm1; s2 = su2 + sm2; s3 = su3 + sm3;
+      // rho U - rho_inf (umf . grad xi)
+      const double q1 = e.qa[g];
+      const R q = (R)q1, qp = (R)(q1 - S.rhooo);
+      F[g] = q * su1 + qp * sm1; F[g + N] = q * su2 + qp * sm2; F[g + 2 * N] = q * su3 + qp * sm3;
+    } else {
+      const R r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
+      s1 = x1 * r1 + x2 * r2 + x3 * r3;
+      s2 = e1 * r1 + e2 * r2 + e3 * r3;
+      s3 = z1 * r1 + z2 * r2 + z3 * r3;
       const R q = (R)e.qa[g];
       F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
     }
@@ -669,10 +704,20 @@ __global__ void k_flux(Eng<R> e) {
       F[g + ((m - 1) * 3 + 2) * N] = c;
     }
     {
-      const R d5 = (R)e.qa[g + 4 * N] + pp;
-      R a = d5 * s1 - pp * (u1 * x1 + u2 * x2 + u3 * x3);
-      R b = d5 * s2 - pp * (u1 * e1 + u2 * e2 + u3 * e3);
-      R c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
+      R a, b, c;
+      if constexpr (Freestream<R>::on) {
+        // (rhoE + p) U - p (umf . grad xi) - rhoE_inf (umf . grad xi)
+        const double q5 = e.qa[g + 4 * N];
+        const R d5 = (R)q5 + (R)S.poo + pp, re = (R)(q5 - S.hamm1 * S.poo);
+        a = d5 * su1 + re * sm1;
+        b = d5 * su2 + re * sm2;
+        c = d5 * su3 + re * sm3;
+      } else {
+        const R d5 = (R)e.qa[g + 4 * N] + pp;
+        a = d5 * s1 - pp * (u1 * x1 + u2 * x2 + u3 * x3);
+        b = d5 * s2 - pp * (u1 * e1 + u2 * e2 + u3 * e3);
+        c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
+      }
       if (visc) {
         const R ha = t[g + 6 * N], hb = t[g + 7 * N], hc = t[g + 8 * N];
         a = a - x1 * ha - x2 * hb - x3 * hc;
@@ -692,16 +737,36 @@ __global__ void k_div(Eng<R> e) {
   const int64_t N = e.N;
   const R ham = (R)S.ham;
   const R *F = e.flx;
+  R u1 = 0, u2 = 0, u3 = 0;
+  if constexpr (Freestream<R>::on) {
+    u1 = (R)e.scal->umf[1]; u2 = (R)e.scal->umf[2]; u3 = (R)e.scal->umf[3];
+  }
   GRID_STRIDE(g, N) {
     const R as = e.asz[g], bs = e.bsz[g];
     const bool sponge = as != (R)0 || bs != (R)0;
+    R fs[5] = {0, 0, 0, 0, 0};
+    if constexpr (Freestream<R>::on) {
+      // divergence of the freestream fluxes: rho_inf, p_inf, rhoE_inf times the metric divergence
+      const R g1 = e.gm[g], g2 = e.gm[g + N], g3 = e.gm[g + 2 * N];
+      const R ug = u1 * g1 + u2 * g2 + u3 * g3;
+      fs[0] = (R)S.rhooo * ug;
+      fs[1] = (R)S.poo * g1; fs[2] = (R)S.poo * g2; fs[3] = (R)S.poo * g3;
+      fs[4] = (R)(S.hamm1 * S.poo) * ug;
+    }
 #pragma unroll
     for (int m = 1; m <= 5; m++) {
       R d = F[g + ((m - 1) * 3 + 0) * N] + F[g + ((m - 1) * 3 + 1) * N] + F[g + ((m - 1) * 3 + 2) * N];
+      if constexpr (Freestream<R>::on) d = d + fs[m - 1];
       if (sponge) {
-        if (m == 1) d = d + as * ((R)e.qa[g] - (R)1);
-        else if (m <= 4) d = d + as * ((R)e.qa[g + (m - 1) * N] - (R)0);
-        else d = d + bs * (e.p[g] - ham * (R)1);
+        if constexpr (Freestream<R>::on) {  // the pressure plane already holds p - p_inf, p_inf = 1/gamma
+          if (m == 1) d = d + as * (R)(e.qa[g] - 1.0);
+          else if (m <= 4) d = d + as * (R)e.qa[g + (m - 1) * N];
+          else d = d + bs * e.p[g];
+        } else {
+          if (m == 1) d = d + as * ((R)e.qa[g] - (R)1);
+          else if (m <= 4) d = d + as * ((R)e.qa[g + (m - 1) * N] - (R)0);
+          else d = d + bs * (e.p[g] - ham * (R)1);
+        }
       }
       e.de[g + (m - 1) * N] = d;
     }
@@ -735,7 +800,8 @@ __device__ __forceinline__ void eleme(const Scheme &S, const Eng<R> &e, int64_t 
                                       Elem<R> &el) {
   const int64_t N = e.N;
   el.rhoi = (R)1 / (R)e.qa[g];
-  el.ao = sqrt((R)S.gam * el.rhoi * e.p[g]);
+  const R pabs = Freestream<R>::on ? (R)S.poo + e.p[g] : e.p[g];
+  el.ao = sqrt((R)S.gam * el.rhoi * pabs);
   el.aoi = (R)1 / el.ao;
   el.ve[0] = el.rhoi * (R)e.qa[g + N];
   el.ve[1] = el.rhoi * (R)e.qa[g + 2 * N];
@@ -836,10 +902,22 @@ __global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
   eleme(S, e, g, cm, umf, el);
   R xt[5][5];
   xtq2r(S, el, cm, xt);
-  R v[5];
+  R v[5], dinf[5] = {0, 0, 0, 0, 0};
+  if constexpr (Freestream<R>::on) {
+    // normal derivative of the freestream fluxes at the line end (from the metric derivative)
+    const R *dm = e.drvm + B.face_off[nn] * 10;
+    const R m1 = dm[jk + nbs * (0 + 5 * ip)], m2 = dm[jk + nbs * (1 + 5 * ip)], m3 = dm[jk + nbs * (2 + 5 * ip)];
+    const R ug = umf[1] * m1 + umf[2] * m2 + umf[3] * m3;
+    dinf[0] = (R)S.rhooo * ug;
+    dinf[1] = (R)S.poo * m1; dinf[2] = (R)S.poo * m2; dinf[3] = (R)S.poo * m3;
+    dinf[4] = (R)(S.hamm1 * S.poo) * ug;
+  }
   const R yac = e.yaco[g];
 #pragma unroll
-  for (int q = 0; q < 5; q++) v[q] = yac * (ra0 * drva[jk + nbs * (q + 5 * ip)] + ra1 * e.de[g + q * N]);
+  for (int q = 0; q < 5; q++) {
+    if constexpr (Freestream<R>::on) v[q] = yac * (ra0 * (drva[jk + nbs * (q + 5 * ip)] + dinf[q]) + ra1 * e.de[g + q * N]);
+    else v[q] = yac * (ra0 * drva[jk + nbs * (q + 5 * ip)] + ra1 * e.de[g + q * N]);
+  }
 #pragma unroll
   for (int r = 0; r < 5; r++) {
     R s = 0;
@@ -1115,7 +1193,8 @@ __global__ void k_forces(Eng<R> e, const FaceTask *tasks, const double *area, co
     const int64_t g = B.off + ((int64_t)kk * (B.let + 1) + jw) * (B.lxi + 1) + ii;
     const double w1 = wn[ll], w2 = wn[ll + nw], w3 = wn[ll + 2 * nw];
     for (int dir = 0; dir < 2; dir++) {
-      double v = (double)e.p[g] * (dir == 0 ? w1 : w2) * ar[ll];
+      const double pw = Freestream<R>::on ? (double)e.p[g] + e.sc->poo : (double)e.p[g];
+      double v = pw * (dir == 0 ? w1 : w2) * ar[ll];
       if (e.sc->nviscous == 1) {
         const R *t = e.tau;
         double tw;
@@ -1140,6 +1219,16 @@ __global__ void k_forces(Eng<R> e, const FaceTask *tasks, const double *area, co
   if (threadIdx.x == 0) {
     out[blockIdx.x * 2 + 0] = sh[0][0];
     out[blockIdx.x * 2 + 1] = sh[1][0];
+  }
+}
+
+// metric divergence of the mixed path: gm(k) = D_xi(xim_k) + D_eta(etm_k) +
+// D_zeta(zem_k), from three FP64 derivative sets d3 (planes 0-2: xi, 3-5: eta,
+// 6-8: zeta), rounded once to FP32
+__global__ void k_metric_div(const double *d3, int64_t N, float *gm) {
+  GRID_STRIDE(g, N) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) gm[g + k * N] = (float)(d3[g + k * N] + d3[g + (3 + k) * N] + d3[g + (6 + k) * N]);
   }
 }
 
@@ -1192,11 +1281,11 @@ void sweep_ddf(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const Sw
 
 template <typename TI, typename TC>
 static void mpigo_t(const Eng<TC> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
-                    const TI *s1, const TI *s2, const TI *s3, int64_t fs, int nf) {
+                    const TI *s1, const TI *s2, const TI *s3, int64_t fs, int nf, const FieldOfs<TI> &fo = {}) {
   if (ntask == 0 || nf == 0) return;
   const int tpb = 128;
   k_mpigo<TI, TC><<<dim3((maxline + tpb - 1) / tpb, ntask, nf), tpb, 0, st>>>(e.blk, e.cf, tasks, nt, n45, s1, s2, s3,
-                                                                              fs, e.recv, e.F * 6);
+                                                                              fs, e.recv, e.F * 6, fo);
 }
 void mpigo_ddd(const Eng<double> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
                const double *s1, const double *s2, const double *s3, int64_t fs, int nf) {
@@ -1207,8 +1296,8 @@ void mpigo_fff(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int 
   mpigo_t<float, float>(e, st, tasks, ntask, maxline, nt, n45, s1, s2, s3, fs, nf);
 }
 void mpigo_ddf(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt, int n45,
-               const double *s1, const double *s2, const double *s3, int64_t fs, int nf) {
-  mpigo_t<double, float>(e, st, tasks, ntask, maxline, nt, n45, s1, s2, s3, fs, nf);
+               const double *s1, const double *s2, const double *s3, int64_t fs, int nf, const FieldOfs<double> &ofs) {
+  mpigo_t<double, float>(e, st, tasks, ntask, maxline, nt, n45, s1, s2, s3, fs, nf, ofs);
 }
 
 static int pw_grid(int64_t N) {
@@ -1253,6 +1342,10 @@ void face_f(const Eng<float> &e, cudaStream_t st, int which, const FaceTask *tas
     case FK_GCBC_APPLY: k_gcbc_apply<float><<<grid, tpb, 0, st>>>(e, tasks); break;
     default: break;  // wall, pack and averaging act on the FP64 state: face_d
   }
+}
+
+void metric_divergence(const Eng<double> &e, cudaStream_t st, const double *d3, float *gm) {
+  k_metric_div<<<pw_grid(e.N), 256, 0, st>>>(d3, e.N, gm);
 }
 
 void junction(const Eng<double> &e, cudaStream_t st, const JunctionDev *jn, int njct, int nk) {

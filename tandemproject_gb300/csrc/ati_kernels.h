@@ -48,6 +48,22 @@ struct Eng {
   const R *cm;
   const R *facd, *facf, *sbcc, *rpex;
   int64_t F;            // face index count (face buffers of one field: 6*F for recv)
+  // mixed path only (the fluxes there are taken relative to the freestream):
+  const R *gm;          // metric divergence sum_d D_d(metric_d) per component (3 planes)
+  const R *drvm;        // its line-end values per direction, drva layout (components 0..2)
+};
+
+// The mixed path (R = float) works on deviations from the freestream
+// (rho = 1, u = 0, p = 1/gamma): the pressure plane holds p - p_inf, the
+// fluxes drop their freestream part, whose divergence is added back from the
+// FP64 metric divergence gm.  Constants of that split:
+template <typename R>
+struct Freestream {
+  static constexpr bool on = false;
+};
+template <>
+struct Freestream<float> {
+  static constexpr bool on = true;
 };
 
 enum { PW_PRIM, PW_CFL, PW_VISC, PW_FLUX, PW_DIV, PW_RK };
@@ -57,7 +73,9 @@ enum { SC_MOVEF_A, SC_CFL_RESET, SC_DT_NEW, SC_DT, SC_MOVEF_B, SC_ADVANCE, SC_IN
 // One line sweep over every block: nf fields, field f reads in + f*in_fs and
 // writes out + f*out_fs (out2 + f*out_fs too when out2 is set); recv holds the
 // closure of field f at recv + f*6*F; a derivative writes its line-end values
-// to drva component m0 + f when drva is set.
+// to drva component m0 + f when drva is set.  When the input is wider than the
+// compute type, field f is converted as (in - ofs[f]) (a constant the
+// operator annihilates, removed before rounding).
 template <typename TI, typename TO>
 struct SweepIO {
   const TI *in;
@@ -67,6 +85,13 @@ struct SweepIO {
   TO *out2;
   int nf, m0;
   bool drva;
+  TI ofs[5];
+};
+
+// per-field offsets of a closure (mpigo) over a wider input type
+template <typename TI>
+struct FieldOfs {
+  TI v[5];
 };
 
 // Launchers, declared once per arithmetic mode: ati::fast (FMA contraction)
@@ -85,7 +110,9 @@ struct SweepIO {
   void mpigo_fff(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,       \
                  int n45, const float *s1, const float *s2, const float *s3, int64_t fs, int nf);                 \
   void mpigo_ddf(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,       \
-                 int n45, const double *s1, const double *s2, const double *s3, int64_t fs, int nf);              \
+                 int n45, const double *s1, const double *s2, const double *s3, int64_t fs, int nf,               \
+                 const FieldOfs<double> &ofs);                                                                     \
+  void metric_divergence(const Eng<double> &e, cudaStream_t st, const double *d3, float *gm);                     \
   void pointwise_d(const Eng<double> &e, cudaStream_t st, int which);                                             \
   void pointwise_f(const Eng<float> &e, cudaStream_t st, int which);                                              \
   void face_d(const Eng<double> &e, cudaStream_t st, int which, const FaceTask *tasks, int ntask, int maxline);    \

@@ -1,6 +1,7 @@
 """Mixed precision (ATI_MIXED): line solves, filters and fluxes in FP32, FP64
-metrics, Jacobian and RK state.  Errors are measured against the FP64 path,
-which itself matches the CPU restatement to ~1e-14 after 100 steps."""
+metrics, Jacobian and RK state, fluxes taken relative to the freestream.
+Errors are measured against the FP64 path, which itself matches the CPU
+restatement to ~1e-14 after 100 steps."""
 import numpy as np
 import pytest
 
@@ -8,14 +9,17 @@ pytestmark = pytest.mark.gpu
 
 
 def state_rel_l2(a, b, nb=6):
+    """Relative L2 per conserved variable (momentum components share the
+    momentum-vector norm) and of the whole state."""
     num = np.zeros(5)
     den = np.zeros(5)
     for mb in range(nb):
         qa, qb = a.get_state(mb), b.get_state(mb)
         num += np.sum((qa - qb) ** 2, axis=1)
         den += np.sum(qb ** 2, axis=1)
+    whole = np.sqrt(num.sum() / den.sum())
     den[1:4] = den[1:4].sum()
-    return np.sqrt(num / den)
+    return np.sqrt(num / den), whole
 
 
 def make(cfg):
@@ -23,25 +27,38 @@ def make(cfg):
     return setup_case(cfg)
 
 
-def test_mixed_tracks_fp64(ati_lib):
+def test_mixed_tracks_fp64_1000_steps(ati_lib):
+    """1000 RK4 steps of the 0.61 M-point NACA 0012 case from the reference
+    deck's smooth start (nsmf = 0; timf = 1 so the flow develops within the run)."""
+    from tandemproject_gb300.config import MIXED, PRESETS
+    cfg = PRESETS["naca0012_0p6m"].replace(nsmf=0, timf=1.0)
+    d = make(cfg)
+    m = make(cfg.replace(precision=MIXED))
+    d.step(1000)
+    m.step(1000)
+    e, whole = state_rel_l2(m, d)
+    print("mixed vs fp64 after 1000 steps: per variable", e, "whole state", whole)
+    assert e[0] < 1e-6 and e[4] < 1e-6 and whole < 1e-6
+    assert np.all(e[1:4] < 1e-4)  # momentum starts from rest: its norm is small
+    td, tm = d.get_time(), m.get_time()
+    assert td[0] == tm[0] and abs(td[2] - tm[2]) < 1e-6 * td[2]
+    fd, fm = d.forces(), m.forces()
+    print("forces fp64", fd, "mixed", fm)
+    assert abs(fd[0] - fm[0]) < 1e-4 * abs(fd[0])
+
+
+def test_mixed_impulsive_start_tracks_fp64(ati_lib):
+    """The impulsive start (nsmf = 1) is the harsher transient."""
     from tandemproject_gb300.config import MIXED, small_case
     cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,))
     d = make(cfg)
     m = make(cfg.replace(precision=MIXED))
-    d.step(2)
-    m.step(2)
-    e2 = state_rel_l2(m, d)
-    d.step(98)
-    m.step(98)
-    e100 = state_rel_l2(m, d)
-    print("mixed vs fp64 rel L2 after 2 steps", e2, "after 100 steps", e100)
-    assert np.all(e2 < 1e-6)
-    assert np.all(e100 < 1e-5)
-    td, tm = d.get_time(), m.get_time()
-    assert td[0] == tm[0] and abs(td[2] - tm[2]) < 1e-5 * td[2]
-    fd, fm = d.forces(), m.forces()
-    print("forces fp64", fd, "mixed", fm)
-    assert np.allclose(fd, fm, rtol=1e-3, atol=1e-6)
+    d.step(100)
+    m.step(100)
+    e, whole = state_rel_l2(m, d)
+    print("impulsive start, mixed vs fp64 after 100 steps", e, whole)
+    assert e[0] < 2e-6 and e[4] < 2e-6 and whole < 2e-6
+    assert np.all(e[1:4] < 1e-4)
 
 
 def test_mixed_filter_step_matches_fp64_closely(ati_lib):
@@ -62,5 +79,18 @@ def test_mixed_filter_step_matches_fp64_closely(ati_lib):
         m.set_state(mb, q)
     d.filter_step()
     m.filter_step()
-    e = state_rel_l2(m, d)
+    e, whole = state_rel_l2(m, d)
     assert np.all(e < 1e-7), e
+
+
+def test_mixed_pressure_field_is_absolute(ati_lib):
+    """The mixed engine keeps p - p_inf internally; ati_get_field returns p."""
+    from tandemproject_gb300.config import MIXED, small_case
+    cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,))
+    d = make(cfg)
+    m = make(cfg.replace(precision=MIXED))
+    d.step(3)
+    m.step(3)
+    from tandemproject_gb300.solver import F_P
+    pd, pm = d.get_field(0, F_P), m.get_field(0, F_P)
+    assert np.allclose(pd, pm, rtol=1e-6, atol=0)
