@@ -38,10 +38,23 @@ METRIC = "grid-pt-stage updates/s FP64 vs mixed (rel L2 ≤1e-6); p50/p99 solve 
 UNIT = "grid-pt-stage updates/s"
 L2_BYTES = 129 * 2 ** 20
 
-# algorithmic work per point of one line-sweep launch (one input plane read,
-# one output plane written; flops of the 7-point RHS + forward + backward pass)
+# algorithmic work per unit of a line-sweep launch, a unit being one point of
+# one field (one input value read, one output value written; flops of the
+# 7-point RHS + forward + backward pass).  A launch sweeps every line of one
+# direction over all blocks for several fields at once.
 SWEEP_BYTES = {"deriv": 16, "filter": 16}
 SWEEP_FLOPS = {"deriv": 17, "filter": 22}
+# the mixed path: FP32 derivative sweeps (4 B in, 4 B out); the filter reads
+# and writes the FP64 state
+SWEEP_BYTES_MIXED = {"deriv": 8, "filter": 16}
+# fields swept per direction per time step: 4 viscous gradients + 5 fluxes in
+# each of the 4 stages, or the 5 variables once for the filter
+FIELD_SWEEPS_PER_STEP = {"deriv": 4 * (4 + 5), "filter": 5}
+# DRAM bytes per unit of the FP64 xi derivative sweep measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum of one 5-field launch on the
+# 3.54 M-point case: 489.35 MB for 17.69 M units); the kernel streams, so the
+# traffic of a launch scales with the units it processes
+SWEEP_TRAFFIC_PER_UNIT = {"deriv_xi": 489.35e6 / (5 * 3538944)}
 # canonical bytes per grid-point-stage of the whole stage: 141 FP64 words, or
 # the mixed data flow with FP32 intermediates and FP64 state/metrics
 STAGE_BYTES_FP64 = 1128
@@ -270,6 +283,17 @@ def main():
         cm.profile(False)
         cm.close()
         mtot = sum(v[0] for v in mprof.values())
+        mdom = max(mprof, key=lambda k: mprof[k][0])
+        mkind = "filter" if mdom.startswith("filter") else "deriv"
+        if mdom.startswith(("deriv", "filter")):
+            munits = npts * FIELD_SWEEPS_PER_STEP[mkind] * 2 / max(mprof[mdom][1], 1)
+            mt = mprof[mdom][0] / max(mprof[mdom][1], 1) / 1e3
+            mach = SWEEP_BYTES_MIXED[mkind] * munits / mt / 1e9
+            mroof = {"bound": "hbm", "kernel": f"k_sweep<{mdom}> in FP32, {SWEEP_BYTES_MIXED[mkind]} B per point-field",
+                     "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
+                     "frac": mach / measured_peaks()[0]}
+        else:
+            mroof = {"kernel": mdom, "note": "dominant class is not a line sweep"}
         mixed = {"value": npts * cfg.nkrk * args.steps * ws / t_mix, "ms_per_step": t_mix / args.steps * 1e3,
                  "dtype": "f32 line solves/filters/fluxes, f64 metrics, Jacobian and RK state",
                  "speedup_vs_fp64": (npts * cfg.nkrk * args.steps * ws / t_mix) / value,
@@ -279,6 +303,7 @@ def main():
                                                 "rhoE": float(np.sqrt(num[4] / den[4]))},
                  "stage_hbm_frac_728B": STAGE_BYTES_MIXED * (npts * cfg.nkrk * args.steps / t_mix) / 1e9
                  / measured_peaks()[0],
+                 "roofline": mroof,
                  "kernel_share": {k: round(v[0] / mtot, 4) for k, v in mprof.items() if v[1]}}
 
     # end to end through the C ABI: pinned host state in, step, state out
@@ -314,13 +339,19 @@ def main():
     dom_ms, dom_n = prof[dom]
     kind = "filter" if dom.startswith("filter") else "deriv"
     hbm_peak, peak_src = measured_peaks()
+    # units (point x field) one launch of this class processes, on average over the profiled steps
+    units = npts * FIELD_SWEEPS_PER_STEP[kind] * 2 / max(dom_n, 1)
     t_launch = dom_ms / max(dom_n, 1) / 1e3
-    achieved = SWEEP_BYTES[kind] * npts / t_launch / 1e9
+    achieved = SWEEP_BYTES[kind] * units / t_launch / 1e9
     fp64_peak = probe_fma_tflops(True)
-    fp64_ach = SWEEP_FLOPS[kind] * npts / t_launch / 1e12
+    fp64_ach = SWEEP_FLOPS[kind] * units / t_launch / 1e12
+    traffic = SWEEP_TRAFFIC_PER_UNIT[dom] * units if dom in SWEEP_TRAFFIC_PER_UNIT else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": None, "kernel": f"k_sweep<{dom}> (one launch = every line of one direction over all "
-                                            f"blocks, {SWEEP_BYTES[kind]} B and {SWEEP_FLOPS[kind]} flop per point)",
+                "traffic": traffic,
+                "traffic_source": "ncu DRAM bytes per unit of one launch on the 3.54 M-point case, scaled by units",
+                "kernel": f"k_sweep<{dom}>: one launch = every line of one direction over all blocks for "
+                          f"{units / npts:.1f} fields on average ({units:.3e} point-fields), "
+                          f"{SWEEP_BYTES[kind]} B and {SWEEP_FLOPS[kind]} flop per point-field",
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
                          "peak_source": "measured FP64 FMA throughput of this GPU (ati_probe_fma_tflops)"},

@@ -71,7 +71,9 @@ extern "C" {
 #define ATI_F_YACO 9  /* yaco [1] Jacobian J = 3 / sum(...)                       */
 #define ATI_F_STRESS 10 /* [9] txx,tyy,tzz,txy,tyz,tzx,hxx,hyy,hzz              */
 #define ATI_F_SPONGE 11 /* [2] dense sponge coefficients asz, bsz (0 outside)    */
-#define ATI_NFIELDS 12
+#define ATI_F_CP 12   /* [1] derived, ati_get_field only: pressure coefficient of the
+                         current qa, (p - p_inf) * 2 / M^2 (getCp, src/rptPost.f90:1456-1465) */
+#define ATI_NFIELDS 13
 
 /* ---- face buffers: drva/drvb/recv/cm (src/MainVar3D.f90:96-102) --------
  * Layout as in the reference: buf(0:nbsize(nn)-1, ncomp, 0:1), face index
@@ -247,6 +249,40 @@ int ati_deriv_lines_noalloc(const double *in, double *out, int64_t nlines, int32
  * (src/rpt.f90:1017-1056), from the p and stresses of the last stage:
  * out[0] = force coefficient along x, out[1] = along y. */
 int ati_forces(ati_handle_t *h, double out[2]);
+
+/* ---- outputs and on-disk formats ---------------------------------------- */
+/* The configuration the handle was created with. */
+int ati_get_config(ati_handle_t *h, ati_config_t *cfg);
+/* Moving-frame velocity umf(1:3) and angle of attack aoa (degrees) of the
+ * current time (movef / pitch, src/Subroutineso.f90:192-259). */
+int ati_get_frame(ati_handle_t *h, double umf[3], double *aoa);
+
+/* Surface-pressure recorder (no counterpart in the reference, which writes
+ * whole fields at intervals): with capacity > 0, every time step ends with one
+ * record of the static pressure, from the new qa in FP64, on the mid-span line
+ * (k = lze/2, i = 0..lxi) of every wall face (BC 20/25, the order of
+ * ati_forces), into a device ring buffer of `capacity` records; capacity 0
+ * turns it off.  ati_wall_probe_read copies the last min(steps, capacity)
+ * records, oldest first: p[r*npts + i] and the time t[r] of record r; with
+ * p == NULL it only returns nrec and npts. */
+int ati_wall_probe_enable(ati_handle_t *h, int capacity);
+int ati_wall_probe_read(ati_handle_t *h, double *p, double *t, int64_t *nrec, int64_t *npts);
+
+/* Restart file of block blk in the layout of wrRsta (src/rpt.f90:555-621,
+ * one block per file, npc = 1): six 8-byte header slots -- n and ndt as int32
+ * in the first 4 bytes of their slot, then dt, dts, dte, timo as float64 --
+ * followed by qa(0:lmx,1:5) as float64, native byte order. */
+int ati_write_restart(ati_handle_t *h, int blk, const char *path);
+/* rdRsta (src/rpt.f90:626-668): the header sets the time scalars, the body
+ * the state of block blk. */
+int ati_read_restart(ati_handle_t *h, int blk, const char *path);
+/* Plot3D multi-block files as wrP3dG and wrP3dS write them with mblk = 1
+ * (src/rpt.f90:246-330 and 115-241): int32 block count, int32
+ * (IMax, JMax, KMax) per block, then per block x, y, z as float32 (grid), or
+ * Mach, AoA, Re, time followed by rho, u, v, w, p as float32 (solution; the
+ * velocities rho u / rho + umf, p the pressure of the last stage). */
+int ati_write_plot3d_grid(ati_handle_t *h, const char *path);
+int ati_write_plot3d_solution(ati_handle_t *h, const char *path);
 
 #ifdef __cplusplus
 }

@@ -28,6 +28,7 @@ SOURCES = [
     ("ati_scheme.cpp", "ati_scheme.o", []),
     ("ati_probe.cu", "ati_probe.o", []),
     ("ati_noalloc.cu", "ati_noalloc.o", ["-fmad=false"]),
+    ("ati_io.cpp", "ati_io.o", []),
 ]
 
 

@@ -78,10 +78,18 @@ struct ati_handle {
   std::vector<Ev> ev_used, ev_free;
   double prof_ms[ATI_K_NSLOTS] = {0};
   int64_t prof_n[ATI_K_NSLOTS] = {0};
+  // surface-pressure recorder (ring buffer of wall pressure on the mid-span lines)
+  int probe_cap = 0;
+  int64_t probe_npts = 0, probe_n0 = 0;
+  double *probe_p = nullptr, *probe_t = nullptr;
 };
 
 // error text for calls that have no handle (ati_last_error(NULL))
 void ati_set_thread_error(const char *msg) { g_create_err = msg ? msg : ""; }
+void ati_set_handle_error(ati_handle_t *h, const char *msg) {
+  if (h) h->err = msg ? msg : "";
+  else g_create_err = msg ? msg : "";
+}
 
 static int fail(ati_handle *h, int code, const std::string &msg) {
   if (h) h->err = msg;
@@ -288,6 +296,41 @@ __global__ void k_to_float(const double *src, float *dst, int64_t n) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     dst[g] = (float)src[g];
 }
+// pressure coefficient of the current qa (getCp, src/rptPost.f90:1456-1465)
+__global__ void k_cp(Eng<double> c, double *cp) {
+  const Scheme &S = *c.sc;
+  const int64_t N = c.N;
+  const double ra0 = 2.0 / (S.amachoo * S.amachoo);
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+    const double q1 = c.qa[g], q2 = c.qa[g + N], q3 = c.qa[g + 2 * N], q4 = c.qa[g + 3 * N];
+    const double pp = S.gamm1 * (c.qa[g + 4 * N] - 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
+    cp[g] = (pp - S.poo) * ra0;
+  }
+}
+
+// one record of the wall pressure (FP64, from qa) on the mid-span line of every
+// wall face; record slot (n - n0 - 1) mod cap, n = steps done (already advanced)
+__global__ void k_wall_probe(Eng<double> c, const FaceTask *tasks, int ntask, int64_t n0, int cap, int64_t npts,
+                             double *pbuf, double *tbuf) {
+  const Scheme &S = *c.sc;
+  const int64_t N = c.N;
+  const int64_t r = (c.scal->n - n0 - 1) % cap;
+  int64_t base = 0;
+  for (int q = 0; q < ntask; q++) {
+    const FaceTask T = tasks[q];
+    const BlockDev &B = c.blk[T.b];
+    const int nx = B.lxi + 1;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx; i += gridDim.x * blockDim.x) {
+      const int j = T.ip * B.let, k = B.lze / 2;
+      const int64_t g = B.off + ((int64_t)k * (B.let + 1) + j) * nx + i;
+      const double q1 = c.qa[g], q2 = c.qa[g + N], q3 = c.qa[g + 2 * N], q4 = c.qa[g + 3 * N];
+      pbuf[r * npts + base + i] = S.gamm1 * (c.qa[g + 4 * N] - 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
+    }
+    base += nx;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) tbuf[r] = c.scal->timo;
+}
+
 __global__ void k_to_double(const float *src, double *dst, int64_t n, double add) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     dst[g] = (double)src[g] + add;
@@ -607,6 +650,13 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
   return ATI_OK;
 }
 
+static void probe_free(ati_handle *h) {
+  if (h->probe_p) cudaFree(h->probe_p);
+  if (h->probe_t) cudaFree(h->probe_t);
+  h->probe_p = h->probe_t = nullptr;
+  h->probe_cap = 0;
+}
+
 static void drop_graphs(ati_handle *h) {
   for (auto &g : h->gexec)
     if (g) {
@@ -624,6 +674,7 @@ extern "C" int ati_destroy(ati_handle_t *h) {
     cudaEventDestroy(e.b);
   }
   drop_graphs(h);
+  probe_free(h);
   if (h->arena) cudaFree(h->arena);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
@@ -662,6 +713,7 @@ static double *field_base(ati_handle *h, int field, int &ncomp, const float **f3
     case ATI_F_YACO: ncomp = 1; return const_cast<double *>(c.yaco);
     case ATI_F_STRESS: ncomp = 9; if (h->mixed) *f32 = h->ef.tau; return c.tau;
     case ATI_F_SPONGE: ncomp = 2; return const_cast<double *>(c.asz);  // asz and bsz are adjacent planes
+    case ATI_F_CP: ncomp = 1; return h->fw1;  // derived into the granular scratch plane by copy_field
     default: ncomp = 0; return nullptr;
   }
 }
@@ -674,6 +726,12 @@ static int copy_field(ati_handle *h, int blk, int field, double *host, bool to_d
   if (!base) return fail(h, ATI_EINVAL, "unknown field id");
   const BlockDev &B = h->blk[blk];
   const size_t w = (size_t)B.npts * sizeof(double), dp = (size_t)h->N * sizeof(double);
+  if (field == ATI_F_CP) {
+    if (to_dev) return fail(h, ATI_EINVAL, "ATI_F_CP is derived: ati_get_field only");
+    if (!h->inited) return fail(h, ATI_ESTATE, "ATI_F_CP needs ati_init");
+    k_cp<<<256, 256, 0, h->st>>>(h->ed, base);
+    CKL();
+  }
   if (to_dev) {
     CK(cudaMemcpy2DAsync(base + B.off, dp, host, w, w, nc, cudaMemcpyHostToDevice, h->st));
   } else {
@@ -1017,6 +1075,11 @@ static int one_step(ati_handle *h) {
   if (rc) return rc;
   const bool strict = h->cfg.precision == ATI_FP64_STRICT;
   PROF(h, ATI_K_SCALAR, (strict ? strict::scalar : fast::scalar)(h->ed, h->st, SC_ADVANCE, 0));
+  if (h->probe_cap > 0 && h->tl_force.n) {
+    h->launches++;
+    k_wall_probe<<<1, 256, 0, h->st>>>(h->ed, tp(h, h->tl_force), h->tl_force.n, h->probe_n0, h->probe_cap,
+                                       h->probe_npts, h->probe_p, h->probe_t);
+  }
   CKL();
   return ATI_OK;
 }
@@ -1100,6 +1163,67 @@ extern "C" int ati_forces(ati_handle_t *h, double out[2]) {
     out[0] = out[0] + part[2 * q] * dynp;
     out[1] = out[1] + part[2 * q + 1] * dynp;
   }
+  return ATI_OK;
+}
+
+extern "C" int ati_get_config(ati_handle_t *h, ati_config_t *cfg) {
+  if (!h || !cfg) return fail(h, ATI_EINVAL, "ati_get_config: bad argument");
+  *cfg = h->cfg;
+  return ATI_OK;
+}
+
+extern "C" int ati_get_frame(ati_handle_t *h, double umf[3], double *aoa) {
+  if (!h || !umf || !aoa) return fail(h, ATI_EINVAL, "ati_get_frame: bad argument");
+  Scalars sc;
+  CK(cudaMemcpyAsync(&sc, h->ed.scal, sizeof(sc), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int q = 0; q < 3; q++) umf[q] = sc.umf[q + 1];
+  *aoa = sc.aoa;
+  return ATI_OK;
+}
+
+// ---- surface-pressure recorder ----------------------------------------------------
+
+extern "C" int ati_wall_probe_enable(ati_handle_t *h, int capacity) {
+  if (!h || capacity < 0) return fail(h, ATI_EINVAL, "ati_wall_probe_enable: bad argument");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  CK(cudaStreamSynchronize(h->st));
+  probe_free(h);
+  drop_graphs(h);  // the step graphs hold (or lack) the recording kernel
+  if (capacity == 0) return ATI_OK;
+  int64_t npts = 0;
+  for (int q = 0; q < h->tl_force.n; q++) npts += h->blk[h->htasks[h->tl_force.off + q].b].lxi + 1;
+  if (npts == 0) return fail(h, ATI_EINVAL, "ati_wall_probe_enable: the case has no wall face");
+  if (cudaMalloc(&h->probe_p, sizeof(double) * npts * capacity) != cudaSuccess ||
+      cudaMalloc(&h->probe_t, sizeof(double) * capacity) != cudaSuccess) {
+    cudaGetLastError();
+    probe_free(h);
+    return fail(h, ATI_ENOMEM, "ati_wall_probe_enable: device allocation failed");
+  }
+  h->probe_cap = capacity;
+  h->probe_npts = npts;
+  h->probe_n0 = h->n_host;
+  return ATI_OK;
+}
+
+extern "C" int ati_wall_probe_read(ati_handle_t *h, double *p, double *t, int64_t *nrec, int64_t *npts) {
+  if (!h || !nrec || !npts) return fail(h, ATI_EINVAL, "ati_wall_probe_read: bad argument");
+  if (h->probe_cap == 0) return fail(h, ATI_ESTATE, "ati_wall_probe_read: recorder not enabled");
+  const int64_t done = h->n_host - h->probe_n0, cap = h->probe_cap;
+  const int64_t nr = done < cap ? done : cap;
+  *nrec = nr;
+  *npts = h->probe_npts;
+  if (!p) return ATI_OK;
+  // oldest record kept sits at slot (done - nr) mod cap: at most two contiguous runs
+  const int64_t s0 = (done - nr) % cap, run1 = nr < cap - s0 ? nr : cap - s0, np = h->probe_npts;
+  CK(cudaMemcpyAsync(p, h->probe_p + s0 * np, sizeof(double) * np * run1, cudaMemcpyDeviceToHost, h->st));
+  if (nr > run1)
+    CK(cudaMemcpyAsync(p + run1 * np, h->probe_p, sizeof(double) * np * (nr - run1), cudaMemcpyDeviceToHost, h->st));
+  if (t) {
+    CK(cudaMemcpyAsync(t, h->probe_t + s0, sizeof(double) * run1, cudaMemcpyDeviceToHost, h->st));
+    if (nr > run1) CK(cudaMemcpyAsync(t + run1, h->probe_t, sizeof(double) * (nr - run1), cudaMemcpyDeviceToHost, h->st));
+  }
+  CK(cudaStreamSynchronize(h->st));
   return ATI_OK;
 }
 

@@ -25,10 +25,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libati.so")
 
 ATI_OK, ATI_EINVAL, ATI_ENOMEM, ATI_ECUDA, ATI_ENONFINITE, ATI_ETIMEDOUT, ATI_ESTATE = range(7)
-F_QA, F_QO, F_DE, F_RR, F_SS, F_XIM, F_ETM, F_ZEM, F_P, F_YACO, F_STRESS, F_SPONGE = range(12)
+F_QA, F_QO, F_DE, F_RR, F_SS, F_XIM, F_ETM, F_ZEM, F_P, F_YACO, F_STRESS, F_SPONGE, F_CP = range(13)
 FACE_DRVA, FACE_DRVB, FACE_RECV, FACE_CM = range(4)
 NCOMP = {F_QA: 5, F_QO: 5, F_DE: 5, F_RR: 3, F_SS: 3, F_XIM: 3, F_ETM: 3, F_ZEM: 3, F_P: 1, F_YACO: 1,
-         F_STRESS: 9, F_SPONGE: 2}
+         F_STRESS: 9, F_SPONGE: 2, F_CP: 1}
 
 # every entry point declared in include/ati.h, with its ctypes signature
 _vp, _i32, _dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
@@ -61,6 +61,14 @@ SIGNATURES = {
     "ati_stream": ([_vp], ctypes.c_void_p),
     "ati_probe_fma_tflops": ([_i32, _dp], ctypes.c_int),
     "ati_deriv_lines_noalloc": ([_vp, _vp, ctypes.c_int64, ctypes.c_int32, _vp], ctypes.c_int),
+    "ati_get_config": ([_vp, _vp], ctypes.c_int),
+    "ati_get_frame": ([_vp, _dp, _dp], ctypes.c_int),
+    "ati_wall_probe_enable": ([_vp, _i32], ctypes.c_int),
+    "ati_wall_probe_read": ([_vp, _dp, _dp, _vp, _vp], ctypes.c_int),
+    "ati_write_restart": ([_vp, _i32, ctypes.c_char_p], ctypes.c_int),
+    "ati_read_restart": ([_vp, _i32, ctypes.c_char_p], ctypes.c_int),
+    "ati_write_plot3d_grid": ([_vp, ctypes.c_char_p], ctypes.c_int),
+    "ati_write_plot3d_solution": ([_vp, ctypes.c_char_p], ctypes.c_int),
 }
 
 KERNEL_CLASSES = ["deriv_xi", "deriv_eta", "deriv_zeta", "filter_xi", "filter_eta", "filter_zeta", "mpigo",
@@ -229,6 +237,43 @@ class Case:
         out = np.zeros(2)
         self._chk(self.L.ati_forces(self.h, _dp_of(out)))
         return out
+
+    # -- outputs and files
+    def cp(self, mb):
+        """Pressure coefficient of the current state (getCp, src/rptPost.f90:1456-1465)."""
+        return self.get_field(mb, F_CP)[0]
+
+    def frame(self):
+        """(umf[3], aoa in degrees) of the current time."""
+        u = np.zeros(3)
+        a = ctypes.c_double()
+        self._chk(self.L.ati_get_frame(self.h, _dp_of(u), ctypes.byref(a)))
+        return u, a.value
+
+    def wall_probe(self, capacity):
+        """Record the mid-span wall pressure every step (capacity records, 0 = off)."""
+        self._chk(self.L.ati_wall_probe_enable(self.h, int(capacity)))
+
+    def wall_probe_read(self):
+        """(times[nrec], p[nrec, npts]) of the recorded steps, oldest first."""
+        nr, npt = ctypes.c_int64(), ctypes.c_int64()
+        self._chk(self.L.ati_wall_probe_read(self.h, None, None, ctypes.byref(nr), ctypes.byref(npt)))
+        p = np.empty((nr.value, npt.value))
+        t = np.empty(nr.value)
+        self._chk(self.L.ati_wall_probe_read(self.h, _dp_of(p), _dp_of(t), ctypes.byref(nr), ctypes.byref(npt)))
+        return t, p
+
+    def write_restart(self, mb, path):
+        self._chk(self.L.ati_write_restart(self.h, mb, os.fsencode(path)))
+
+    def read_restart(self, mb, path):
+        self._chk(self.L.ati_read_restart(self.h, mb, os.fsencode(path)))
+
+    def write_plot3d_grid(self, path):
+        self._chk(self.L.ati_write_plot3d_grid(self.h, os.fsencode(path)))
+
+    def write_plot3d_solution(self, path):
+        self._chk(self.L.ati_write_plot3d_solution(self.h, os.fsencode(path)))
 
 
 def probe_fma_tflops(fp64=True):
