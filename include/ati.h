@@ -136,6 +136,23 @@ typedef struct ati_handle ati_handle_t;
 /* Allocate all device arrays of one case (src/Main3D.f90:270-291) and build
  * the scheme coefficients (penta, fcbcm, fcint, sbcco: src/Main3D.f90:295-332). */
 int ati_create(const ati_config_t *cfg, ati_handle_t **out);
+/* A batch: ncase independent cases in one handle (no counterpart in the
+ * reference, which runs one case per MPI job).  Their blocks are concatenated
+ * (case c owns blocks 6c .. 6c+5), every kernel launch of a step covers all
+ * cases through a work queue of (case, block, line tile) and (case, point
+ * tile) entries, and one CUDA graph replays a step of the whole batch.  The
+ * cases may differ in block sizes and physics (Re, T_inf, Mach, angle of
+ * attack, wall temperature, CFL, sponge, span) but share the numerics:
+ * nkrk, nviscous, les, precision, fltk and fltkbc.  They step together (one
+ * step count n), each with its own dt.  Calls without a case argument refer
+ * to case 0, except ati_set_time (every case) and the block-indexed ones. */
+int ati_create_batch(const ati_config_t *cfgs, int ncase, ati_handle_t **out);
+int ati_case_count(ati_handle_t *h, int *ncase);
+int ati_case_blocks(ati_handle_t *h, int cs, int *first_block, int *nblocks);
+int ati_case_time(ati_handle_t *h, int cs, ati_time_t *t);
+/* t->n must equal the batch's step count when the handle holds several cases. */
+int ati_case_set_time(ati_handle_t *h, int cs, const ati_time_t *t);
+int ati_case_config(ati_handle_t *h, int cs, ati_config_t *cfg);
 int ati_destroy(ati_handle_t *h);
 const char *ati_last_error(const ati_handle_t *h);
 int ati_abi_version(void);
@@ -249,6 +266,7 @@ int ati_deriv_lines_noalloc(const double *in, double *out, int64_t nlines, int32
  * (src/rpt.f90:1017-1056), from the p and stresses of the last stage:
  * out[0] = force coefficient along x, out[1] = along y. */
 int ati_forces(ati_handle_t *h, double out[2]);
+int ati_case_forces(ati_handle_t *h, int cs, double out[2]);
 
 /* ---- outputs and on-disk formats ---------------------------------------- */
 /* The configuration the handle was created with. */
@@ -256,6 +274,7 @@ int ati_get_config(ati_handle_t *h, ati_config_t *cfg);
 /* Moving-frame velocity umf(1:3) and angle of attack aoa (degrees) of the
  * current time (movef / pitch, src/Subroutineso.f90:192-259). */
 int ati_get_frame(ati_handle_t *h, double umf[3], double *aoa);
+int ati_case_frame(ati_handle_t *h, int cs, double umf[3], double *aoa);
 
 /* Surface-pressure recorder (no counterpart in the reference, which writes
  * whole fields at intervals): with capacity > 0, every time step ends with one
@@ -280,7 +299,8 @@ int ati_read_restart(ati_handle_t *h, int blk, const char *path);
  * (src/rpt.f90:246-330 and 115-241): int32 block count, int32
  * (IMax, JMax, KMax) per block, then per block x, y, z as float32 (grid), or
  * Mach, AoA, Re, time followed by rho, u, v, w, p as float32 (solution; the
- * velocities rho u / rho + umf, p the pressure of the last stage). */
+ * velocities rho u / rho + umf, p the pressure of the last stage).  A batch
+ * writes every block of every case, each with its own case's header values. */
 int ati_write_plot3d_grid(ati_handle_t *h, const char *path);
 int ati_write_plot3d_solution(ati_handle_t *h, const char *path);
 

@@ -32,16 +32,27 @@ struct TaskRange {
   int off = 0, n = 0, maxline = 0;
 };
 
+constexpr int SPG_PER_BLOCK = 14;
+
 thread_local std::string g_create_err;
 
 }  // namespace
 
 struct ati_handle {
-  ati_config_t cfg{};
+  ati_config_t cfg{};  // case 0; the numerics every case of a batch shares
   int nb = 0;
   bool mixed = false;
   std::vector<BlockDev> blk;
-  SchemeHost sh{};
+  SchemeHost sh{};     // case 0: scheme coefficients (shared) and its physics
+  // a batch: cases 0..ncase-1, case c owns blocks [case_b0[c], case_b0[c] + 6)
+  int ncase = 1;
+  std::vector<ati_config_t> cfgs;
+  std::vector<SchemeHost> shc;
+  std::vector<int> case_b0;
+  std::vector<TaskRange> tl_force_c;
+  bool any_cfl = false;  // some case takes its dt from the CFL condition (dto < 0)
+  std::vector<PTile> hpt;
+  std::vector<LTile> hlt[4];
   int64_t N = 0, F = 0, nfac = 0, nsbcc = 0, nwall = 0;
   int maxlen[4] = {0, 0, 0, 0};
   int maxlines[4] = {0, 0, 0, 0};
@@ -224,10 +235,12 @@ __global__ void k_sbcc_weight(Eng<double> c, const FaceTask *tasks, const double
 }
 
 // sponge coefficients (spongeup, src/SingleTurbulence3D.f90:209-249); spg per
-// block: [0..2] nsz(0,:)*szr(0,:), [3..5] szp(0,:), [6..8] nsz(1,:)*szr(1,:), [9..11] szp(1,:)
-__global__ void k_sponge(Eng<double> c, const double *xyz, const double *spg, double szco, double domlen, double pi) {
+// block: [0..2] nsz(0,:)*szr(0,:), [3..5] szp(0,:), [6..8] nsz(1,:)*szr(1,:), [9..11] szp(1,:),
+// [12] szco, [13] domlen of the block's case
+__global__ void k_sponge(Eng<double> c, const double *xyz, const double *spg, double pi) {
   const BlockDev &B = c.blk[blockIdx.y];
-  const double *P = spg + 12 * blockIdx.y;
+  const double *P = spg + SPG_PER_BLOCK * blockIdx.y;
+  const double szco = P[12], domlen = P[13];
   const int64_t N = c.N;
   const double ra1 = 0.25, ra2 = pi / (2.0 * domlen);
   double *asz = const_cast<double *>(c.asz), *bsz = const_cast<double *>(c.bsz);
@@ -243,7 +256,7 @@ __global__ void k_sponge(Eng<double> c, const double *xyz, const double *spg, do
     if (sig > 0.0) {
       const double res = 1.0 / c.yaco[g];
       asz[g] = res * sig * lam;
-      bsz[g] = res * c.sc->hamm1 * sig;
+      bsz[g] = res * c.sc[B.cs].hamm1 * sig;
     } else {
       asz[g] = 0.0;
       bsz[g] = 0.0;
@@ -296,12 +309,14 @@ __global__ void k_to_float(const double *src, float *dst, int64_t n) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     dst[g] = (float)src[g];
 }
-// pressure coefficient of the current qa (getCp, src/rptPost.f90:1456-1465)
+// pressure coefficient of the current qa (getCp, src/rptPost.f90:1456-1465), one grid row per block
 __global__ void k_cp(Eng<double> c, double *cp) {
-  const Scheme &S = *c.sc;
+  const BlockDev &B = c.blk[blockIdx.y];
+  const Scheme &S = c.sc[B.cs];
   const int64_t N = c.N;
   const double ra0 = 2.0 / (S.amachoo * S.amachoo);
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < N; g += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t g = B.off + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < B.off + B.npts;
+       g += (int64_t)gridDim.x * blockDim.x) {
     const double q1 = c.qa[g], q2 = c.qa[g + N], q3 = c.qa[g + 2 * N], q4 = c.qa[g + 3 * N];
     const double pp = S.gamm1 * (c.qa[g + 4 * N] - 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
     cp[g] = (pp - S.poo) * ra0;
@@ -373,17 +388,23 @@ extern "C" int ati_abi_version(void) { return ATI_ABI_VERSION; }
 extern "C" const char *ati_last_error(const ati_handle_t *h) { return h ? h->err.c_str() : g_create_err.c_str(); }
 
 static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<double> &facf, std::vector<double> &spg) {
-  const ati_config_t &cfg = h->cfg;
   int64_t off = 0, face = 0, fac = 0;
-  spg.assign((size_t)12 * h->nb, 0.0);
-  for (int mb = 0; mb < h->nb; mb++) {
-    BlockDev &B = h->blk[mb];
+  spg.assign((size_t)SPG_PER_BLOCK * h->nb, 0.0);
+  const int nbc = h->cfg.bkx * h->cfg.bky * h->cfg.bkz;  // blocks per case
+  h->case_b0.assign(h->ncase, 0);
+  for (int gb = 0; gb < h->nb; gb++) {
+    const int cs = gb / nbc, mb = gb % nbc, b0 = cs * nbc;
+    const ati_config_t &cfg = h->cfgs[cs];
+    h->case_b0[cs] = b0;
+    BlockDev &B = h->blk[gb];
     std::memset(&B, 0, sizeof(B));
     const int i = mb % cfg.bkx, j = (mb / cfg.bkx) % cfg.bky, k = mb / (cfg.bkx * cfg.bky);
     B.lxi = cfg.lxibk[i]; B.let = cfg.letbk[j]; B.lze = cfg.lzebk[k];
     if (B.lxi < 6 || B.let < 6 || B.lze < 12) return fail(h, ATI_EINVAL, "block sizes: lxi, let >= 6 and lze >= 12 required");
     int nbcs[4], nbce[4];
     topology(cfg, mb, B, nbcs, nbce);
+    for (int nn = 1; nn <= 3; nn++) { B.ncd[0][nn] += b0; B.ncd[1][nn] += b0; }  // neighbours within the case
+    B.cs = cs;
     B.off = off;
     B.npts = (int64_t)(B.lxi + 1) * (B.let + 1) * (B.lze + 1);
     off += B.npts;
@@ -406,11 +427,13 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
                         {0, dl - cfg.szth1, dl + cfg.szxt - cfg.szth2, 0}};
     for (int nn = 1; nn <= 3; nn++) {
       const double n0 = nbcs[nn] == 10 ? 1.0 : 0.0, n1 = nbce[nn] == 10 ? 1.0 : 0.0;
-      spg[12 * mb + (nn - 1)] = n0 * szr[0][nn];
-      spg[12 * mb + 3 + (nn - 1)] = szp[0][nn];
-      spg[12 * mb + 6 + (nn - 1)] = n1 * szr[1][nn];
-      spg[12 * mb + 9 + (nn - 1)] = szp[1][nn];
+      spg[SPG_PER_BLOCK * gb + (nn - 1)] = n0 * szr[0][nn];
+      spg[SPG_PER_BLOCK * gb + 3 + (nn - 1)] = szp[0][nn];
+      spg[SPG_PER_BLOCK * gb + 6 + (nn - 1)] = n1 * szr[1][nn];
+      spg[SPG_PER_BLOCK * gb + 9 + (nn - 1)] = szp[1][nn];
     }
+    spg[SPG_PER_BLOCK * gb + 12] = cfg.szco;
+    spg[SPG_PER_BLOCK * gb + 13] = cfg.domlen;
   }
   h->N = off;
   h->F = face;
@@ -455,7 +478,7 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
   for (int d = 1; d <= 3; d++)
     add(h->tl_avg_dir[d], [d](const BlockDev &B, int nn, int ip) { return nn == d && is_avg(B.nbc[ip][nn]); });
   add(h->tl_all, [](const BlockDev &, int, int) { return true; });
-  const int bcw = 20 + 5 * cfg.nviscous;
+  const int bcw = 20 + 5 * h->cfg.nviscous;
   add(h->tl_force, [bcw](const BlockDev &B, int nn, int ip) {
     if (nn != 2) return false;
     if (ip == 0) return B.nbc[0][2] == bcw;
@@ -478,6 +501,29 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
   }
   h->nsbcc = ns;
   h->nwall = nw;
+  // wall faces of each case (contiguous: the task lists follow the block order)
+  h->tl_force_c.assign(h->ncase, TaskRange{});
+  for (int q = 0; q < h->tl_force.n; q++) {
+    const int cs = h->blk[T[h->tl_force.off + q].b].cs;
+    TaskRange &r = h->tl_force_c[cs];
+    if (r.n == 0) r.off = h->tl_force.off + q;
+    r.n++;
+    r.maxline = std::max(r.maxline, T[h->tl_force.off + q].nline);
+  }
+  // work queues: point tiles of one case, line tiles of one block
+  h->hpt.clear();
+  for (int cs = 0; cs < h->ncase; cs++) {
+    const int64_t g0 = h->blk[h->case_b0[cs]].off;
+    const BlockDev &Bl = h->blk[h->case_b0[cs] + nbc - 1];
+    const int64_t g1 = Bl.off + Bl.npts;
+    for (int64_t g = g0; g < g1; g += PT_POINTS) h->hpt.push_back(PTile{cs, 0, g, std::min(g + PT_POINTS, g1)});
+  }
+  for (int nn = 1; nn <= 3; nn++) {
+    h->hlt[nn].clear();
+    const int step = nn == 1 ? XC_NL : SG_LINES;
+    for (int gb = 0; gb < h->nb; gb++)
+      for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += step) h->hlt[nn].push_back(LTile{gb, t0});
+  }
   return ATI_OK;
 }
 
@@ -498,25 +544,44 @@ static Coef<T> make_coef(const Scheme &S) {
   return c;
 }
 
-extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
+static bool same_numerics(const ati_config_t &a, const ati_config_t &b) {
+  return a.bkx == b.bkx && a.bky == b.bky && a.bkz == b.bkz && a.nkrk == b.nkrk && a.nviscous == b.nviscous &&
+         a.les == b.les && a.precision == b.precision && a.fltk == b.fltk && a.fltkbc == b.fltkbc;
+}
+
+static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) {
   ati_handle *h = nullptr;
-  if (!cfg || !out) return fail(h, ATI_EINVAL, "null argument");
+  if (!cfgs || !out || ncase < 1) return fail(h, ATI_EINVAL, "null argument or ncase < 1");
   *out = nullptr;
-  if (cfg->bkx != 3 || cfg->bky != 2 || cfg->bkz != 1)
-    return fail(h, ATI_EINVAL, "the aerofoil H-grid topology has bkx=3, bky=2, bkz=1 blocks");
-  if (cfg->nkrk < 1 || cfg->nkrk > 8) return fail(h, ATI_EINVAL, "nkrk must be 1..8");
-  if (cfg->precision != ATI_FP64 && cfg->precision != ATI_FP64_STRICT && cfg->precision != ATI_MIXED)
-    return fail(h, ATI_EINVAL, "precision: ATI_FP64, ATI_FP64_STRICT or ATI_MIXED");
+  for (int c = 0; c < ncase; c++) {
+    const ati_config_t *cfg = &cfgs[c];
+    if (cfg->bkx != 3 || cfg->bky != 2 || cfg->bkz != 1)
+      return fail(h, ATI_EINVAL, "the aerofoil H-grid topology has bkx=3, bky=2, bkz=1 blocks");
+    if (cfg->nkrk < 1 || cfg->nkrk > 8) return fail(h, ATI_EINVAL, "nkrk must be 1..8");
+    if (cfg->precision != ATI_FP64 && cfg->precision != ATI_FP64_STRICT && cfg->precision != ATI_MIXED)
+      return fail(h, ATI_EINVAL, "precision: ATI_FP64, ATI_FP64_STRICT or ATI_MIXED");
+    if (!same_numerics(*cfg, cfgs[0]))
+      return fail(h, ATI_EINVAL, "a batch shares its numerics: nkrk, nviscous, les, precision, fltk and fltkbc of "
+                                 "every case must equal case 0's (case " + std::to_string(c) + " differs)");
+  }
+  if (6 * ncase > MAXB) return fail(h, ATI_EINVAL, "too many cases in one batch");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
     return fail(h, ATI_ECUDA, "no CUDA device: this library has no CPU fallback");
   h = new ati_handle();
-  h->cfg = *cfg;
-  h->mixed = cfg->precision == ATI_MIXED;
-  h->nb = cfg->bkx * cfg->bky * cfg->bkz;
+  h->ncase = ncase;
+  h->cfgs.assign(cfgs, cfgs + ncase);
+  h->cfg = cfgs[0];
+  h->mixed = h->cfg.precision == ATI_MIXED;
+  h->nb = 6 * ncase;
   h->blk.resize(h->nb);
   h->grid_set.assign(h->nb, 0);
-  build_scheme(*cfg, h->sh);
+  h->shc.resize(ncase);
+  for (int c = 0; c < ncase; c++) {
+    build_scheme(cfgs[c], h->shc[c]);
+    if (cfgs[c].dto < 0) h->any_cfl = true;
+  }
+  h->sh = h->shc[0];
   std::vector<double> facd, facf, spg;
   int rc = build_tables(h, facd, facf, spg);
   if (rc) {
@@ -532,6 +597,7 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
     return o;
   };
   const size_t D8 = sizeof(double), F4 = sizeof(float);
+  const size_t nforce = std::max<size_t>(h->tl_force.n, 1);
   // FP64 set: qa qo de(5) rr ss(3) xim etm zem(3) yaco p mu(1) tau(9) asz bsz(1) cnt(2) prim(4) dv(12) flx(15)
   // fw(5) fw1(1)
   const int np64 = 5 + 5 + 5 + 3 + 3 + 9 + 1 + 1 + 1 + 9 + 2 + 2 + 4 + 12 + 15 + 5 + 1;
@@ -539,10 +605,13 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
                o_recv = take(30 * F * D8), o_cm = take(6 * F * D8), o_facd = take(facd.size() * D8),
                o_facf = take(facf.size() * D8), o_sbcc = take(std::max<int64_t>(h->nsbcc, 1) * D8),
                o_rpex = take(std::max<int64_t>(h->nwall, 1) * D8), o_area = take(std::max<int64_t>(h->nwall, 1) * D8),
-               o_wnor = take(3 * std::max<int64_t>(h->nwall, 1) * D8), o_frc = take(64 * D8), o_spg = take(spg.size() * D8),
-               o_blk = take(sizeof(BlockDev) * h->nb), o_sc = take(sizeof(Scheme)), o_cfd = take(sizeof(Coef<double>)),
-               o_scal = take(sizeof(Scalars)), o_task = take(sizeof(FaceTask) * h->htasks.size()),
-               o_jn = take(sizeof(JunctionDev) * 4), o_woff = take(16 * sizeof(int64_t));
+               o_wnor = take(3 * std::max<int64_t>(h->nwall, 1) * D8), o_frc = take(2 * nforce * D8),
+               o_spg = take(spg.size() * D8), o_blk = take(sizeof(BlockDev) * h->nb),
+               o_sc = take(sizeof(Scheme) * ncase), o_cfd = take(sizeof(Coef<double>)),
+               o_scal = take(sizeof(Scalars) * ncase), o_task = take(sizeof(FaceTask) * h->htasks.size()),
+               o_jn = take(sizeof(JunctionDev) * 2 * ncase), o_woff = take(nforce * sizeof(int64_t)),
+               o_pt = take(sizeof(PTile) * h->hpt.size()), o_lt1 = take(sizeof(LTile) * h->hlt[1].size()),
+               o_lt2 = take(sizeof(LTile) * h->hlt[2].size()), o_lt3 = take(sizeof(LTile) * h->hlt[3].size());
   // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
          o_frpex = 0, o_cff = 0, o_fdrvm = 0;
@@ -567,9 +636,14 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
   BlockDev *dblk = (BlockDev *)(h->arena + o_blk);
   Scheme *dsc = (Scheme *)(h->arena + o_sc);
   Scalars *dscal = (Scalars *)(h->arena + o_scal);
+  const PTile *dpt = (const PTile *)(h->arena + o_pt);
+  const LTile *dlt[4] = {nullptr, (const LTile *)(h->arena + o_lt1), (const LTile *)(h->arena + o_lt2),
+                         (const LTile *)(h->arena + o_lt3)};
   Eng<double> &d = h->ed;
   double *f = D(o_f);
   d.blk = dblk; d.sc = dsc; d.cf = (Coef<double> *)(h->arena + o_cfd); d.scal = dscal; d.N = N; d.F = F;
+  d.ncase = ncase; d.pt = dpt; d.npt = (int)h->hpt.size();
+  for (int nn = 1; nn <= 3; nn++) { d.lt[nn] = dlt[nn]; d.nlt[nn] = (int)h->hlt[nn].size(); }
   d.qa = f; f += 5 * N; d.qo = f; f += 5 * N; d.de = f; f += 5 * N;
   h->rr = f; f += 3 * N; h->ss = f; f += 3 * N;
   d.xim = f; f += 3 * N; d.etm = f; f += 3 * N; d.zem = f; f += 3 * N; d.yaco = f; d.yacod = f; f += N;
@@ -586,6 +660,8 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
     Eng<float> &m = h->ef;
     float *g = Fp(o_ff);
     m.blk = dblk; m.sc = dsc; m.cf = (Coef<float> *)(h->arena + o_cff); m.scal = dscal; m.N = N; m.F = F;
+    m.ncase = ncase; m.pt = dpt; m.npt = d.npt;
+    for (int nn = 1; nn <= 3; nn++) { m.lt[nn] = dlt[nn]; m.nlt[nn] = d.nlt[nn]; }
     m.qa = d.qa; m.qo = d.qo; m.yacod = d.yacod; m.cnt = d.cnt;
     m.de = g; g += 5 * N; m.prim = g; g += 4 * N; m.mu = g; g += N; m.p = g; g += N; m.dv = g; g += 12 * N;
     m.tau = g; g += 9 * N; m.flx = g; g += 15 * N; m.fw = g; g += 5 * N;
@@ -595,30 +671,36 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
     m.drva = Fp(o_fdrva); m.drvb = Fp(o_fdrvb); m.recv = Fp(o_frecv); m.cm = Fp(o_fcm);
     m.facd = Fp(o_ffacd); m.facf = Fp(o_ffacf); m.sbcc = Fp(o_fsbcc); m.rpex = Fp(o_frpex);
   }
-  // junctions (src/SingleTurbulence3D.f90:386-398), bkx = 3, bky = 2
+  // junctions (src/SingleTurbulence3D.f90:386-398), bkx = 3, bky = 2, per case
   std::vector<JunctionDev> jn;
-  for (int nn = 0; nn <= (cfg->bkx - 1) * (cfg->bky - 1) - 1; nn++) {
-    const int njct = nn + nn / (cfg->bkx - 1);
-    const int mm[4] = {njct, njct + 1, njct + cfg->bkx, njct + cfg->bkx + 1};
-    const int cip[4] = {1, 0, 1, 0}, cjp[4] = {1, 1, 0, 0};
-    JunctionDev J{};
-    for (int q = 0; q < 4; q++) {
-      const BlockDev &B = h->blk[mm[q]];
-      const int i = cip[q] * B.lxi, j = cjp[q] * B.let;
-      J.base[q] = B.off + (int64_t)j * (B.lxi + 1) + i;
-      J.kstr[q] = (int64_t)(B.lxi + 1) * (B.let + 1);
+  for (int cs = 0; cs < ncase; cs++) {
+    const ati_config_t *cfg = &h->cfgs[cs];
+    const int b0 = h->case_b0[cs];
+    for (int nn = 0; nn <= (cfg->bkx - 1) * (cfg->bky - 1) - 1; nn++) {
+      const int njct = nn + nn / (cfg->bkx - 1);
+      const int mm[4] = {njct, njct + 1, njct + cfg->bkx, njct + cfg->bkx + 1};
+      const int cip[4] = {1, 0, 1, 0}, cjp[4] = {1, 1, 0, 0};
+      JunctionDev J{};
+      for (int q = 0; q < 4; q++) {
+        const BlockDev &B = h->blk[b0 + mm[q]];
+        const int i = cip[q] * B.lxi, j = cjp[q] * B.let;
+        J.base[q] = B.off + (int64_t)j * (B.lxi + 1) + i;
+        J.kstr[q] = (int64_t)(B.lxi + 1) * (B.let + 1);
+      }
+      J.nk = h->blk[b0 + mm[0]].lze + 1;
+      J.pa = (1 - nn) == 1 ? 2 : 1;
+      J.pb = (1 - nn) == 1 ? 4 : 3;
+      jn.push_back(J);
+      h->jnk = std::max(h->jnk, J.nk);
     }
-    J.nk = h->blk[mm[0]].lze + 1;
-    J.pa = (1 - nn) == 1 ? 2 : 1;
-    J.pb = (1 - nn) == 1 ? 4 : 3;
-    jn.push_back(J);
-    h->jnk = std::max(h->jnk, J.nk);
   }
   h->njct = (int)jn.size();
   std::vector<int64_t> woff;
   for (int q = 0; q < h->tl_force.n; q++) woff.push_back(h->htasks[h->tl_force.off + q].wall_off);
   const Coef<double> cfd = make_coef<double>(h->sh.s);
   const Coef<float> cff = make_coef<float>(h->sh.s);
+  std::vector<Scheme> schemes;
+  for (int c = 0; c < ncase; c++) schemes.push_back(h->shc[c].s);
   std::vector<float> facd32(facd.begin(), facd.end()), facf32(facf.begin(), facf.end());
   e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->arena, 0, bytes, h->st);
@@ -629,11 +711,13 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
   up(d.facf, facf.data(), facf.size() * D8);
   up(h->dspg, spg.data(), spg.size() * D8);
   up(dblk, h->blk.data(), sizeof(BlockDev) * h->nb);
-  up(dsc, &h->sh.s, sizeof(Scheme));
+  up(dsc, schemes.data(), sizeof(Scheme) * ncase);
   up(d.cf, &cfd, sizeof(cfd));
   up(h->dtasks, h->htasks.data(), sizeof(FaceTask) * h->htasks.size());
   up(h->djn, jn.data(), sizeof(JunctionDev) * jn.size());
   up(h->dwoff, woff.data(), sizeof(int64_t) * woff.size());
+  up(dpt, h->hpt.data(), sizeof(PTile) * h->hpt.size());
+  for (int nn = 1; nn <= 3; nn++) up(dlt[nn], h->hlt[nn].data(), sizeof(LTile) * h->hlt[nn].size());
   if (h->mixed) {
     up(h->ef.cf, &cff, sizeof(cff));
     up(h->ef.facd, facd32.data(), facd32.size() * F4);
@@ -648,6 +732,12 @@ extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) {
   }
   *out = h;
   return ATI_OK;
+}
+
+extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) { return create_impl(cfg, 1, out); }
+
+extern "C" int ati_create_batch(const ati_config_t *cfgs, int ncase, ati_handle_t **out) {
+  return create_impl(cfgs, ncase, out);
 }
 
 static void probe_free(ati_handle *h) {
@@ -729,7 +819,7 @@ static int copy_field(ati_handle *h, int blk, int field, double *host, bool to_d
   if (field == ATI_F_CP) {
     if (to_dev) return fail(h, ATI_EINVAL, "ATI_F_CP is derived: ati_get_field only");
     if (!h->inited) return fail(h, ATI_ESTATE, "ATI_F_CP needs ati_init");
-    k_cp<<<256, 256, 0, h->st>>>(h->ed, base);
+    k_cp<<<dim3(64, h->nb), 256, 0, h->st>>>(h->ed, base);
     CKL();
   }
   if (to_dev) {
@@ -772,26 +862,60 @@ extern "C" int ati_get_face(ati_handle_t *h, int blk, int which, int nn, double 
   return ATI_OK;
 }
 
-extern "C" int ati_get_time(ati_handle_t *h, ati_time_t *t) {
-  if (!h || !t) return fail(h, ATI_EINVAL, "ati_get_time: bad argument");
+static int case_time(ati_handle *h, int cs, ati_time_t *t) {
+  if (!h || !t || cs < 0 || cs >= h->ncase) return fail(h, ATI_EINVAL, "time: bad argument");
   Scalars s;
-  CK(cudaMemcpyAsync(&s, h->ed.scal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(&s, h->ed.scal + cs, sizeof(s), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   t->n = s.n; t->ndt = s.ndt; t->dt = s.dt; t->dts = s.dts; t->dte = s.dte; t->timo = s.timo;
   return ATI_OK;
 }
 
-extern "C" int ati_set_time(ati_handle_t *h, const ati_time_t *t) {
-  if (!h || !t) return fail(h, ATI_EINVAL, "ati_set_time: bad argument");
+static int case_set_time(ati_handle *h, int cs, const ati_time_t *t) {
+  if (!h || !t || cs < 0 || cs >= h->ncase) return fail(h, ATI_EINVAL, "set time: bad argument");
+  if (h->ncase > 1 && t->n != h->n_host)
+    return fail(h, ATI_EINVAL, "the cases of a batch step together: n must equal the batch's step count");
   Scalars s;
-  CK(cudaMemcpyAsync(&s, h->ed.scal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(&s, h->ed.scal + cs, sizeof(s), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   s.n = t->n; s.ndt = t->ndt; s.dt = t->dt; s.dts = t->dts; s.dte = t->dte; s.timo = t->timo;
-  CK(cudaMemcpyAsync(h->ed.scal, &s, sizeof(s), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->ed.scal + cs, &s, sizeof(s), cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
   h->n_host = t->n;
   return ATI_OK;
 }
+
+extern "C" int ati_get_time(ati_handle_t *h, ati_time_t *t) { return case_time(h, 0, t); }
+
+extern "C" int ati_set_time(ati_handle_t *h, const ati_time_t *t) {
+  if (!h || !t) return fail(h, ATI_EINVAL, "ati_set_time: bad argument");
+  const int64_t n0 = h->n_host;
+  h->n_host = t->n;  // every case at once: the batch keeps one step count
+  for (int c = 0; c < h->ncase; c++) {
+    int rc = case_set_time(h, c, t);
+    if (rc) {
+      h->n_host = n0;
+      return rc;
+    }
+  }
+  return ATI_OK;
+}
+
+extern "C" int ati_case_count(ati_handle_t *h, int *ncase) {
+  if (!h || !ncase) return fail(h, ATI_EINVAL, "ati_case_count: bad argument");
+  *ncase = h->ncase;
+  return ATI_OK;
+}
+
+extern "C" int ati_case_blocks(ati_handle_t *h, int cs, int *first_block, int *nblocks) {
+  if (!h || cs < 0 || cs >= h->ncase || !first_block || !nblocks) return fail(h, ATI_EINVAL, "ati_case_blocks: bad argument");
+  *first_block = h->case_b0[cs];
+  *nblocks = h->nb / h->ncase;
+  return ATI_OK;
+}
+
+extern "C" int ati_case_time(ati_handle_t *h, int cs, ati_time_t *t) { return case_time(h, cs, t); }
+extern "C" int ati_case_set_time(ati_handle_t *h, int cs, const ati_time_t *t) { return case_set_time(h, cs, t); }
 
 extern "C" int ati_set_grid(ati_handle_t *h, int blk, const double *xyz) {
   int rc = copy_field(h, blk, ATI_F_SS, const_cast<double *>(xyz), true);
@@ -805,7 +929,7 @@ static int granular_sweep(ati_handle *h, int nn, bool filt, const double *in, do
   e.fw = h->fw1;
   SweepIO<double, double> io{in, 0, out, 0, nullptr, 1, m, !filt};
   PROF(h, (filt ? ATI_K_FILTER_XI : ATI_K_DERIV_XI) + nn - 1,
-       strict::sweep_ddd(e, h->st, nn, filt, io, h->nb, h->maxlines[nn], h->maxlen[nn]));
+       strict::sweep_ddd(e, h->st, nn, filt, io));
   CKL();
   return ATI_OK;
 }
@@ -879,7 +1003,7 @@ extern "C" int ati_init(ati_handle_t *h) {
     CKL();
   }
   // sponge (the grid coordinates are still in ss)
-  k_sponge<<<dim3(64, h->nb), 256, 0, h->st>>>(c, h->ss, h->dspg, h->cfg.szco, h->cfg.domlen, std::acos(-1.0));
+  k_sponge<<<dim3(64, h->nb), 256, 0, h->st>>>(c, h->ss, h->dspg, std::acos(-1.0));
   CKL();
   if (h->mixed) {  // FP32 copies of everything the mixed stage reads
     Eng<float> &m = h->ef;
@@ -900,7 +1024,7 @@ extern "C" int ati_init(ati_handle_t *h) {
     const double *mf[3] = {c.xim, c.etm, c.zem};
     for (int nn = 1; nn <= 3; nn++) {
       SweepIO<double, double> io{mf[nn - 1], N, c.flx + 3 * (nn - 1) * N, N, nullptr, 3, 1, true};
-      strict::sweep_ddd(c, h->st, nn, false, io, h->nb, h->maxlines[nn], h->maxlen[nn]);
+      strict::sweep_ddd(c, h->st, nn, false, io);
     }
     strict::metric_divergence(c, h->st, c.flx, const_cast<float *>(m.gm));
     CKL();
@@ -910,7 +1034,7 @@ extern "C" int ati_init(ati_handle_t *h) {
   // initial condition and time scalars (src/Main3D.f90:520-522)
   k_ic<<<256, 256, 0, h->st>>>(c);
   CKL();
-  CK(cudaMemsetAsync(c.scal, 0, sizeof(Scalars), h->st));
+  CK(cudaMemsetAsync(c.scal, 0, sizeof(Scalars) * h->ncase, h->st));
   strict::scalar(c, h->st, SC_INIT, 0);
   CKL();
   CK(cudaStreamSynchronize(h->st));
@@ -930,13 +1054,12 @@ struct EngineCalls;
 template <>
 struct EngineCalls<double> {
   static void sweep(bool strict, const Eng<double> &e, cudaStream_t st, int nn, bool filt,
-                    const SweepIO<double, double> &io, int nb, int ml, int mlen) {
-    if (strict) strict::sweep_ddd(e, st, nn, filt, io, nb, ml, mlen);
-    else fast::sweep_ddd(e, st, nn, filt, io, nb, ml, mlen);
+                    const SweepIO<double, double> &io) {
+    if (strict) strict::sweep_ddd(e, st, nn, filt, io);
+    else fast::sweep_ddd(e, st, nn, filt, io);
   }
-  static void qsweep(bool strict, const Eng<double> &e, cudaStream_t st, int nn, const SweepIO<double, double> &io,
-                     int nb, int ml, int mlen) {
-    sweep(strict, e, st, nn, true, io, nb, ml, mlen);
+  static void qsweep(bool strict, const Eng<double> &e, cudaStream_t st, int nn, const SweepIO<double, double> &io) {
+    sweep(strict, e, st, nn, true, io);
   }
   static void mpigo(bool strict, const Eng<double> &e, cudaStream_t st, const FaceTask *t, int n, int ml, int nt,
                     const double *s1, const double *s2, const double *s3, int64_t fs, int nf) {
@@ -959,13 +1082,11 @@ struct EngineCalls<double> {
 
 template <>
 struct EngineCalls<float> {
-  static void sweep(bool, const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io,
-                    int nb, int ml, int mlen) {
-    fast::sweep_fff(e, st, nn, filt, io, nb, ml, mlen);
+  static void sweep(bool, const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io) {
+    fast::sweep_fff(e, st, nn, filt, io);
   }
-  static void qsweep(bool, const Eng<float> &e, cudaStream_t st, int nn, const SweepIO<double, double> &io, int nb,
-                     int ml, int mlen) {
-    fast::sweep_ddf(e, st, nn, true, io, nb, ml, mlen);
+  static void qsweep(bool, const Eng<float> &e, cudaStream_t st, int nn, const SweepIO<double, double> &io) {
+    fast::sweep_ddf(e, st, nn, true, io);
   }
   static void mpigo(bool, const Eng<float> &e, cudaStream_t st, const FaceTask *t, int n, int ml, int nt,
                     const float *s1, const float *s2, const float *s3, int64_t fs, int nf) {
@@ -996,7 +1117,7 @@ static int filter_step_t(ati_handle *h, const Eng<R> &e) {
   for (int nn = 1; nn <= 3; nn++) {
     SweepIO<double, double> io{h->ed.qa, N, h->ed.qa, N, nn == 3 ? h->ed.qo : nullptr, 5, 1, false};
     for (int f = 0; f < 5; f++) io.ofs[f] = fo.v[f];
-    PROF(h, ATI_K_FILTER_XI + nn - 1, C::qsweep(strict, e, h->st, nn, io, h->nb, h->maxlines[nn], h->maxlen[nn]));
+    PROF(h, ATI_K_FILTER_XI + nn - 1, C::qsweep(strict, e, h->st, nn, io));
   }
   CKL();
   return ATI_OK;
@@ -1017,7 +1138,7 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
   PROF(h, ATI_K_PRIM, C::pw(strict, e, st, PW_PRIM));
   if (nk == 1) {
     if (h->n_host % 10 == 1) {
-      if (h->cfg.dto < 0) {
+      if (h->any_cfl) {
         PROF(h, ATI_K_SCALAR, sc(SC_CFL_RESET));
         PROF(h, ATI_K_CFL, C::pw(strict, e, st, PW_CFL));
       }
@@ -1031,7 +1152,7 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
                                   e.prim, e.prim, N, 4));
     for (int nn = 3; nn >= 1; nn--) {
       SweepIO<R, R> io{e.prim, N, e.dv + (nn - 1) * N, 3 * N, nullptr, 4, 2, true};
-      PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io, h->nb, h->maxlines[nn], h->maxlen[nn]));
+      PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io));
     }
     PROF(h, ATI_K_VISC, C::pw(strict, e, st, PW_VISC));
   }
@@ -1041,7 +1162,7 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
                                 e.flx + N, e.flx + 2 * N, 3 * N, 5));
   for (int nn = 1; nn <= 3; nn++) {
     SweepIO<R, R> io{e.flx + (nn - 1) * N, 3 * N, e.flx + (nn - 1) * N, 3 * N, nullptr, 5, 1, true};
-    PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io, h->nb, h->maxlines[nn], h->maxlen[nn]));
+    PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io));
   }
   PROF(h, ATI_K_DIV, C::pw(strict, e, st, PW_DIV));
   // characteristic boundary conditions (src/Main3D.f90:780-869)
@@ -1085,11 +1206,13 @@ static int one_step(ati_handle *h) {
 }
 
 static int check_flag(ati_handle *h) {
-  int flag = 0;
-  CK(cudaMemcpyAsync(&flag, &h->ed.scal->flag, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  std::vector<Scalars> sc(h->ncase);
+  CK(cudaMemcpyAsync(sc.data(), h->ed.scal, sizeof(Scalars) * h->ncase, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  if (flag) return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state (flag " +
-                                               std::to_string(flag) + ")");
+  for (int c = 0; c < h->ncase; c++)
+    if (sc[c].flag)
+      return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state of case " +
+                                         std::to_string(c) + " (flag " + std::to_string(sc[c].flag) + ")");
   return ATI_OK;
 }
 
@@ -1148,45 +1271,56 @@ extern "C" int ati_step(ati_handle_t *h, int nsteps) {
   return check_flag(h);
 }
 
-extern "C" int ati_forces(ati_handle_t *h, double out[2]) {
-  if (!h || !out) return fail(h, ATI_EINVAL, "ati_forces: bad argument");
+extern "C" int ati_case_forces(ati_handle_t *h, int cs, double out[2]) {
+  if (!h || !out || cs < 0 || cs >= h->ncase) return fail(h, ATI_EINVAL, "forces: bad argument");
   if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
-  if (h->mixed) strict::forces_f(h->ef, h->st, tp(h, h->tl_force), h->tl_force.n, h->area, h->wnor, h->dwoff, h->dforce);
-  else strict::forces_d(h->ed, h->st, tp(h, h->tl_force), h->tl_force.n, h->area, h->wnor, h->dwoff, h->dforce);
+  const TaskRange &r = h->tl_force_c[cs];
+  const int q0 = r.off - h->tl_force.off;  // position in the wall-face list
+  if (h->mixed)
+    strict::forces_f(h->ef, h->st, tp(h, r), r.n, h->area, h->wnor, h->dwoff + q0, h->dforce + 2 * q0);
+  else strict::forces_d(h->ed, h->st, tp(h, r), r.n, h->area, h->wnor, h->dwoff + q0, h->dforce + 2 * q0);
   CKL();
-  std::vector<double> part((size_t)2 * h->tl_force.n);
-  CK(cudaMemcpyAsync(part.data(), h->dforce, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->st));
+  std::vector<double> part((size_t)2 * r.n);
+  CK(cudaMemcpyAsync(part.data(), h->dforce + 2 * q0, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
-  const double dynp = 2.0 / (h->sh.s.amachoo * h->sh.s.amachoo * h->cfg.span);
+  const Scheme &S = h->shc[cs].s;
+  const double dynp = 2.0 / (S.amachoo * S.amachoo * h->cfgs[cs].span);
   out[0] = 0.0; out[1] = 0.0;
-  for (int q = 0; q < h->tl_force.n; q++) {  // blocks in rank order, as MPI_REDUCE over wcom
+  for (int q = 0; q < r.n; q++) {  // blocks in rank order, as MPI_REDUCE over wcom
     out[0] = out[0] + part[2 * q] * dynp;
     out[1] = out[1] + part[2 * q + 1] * dynp;
   }
   return ATI_OK;
 }
 
-extern "C" int ati_get_config(ati_handle_t *h, ati_config_t *cfg) {
-  if (!h || !cfg) return fail(h, ATI_EINVAL, "ati_get_config: bad argument");
-  *cfg = h->cfg;
+extern "C" int ati_forces(ati_handle_t *h, double out[2]) { return ati_case_forces(h, 0, out); }
+
+extern "C" int ati_case_config(ati_handle_t *h, int cs, ati_config_t *cfg) {
+  if (!h || !cfg || cs < 0 || cs >= h->ncase) return fail(h, ATI_EINVAL, "config: bad argument");
+  *cfg = h->cfgs[cs];
   return ATI_OK;
 }
 
-extern "C" int ati_get_frame(ati_handle_t *h, double umf[3], double *aoa) {
-  if (!h || !umf || !aoa) return fail(h, ATI_EINVAL, "ati_get_frame: bad argument");
+extern "C" int ati_get_config(ati_handle_t *h, ati_config_t *cfg) { return ati_case_config(h, 0, cfg); }
+
+extern "C" int ati_case_frame(ati_handle_t *h, int cs, double umf[3], double *aoa) {
+  if (!h || !umf || !aoa || cs < 0 || cs >= h->ncase) return fail(h, ATI_EINVAL, "frame: bad argument");
   Scalars sc;
-  CK(cudaMemcpyAsync(&sc, h->ed.scal, sizeof(sc), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(&sc, h->ed.scal + cs, sizeof(sc), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   for (int q = 0; q < 3; q++) umf[q] = sc.umf[q + 1];
   *aoa = sc.aoa;
   return ATI_OK;
 }
 
+extern "C" int ati_get_frame(ati_handle_t *h, double umf[3], double *aoa) { return ati_case_frame(h, 0, umf, aoa); }
+
 // ---- surface-pressure recorder ----------------------------------------------------
 
 extern "C" int ati_wall_probe_enable(ati_handle_t *h, int capacity) {
   if (!h || capacity < 0) return fail(h, ATI_EINVAL, "ati_wall_probe_enable: bad argument");
   if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  if (h->ncase > 1) return fail(h, ATI_EINVAL, "ati_wall_probe_enable: single-case handles only");
   CK(cudaStreamSynchronize(h->st));
   probe_free(h);
   drop_graphs(h);  // the step graphs hold (or lack) the recording kernel

@@ -1,6 +1,10 @@
-// ati_internal.h — device-side data layout of one case (all blocks on one GPU).
+// ati_internal.h — device-side data layout of a handle: one case, or a batch
+// of independent cases, with every block on one GPU.
 //
 // Layout in HBM
+//  * A batch concatenates its cases' blocks: block b of the handle belongs to
+//    case cs_b, and every per-case constant (scheme physics, time scalars)
+//    lives in arrays indexed by case.
 //  * Every point field is stored as [component][Ntot] doubles, where the
 //    points of block b occupy [off_b, off_b + npts_b) of each component plane
 //    and, inside a block, l = i + (lxi+1)*(j + (let+1)*k) (xi fastest), the
@@ -22,7 +26,7 @@ namespace ati {
 constexpr int LMD = 11;
 constexpr int LMF = 8;
 constexpr int MBCI = 3;
-constexpr int MAXB = 64;  // blocks per handle
+constexpr int MAXB = 1024;  // blocks per handle (cases x 6)
 
 struct BlockDev {
   int lxi, let, lze;
@@ -34,6 +38,18 @@ struct BlockDev {
   int64_t npts;
   int64_t face_off[4];  // face index offset (per nn)
   int64_t fac_off[4];   // factor table offset (positions)
+  int cs;               // case of the block
+  int pad;
+};
+
+// Work-queue entries.  Pointwise kernels walk tiles of consecutive points of
+// one case; line sweeps walk tiles of consecutive lines of one block.
+struct PTile {
+  int cs, pad;
+  int64_t g0, g1;  // points [g0, g1)
+};
+struct LTile {
+  int b, t0;  // block, first line
 };
 
 // Scheme coefficients and physical constants of one case (built on the host

@@ -41,9 +41,21 @@ bool put_i4_slot(FILE *f, int64_t v) {
   return put(f, slot, 8);
 }
 
-int nblocks(ati_handle_t *h, ati_config_t &cfg) {
-  if (ati_get_config(h, &cfg) != ATI_OK) return -1;
-  return cfg.bkx * cfg.bky * cfg.bkz;
+// blocks of the handle (all cases of a batch) and the case of a block
+int nblocks(ati_handle_t *h) {
+  int nc = 0, b0 = 0, nb = 0;
+  if (ati_case_count(h, &nc) != ATI_OK || ati_case_blocks(h, nc - 1, &b0, &nb) != ATI_OK) return -1;
+  return b0 + nb;
+}
+int block_case(ati_handle_t *h, int blk) {
+  int nc = 0;
+  if (ati_case_count(h, &nc) != ATI_OK) return -1;
+  for (int c = 0; c < nc; c++) {
+    int b0 = 0, nb = 0;
+    if (ati_case_blocks(h, c, &b0, &nb) != ATI_OK) return -1;
+    if (blk >= b0 && blk < b0 + nb) return c;
+  }
+  return -1;
 }
 
 }  // namespace
@@ -55,7 +67,7 @@ extern "C" int ati_write_restart(ati_handle_t *h, int blk, const char *path) {
   int rc = ati_block_dims(h, blk, dims, &npts);
   if (rc) return rc;
   ati_time_t t;
-  if ((rc = ati_get_time(h, &t))) return rc;
+  if ((rc = ati_case_time(h, block_case(h, blk), &t))) return rc;
   std::vector<double> q((size_t)5 * npts);
   if ((rc = ati_get_state(h, blk, q.data()))) return rc;
   File fl(path, "wb");
@@ -88,13 +100,12 @@ extern "C" int ati_read_restart(ati_handle_t *h, int blk, const char *path) {
   ati_time_t t;
   t.n = n; t.ndt = ndt; t.dt = hd[0]; t.dts = hd[1]; t.dte = hd[2]; t.timo = hd[3];
   if ((rc = ati_set_state(h, blk, q.data()))) return rc;
-  return ati_set_time(h, &t);
+  return ati_case_set_time(h, block_case(h, blk), &t);
 }
 
 extern "C" int ati_write_plot3d_grid(ati_handle_t *h, const char *path) {
   if (!h || !path) return io_fail(h, "ati_write_plot3d_grid: bad argument");
-  ati_config_t cfg;
-  const int nb = nblocks(h, cfg);
+  const int nb = nblocks(h);
   if (nb < 0) return ATI_EINVAL;
   File fl(path, "wb");
   if (!fl.f) return io_fail(h, std::string("ati_write_plot3d_grid: cannot open ") + path);
@@ -119,14 +130,9 @@ extern "C" int ati_write_plot3d_grid(ati_handle_t *h, const char *path) {
 
 extern "C" int ati_write_plot3d_solution(ati_handle_t *h, const char *path) {
   if (!h || !path) return io_fail(h, "ati_write_plot3d_solution: bad argument");
-  ati_config_t cfg;
-  const int nb = nblocks(h, cfg);
+  const int nb = nblocks(h);
   if (nb < 0) return ATI_EINVAL;
-  ati_time_t t;
-  double umf[3], aoa;
-  int rc = ati_get_time(h, &t);
-  if (!rc) rc = ati_get_frame(h, umf, &aoa);
-  if (rc) return rc;
+  int rc = 0;
   File fl(path, "wb");
   if (!fl.f) return io_fail(h, std::string("ati_write_plot3d_solution: cannot open ") + path);
   std::vector<int32_t> hdr{nb};
@@ -137,8 +143,15 @@ extern "C" int ati_write_plot3d_solution(ati_handle_t *h, const char *path) {
     hdr.push_back(d[0] + 1); hdr.push_back(d[1] + 1); hdr.push_back(d[2] + 1);
   }
   if (!put(fl.f, hdr.data(), sizeof(int32_t) * hdr.size())) return io_fail(h, "ati_write_plot3d_solution: write failed");
-  const double mach = std::sqrt(cfg.amach1 * cfg.amach1 + cfg.amach2 * cfg.amach2 + cfg.amach3 * cfg.amach3);
   for (int b = 0; b < nb; b++) {
+    // Mach, AoA, Re and time of the block's case
+    const int cs = block_case(h, b);
+    ati_config_t cfg;
+    ati_time_t t;
+    double umf[3], aoa;
+    if ((rc = ati_case_config(h, cs, &cfg)) || (rc = ati_case_time(h, cs, &t)) || (rc = ati_case_frame(h, cs, umf, &aoa)))
+      return rc;
+    const double mach = std::sqrt(cfg.amach1 * cfg.amach1 + cfg.amach2 * cfg.amach2 + cfg.amach3 * cfg.amach3);
     const int64_t n = np[b];
     std::vector<double> q((size_t)5 * n), p((size_t)n);
     if ((rc = ati_get_state(h, b, q.data()))) return rc;

@@ -259,6 +259,7 @@ struct GlobalSink {
 template <typename TI, typename TO, typename TC>
 struct SweepArgs {
   const BlockDev *blk;
+  const LTile *lt;  // work queue: tile blockIdx.x = lines [t0, t0 + CTA lines) of block b
   const Coef<TC> *cf;
   const TC *fac;
   SweepIO<TI, TO> io;
@@ -269,15 +270,17 @@ struct SweepArgs {
   TC *drva;
 };
 
-// eta and zeta lines: one thread per line; consecutive threads own consecutive xi positions, so each
-// warp access of an eta or zeta sweep is one contiguous row
+// eta and zeta lines: one thread per line; consecutive threads own
+// consecutive xi positions, so each warp access of an eta or zeta sweep is one
+// contiguous row.  A CTA takes SG_LINES lines of one block (one work-queue tile).
 template <int NN, bool FILT, typename TI, typename TO, typename TC>
-__global__ void __launch_bounds__(128) k_sweep_g(SweepArgs<TI, TO, TC> a) {
-  const BlockDev &B = a.blk[blockIdx.y];
-  const int f = blockIdx.z;
+__global__ void __launch_bounds__(SG_LINES) k_sweep_g(SweepArgs<TI, TO, TC> a) {
+  const LTile LT = a.lt[blockIdx.x];
+  const BlockDev &B = a.blk[LT.b];
+  const int f = blockIdx.y;
   int64_t base, stride;
   int jk, L;
-  if (!line_geom<NN>(B, blockIdx.x * blockDim.x + threadIdx.x, base, stride, jk, L)) return;
+  if (!line_geom<NN>(B, LT.t0 + threadIdx.x, base, stride, jk, L)) return;
   const Coef<TC> &C = *a.cf;
   const int ns = B.ndf[0][NN], ne = B.ndf[1][NN];
   const int64_t nbs = B.nbsize[NN];
@@ -308,17 +311,16 @@ __global__ void __launch_bounds__(128) k_sweep_g(SweepArgs<TI, TO, TC> a) {
 // and writes the result of row i at position i.  The six boundary rows use
 // direct loads of the line ends, and the last three forward values stay in
 // registers.  The tile is small (XC_C x XC_NL words), so many CTAs share an SM.
-constexpr int XC_NL = 64;
 constexpr int XC_C = 32;
 
 template <bool FILT, typename TI, typename TO, typename TC>
 __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
   __shared__ TC tile[XC_C][XC_NL + 1];
-  const BlockDev &B = a.blk[blockIdx.y];
-  const int f = blockIdx.z;
+  const LTile LT = a.lt[blockIdx.x];
+  const BlockDev &B = a.blk[LT.b];
+  const int f = blockIdx.y;
   const int L = B.lxi + 1, nline = (B.let + 1) * (B.lze + 1);
-  const int t0 = blockIdx.x * XC_NL;
-  if (t0 >= nline) return;  // uniform over the CTA
+  const int t0 = LT.t0;
   const int nl = min(XC_NL, nline - t0);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   constexpr int NW = XC_NL / 32;
@@ -500,42 +502,50 @@ __global__ void k_mpigo(const BlockDev *blk, const Coef<TC> *cf, const FaceTask 
 }
 
 // ---------------------------------------------------------------------------
-// pointwise stage kernels (grid-stride over all points of all blocks)
+// pointwise stage kernels: each CTA walks the point tiles of the work queue
+// (consecutive points of one case, so per-case constants are per tile)
 // ---------------------------------------------------------------------------
 #define GRID_STRIDE(g, N) \
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < (N); g += (int64_t)gridDim.x * blockDim.x)
+#define TILE_LOOP(e, T) \
+  for (int t_ = blockIdx.x; t_ < (e).npt; t_ += gridDim.x) \
+    if (const PTile T = (e).pt[t_]; true)
+#define POINT_LOOP(T, g) for (int64_t g = (T).g0 + threadIdx.x; g < (T).g1; g += blockDim.x)
 
 // primitives, pressure, temperature, Sutherland viscosity (src/Main3D.f90:576-583)
 template <typename R>
 __global__ void k_prim(Eng<R> e) {
-  const Scheme &S = *e.sc;
   const int64_t N = e.N;
-  const R gamm1 = (R)S.gamm1, gam = (R)S.gam, srefp1dre = (R)S.srefp1dre, srefoo = (R)S.srefoo;
-  int bad = 0;
-  const double rhoE_inf = S.hamm1 * S.poo;
-  GRID_STRIDE(g, N) {
-    const R q1 = (R)e.qa[g], q2 = (R)e.qa[g + N], q3 = (R)e.qa[g + 2 * N], q4 = (R)e.qa[g + 3 * N];
-    const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
-    R pp, d5;
-    if constexpr (Freestream<R>::on) {
-      // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
-      const R re = (R)(e.qa[g + 4 * N] - rhoE_inf);
-      pp = gamm1 * (re - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
-      d5 = gam * ((R)S.poo + pp) * d1;
-    } else {
-      const R q5 = (R)e.qa[g + 4 * N];
-      pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
-      d5 = gam * pp * d1;
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    Scalars &SC = e.scal[T.cs];
+    const R gamm1 = (R)S.gamm1, gam = (R)S.gam, srefp1dre = (R)S.srefp1dre, srefoo = (R)S.srefoo;
+    int bad = 0;
+    const double rhoE_inf = S.hamm1 * S.poo;
+    POINT_LOOP(T, g) {
+      const R q1 = (R)e.qa[g], q2 = (R)e.qa[g + N], q3 = (R)e.qa[g + 2 * N], q4 = (R)e.qa[g + 3 * N];
+      const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
+      R pp, d5;
+      if constexpr (Freestream<R>::on) {
+        // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
+        const R re = (R)(e.qa[g + 4 * N] - rhoE_inf);
+        pp = gamm1 * (re - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
+        d5 = gam * ((R)S.poo + pp) * d1;
+      } else {
+        const R q5 = (R)e.qa[g + 4 * N];
+        pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
+        d5 = gam * pp * d1;
+      }
+      // T^1.5 as T*sqrt(T): the value of pow(T,1.5) to ~1 ulp with far fewer instructions
+      const R mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
+      e.prim[g] = d2; e.prim[g + N] = d3; e.prim[g + 2 * N] = d4; e.prim[g + 3 * N] = d5;
+      e.p[g] = pp;
+      e.mu[g] = mu;
+      const R pabs = Freestream<R>::on ? (R)S.poo + pp : pp;
+      if (!(q1 > (R)0) || !(pabs > (R)0) || !(fabs((double)e.qa[g + 4 * N]) < 1e300)) bad = 1;
     }
-    // T^1.5 as T*sqrt(T): the value of pow(T,1.5) to ~1 ulp with far fewer instructions
-    const R mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
-    e.prim[g] = d2; e.prim[g + N] = d3; e.prim[g + 2 * N] = d4; e.prim[g + 3 * N] = d5;
-    e.p[g] = pp;
-    e.mu[g] = mu;
-    const R pabs = Freestream<R>::on ? (R)S.poo + pp : pp;
-    if (!(q1 > (R)0) || !(pabs > (R)0) || !(fabs((double)e.qa[g + 4 * N]) < 1e300)) bad = 1;
+    if (bad) atomicOr(&SC.flag, 1);
   }
-  if (bad) atomicOr(&e.scal->flag, 1);
 }
 
 __device__ __forceinline__ void atomic_max_pos(unsigned long long *a, double v) {
@@ -546,44 +556,49 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long *a, double v) 
 template <typename R>
 __global__ void k_cfl(Eng<R> e) {
   const int64_t N = e.N;
-  const R u1 = (R)e.scal->umf[1], u2 = (R)e.scal->umf[2], u3 = (R)e.scal->umf[3];
-  R m1 = 0, m2 = 0;
-  GRID_STRIDE(g, N) {
-    const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
-    const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
-    const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
-    const R d2 = e.prim[g] + u1, d3 = e.prim[g + N] + u2, d4 = e.prim[g + 2 * N] + u3;
-    const R r1 = x1 * x1 + x2 * x2 + x3 * x3 + e1 * e1 + e2 * e2 + e3 * e3 + z1 * z1 + z2 * z2 + z3 * z3;
-    const R r2 = fabs(x1 * d2 + x2 * d3 + x3 * d4) + fabs(e1 * d2 + e2 * d3 + e3 * d4) + fabs(z1 * d2 + z2 * d3 + z3 * d4);
-    const R s2 = fabs(e.yaco[g]);
-    const R v1 = (sqrt(e.prim[g + 3 * N] * r1) + r2) * s2;
-    const R d1 = (R)1 / (R)e.qa[g];
-    const R v2 = d1 * e.mu[g] * r1 * s2 * s2;
-    m1 = fmax(m1, v1);
-    m2 = fmax(m2, v2);
-    if (v1 != v1 || v2 != v2) atomicOr(&e.scal->flag, 4);
-  }
-  double dm1 = (double)m1, dm2 = (double)m2;
-  for (int o = 16; o > 0; o >>= 1) {
-    dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
-    dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
-  }
-  __shared__ double s1[32], s2v[32];
-  const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  if (ln == 0) { s1[w] = dm1; s2v[w] = dm2; }
-  __syncthreads();
-  if (w == 0) {
-    const int nw = blockDim.x >> 5;
-    dm1 = ln < nw ? s1[ln] : 0.0;
-    dm2 = ln < nw ? s2v[ln] : 0.0;
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    Scalars &SC = e.scal[T.cs];
+    const R u1 = (R)SC.umf[1], u2 = (R)SC.umf[2], u3 = (R)SC.umf[3];
+    R m1 = 0, m2 = 0;
+    POINT_LOOP(T, g) {
+      const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
+      const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
+      const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+      const R d2 = e.prim[g] + u1, d3 = e.prim[g + N] + u2, d4 = e.prim[g + 2 * N] + u3;
+      const R r1 = x1 * x1 + x2 * x2 + x3 * x3 + e1 * e1 + e2 * e2 + e3 * e3 + z1 * z1 + z2 * z2 + z3 * z3;
+      const R r2 = fabs(x1 * d2 + x2 * d3 + x3 * d4) + fabs(e1 * d2 + e2 * d3 + e3 * d4) + fabs(z1 * d2 + z2 * d3 + z3 * d4);
+      const R s2 = fabs(e.yaco[g]);
+      const R v1 = (sqrt(e.prim[g + 3 * N] * r1) + r2) * s2;
+      const R d1 = (R)1 / (R)e.qa[g];
+      const R v2 = d1 * e.mu[g] * r1 * s2 * s2;
+      m1 = fmax(m1, v1);
+      m2 = fmax(m2, v2);
+      if (v1 != v1 || v2 != v2) atomicOr(&SC.flag, 4);
+    }
+    double dm1 = (double)m1, dm2 = (double)m2;
     for (int o = 16; o > 0; o >>= 1) {
       dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
       dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
     }
-    if (ln == 0) {
-      atomic_max_pos(&e.scal->cflmax[0], dm1);
-      atomic_max_pos(&e.scal->cflmax[1], dm2);
+    __shared__ double s1[32], s2v[32];
+    const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    if (ln == 0) { s1[w] = dm1; s2v[w] = dm2; }
+    __syncthreads();
+    if (w == 0) {
+      const int nw = blockDim.x >> 5;
+      dm1 = ln < nw ? s1[ln] : 0.0;
+      dm2 = ln < nw ? s2v[ln] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
+        dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
+      }
+      if (ln == 0) {
+        atomic_max_pos(&SC.cflmax[0], dm1);
+        atomic_max_pos(&SC.cflmax[1], dm2);
+      }
     }
+    __syncthreads();  // s1/s2v are reused by the next tile
   }
 }
 
@@ -591,57 +606,60 @@ __global__ void k_cfl(Eng<R> e) {
 // (src/Main3D.f90:631-692), from the twelve derivative planes dv
 template <typename R>
 __global__ void k_visc(Eng<R> e) {
-  const Scheme &S = *e.sc;
   const int64_t N = e.N;
-  const R gp = (R)S.gamm1prndtli, tgp = (R)S.tgamm1prndtli, tt = (R)S.two_three;
-  const R sm1 = (R)S.smago1, sm2 = (R)S.smago2;
-  const R *dv = e.dv;
-  R *t = e.tau;
-  GRID_STRIDE(g, N) {
-    const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
-    const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
-    const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
-    R c[4][3];
-#pragma unroll
-    for (int f = 0; f < 4; f++) {
-      const R r1 = dv[g + (f * 3 + 0) * N], r2 = dv[g + (f * 3 + 1) * N], r3 = dv[g + (f * 3 + 2) * N];
-      c[f][0] = x1 * r1 + e1 * r2 + z1 * r3;
-      c[f][1] = x2 * r1 + e2 * r2 + z2 * r3;
-      c[f][2] = x3 * r1 + e3 * r2 + z3 * r3;
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    Scalars &SC = e.scal[T.cs];
+    const R gp = (R)S.gamm1prndtli, tgp = (R)S.tgamm1prndtli, tt = (R)S.two_three;
+    const R sm1 = (R)S.smago1, sm2 = (R)S.smago2;
+    const R *dv = e.dv;
+    R *t = e.tau;
+    POINT_LOOP(T, g) {
+      const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
+      const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
+      const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+      R c[4][3];
+  #pragma unroll
+      for (int f = 0; f < 4; f++) {
+        const R r1 = dv[g + (f * 3 + 0) * N], r2 = dv[g + (f * 3 + 1) * N], r3 = dv[g + (f * 3 + 2) * N];
+        c[f][0] = x1 * r1 + e1 * r2 + z1 * r3;
+        c[f][1] = x2 * r1 + e2 * r2 + z2 * r3;
+        c[f][2] = x3 * r1 + e3 * r2 + z3 * r3;
+      }
+      // txx,hzz,tzx from u; txy,tyy,hxx from v; hyy,tyz,tzz from w; ss(:,1:3) from T
+      R txx = c[0][0], hzz = c[0][1], tzx = c[0][2];
+      R txy = c[1][0], tyy = c[1][1], hxx = c[1][2];
+      R hyy = c[2][0], tyz = c[2][1], tzz = c[2][2];
+      const R yac = e.yaco[g];
+      R r1 = e.mu[g] * yac;
+      R r2 = gp * r1, r3 = 0, d5;
+      if (S.les == 1) {
+        const R d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
+                     (hxx + tyz) * (hxx + tyz);
+        const R varr = (R)pow(-1.0 / (double)yac, 1.5);
+        const R q1 = (R)e.qa[g];
+        r3 = q1 * (sm1 * sm1) * varr * sqrt((R)2 * d1);
+        r1 = r1 + r3 * yac;
+        r2 = r2 + tgp * r3 * yac;
+        r3 = tt * (q1 * sm2 * varr * d1);
+        d5 = tt * (txx + tyy + tzz);
+        txx = r1 * ((R)2 * txx - d5) - r3;
+        tyy = r1 * ((R)2 * tyy - d5) - r3;
+        tzz = r1 * ((R)2 * tzz - d5) - r3;
+      } else {
+        d5 = tt * (txx + tyy + tzz);
+        txx = r1 * ((R)2 * txx - d5);
+        tyy = r1 * ((R)2 * tyy - d5);
+        tzz = r1 * ((R)2 * tzz - d5);
+      }
+      const R ntxy = r1 * (txy + hzz), ntyz = r1 * (tyz + hxx), ntzx = r1 * (tzx + hyy);
+      const R d2 = e.prim[g], d3 = e.prim[g + N], d4 = e.prim[g + 2 * N];
+      t[g] = txx; t[g + N] = tyy; t[g + 2 * N] = tzz;
+      t[g + 3 * N] = ntxy; t[g + 4 * N] = ntyz; t[g + 5 * N] = ntzx;
+      t[g + 6 * N] = r2 * c[3][0] + d2 * txx + d3 * ntxy + d4 * ntzx;
+      t[g + 7 * N] = r2 * c[3][1] + d2 * ntxy + d3 * tyy + d4 * ntyz;
+      t[g + 8 * N] = r2 * c[3][2] + d2 * ntzx + d3 * ntyz + d4 * tzz;
     }
-    // txx,hzz,tzx from u; txy,tyy,hxx from v; hyy,tyz,tzz from w; ss(:,1:3) from T
-    R txx = c[0][0], hzz = c[0][1], tzx = c[0][2];
-    R txy = c[1][0], tyy = c[1][1], hxx = c[1][2];
-    R hyy = c[2][0], tyz = c[2][1], tzz = c[2][2];
-    const R yac = e.yaco[g];
-    R r1 = e.mu[g] * yac;
-    R r2 = gp * r1, r3 = 0, d5;
-    if (S.les == 1) {
-      const R d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
-                   (hxx + tyz) * (hxx + tyz);
-      const R varr = (R)pow(-1.0 / (double)yac, 1.5);
-      const R q1 = (R)e.qa[g];
-      r3 = q1 * (sm1 * sm1) * varr * sqrt((R)2 * d1);
-      r1 = r1 + r3 * yac;
-      r2 = r2 + tgp * r3 * yac;
-      r3 = tt * (q1 * sm2 * varr * d1);
-      d5 = tt * (txx + tyy + tzz);
-      txx = r1 * ((R)2 * txx - d5) - r3;
-      tyy = r1 * ((R)2 * tyy - d5) - r3;
-      tzz = r1 * ((R)2 * tzz - d5) - r3;
-    } else {
-      d5 = tt * (txx + tyy + tzz);
-      txx = r1 * ((R)2 * txx - d5);
-      tyy = r1 * ((R)2 * tyy - d5);
-      tzz = r1 * ((R)2 * tzz - d5);
-    }
-    const R ntxy = r1 * (txy + hzz), ntyz = r1 * (tyz + hxx), ntzx = r1 * (tzx + hyy);
-    const R d2 = e.prim[g], d3 = e.prim[g + N], d4 = e.prim[g + 2 * N];
-    t[g] = txx; t[g + N] = tyy; t[g + 2 * N] = tzz;
-    t[g + 3 * N] = ntxy; t[g + 4 * N] = ntyz; t[g + 5 * N] = ntzx;
-    t[g + 6 * N] = r2 * c[3][0] + d2 * txx + d3 * ntxy + d4 * ntzx;
-    t[g + 7 * N] = r2 * c[3][1] + d2 * ntxy + d3 * tyy + d4 * ntyz;
-    t[g + 8 * N] = r2 * c[3][2] + d2 * ntzx + d3 * ntyz + d4 * tzz;
   }
 }
 
@@ -649,82 +667,85 @@ __global__ void k_visc(Eng<R> e) {
 // (src/Main3D.f90:710-766): flx plane (m-1)*3 + (nn-1)
 template <typename R>
 __global__ void k_flux(Eng<R> e) {
-  const Scheme &S = *e.sc;
   const int64_t N = e.N;
-  const R u1 = (R)e.scal->umf[1], u2 = (R)e.scal->umf[2], u3 = (R)e.scal->umf[3];
-  const bool visc = S.nviscous == 1;
-  const R *t = e.tau;
-  R *F = e.flx;
-  GRID_STRIDE(g, N) {
-    const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
-    const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
-    const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
-    const R pp = e.p[g];
-    R s1, s2, s3;
-    // freestream split: contravariant velocities of u and of umf apart
-    R su1 = 0, su2 = 0, su3 = 0, sm1 = 0, sm2 = 0, sm3 = 0;
-    if constexpr (Freestream<R>::on) {
-      const R r1 = e.prim[g], r2 = e.prim[g + N], r3 = e.prim[g + 2 * N];
-      su1 = x1 * r1 + x2 * r2 + x3 * r3; sm1 = x1 * u1 + x2 * u2 + x3 * u3;
-      su2 = e1 * r1 + e2 * r2 + e3 * r3; sm2 = e1 * u1 + e2 * u2 + e3 * u3;
-      su3 = z1 * r1 + z2 * r2 + z3 * r3; sm3 = z1 * u1 + z2 * u2 + z3 * u3;
-      s1 = su1 + sm1; s2 = su2 + sm2; s3 = su3 + sm3;
-      // rho U - rho_inf (umf . grad xi)
-      const double q1 = e.qa[g];
-      const R q = (R)q1, qp = (R)(q1 - S.rhooo);
-      F[g] = q * su1 + qp * sm1; F[g + N] = q * su2 + qp * sm2; F[g + 2 * N] = q * su3 + qp * sm3;
-    } else {
-      const R r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
-      s1 = x1 * r1 + x2 * r2 + x3 * r3;
-      s2 = e1 * r1 + e2 * r2 + e3 * r3;
-      s3 = z1 * r1 + z2 * r2 + z3 * r3;
-      const R q = (R)e.qa[g];
-      F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
-    }
-    R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
-    if (visc) {
-      ta[0] = t[g]; tb[0] = t[g + 3 * N]; tc[0] = t[g + 5 * N];
-      ta[1] = t[g + 3 * N]; tb[1] = t[g + N]; tc[1] = t[g + 4 * N];
-      ta[2] = t[g + 5 * N]; tb[2] = t[g + 4 * N]; tc[2] = t[g + 2 * N];
-    }
-    const R xm[3] = {x1, x2, x3}, em[3] = {e1, e2, e3}, zm[3] = {z1, z2, z3};
-#pragma unroll
-    for (int m = 2; m <= 4; m++) {
-      const R q = (R)e.qa[g + (m - 1) * N];
-      R a = q * s1 + xm[m - 2] * pp;
-      R b = q * s2 + em[m - 2] * pp;
-      R c = q * s3 + zm[m - 2] * pp;
-      if (visc) {
-        a = a - x1 * ta[m - 2] - x2 * tb[m - 2] - x3 * tc[m - 2];
-        b = b - e1 * ta[m - 2] - e2 * tb[m - 2] - e3 * tc[m - 2];
-        c = c - z1 * ta[m - 2] - z2 * tb[m - 2] - z3 * tc[m - 2];
-      }
-      F[g + ((m - 1) * 3 + 0) * N] = a;
-      F[g + ((m - 1) * 3 + 1) * N] = b;
-      F[g + ((m - 1) * 3 + 2) * N] = c;
-    }
-    {
-      R a, b, c;
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    Scalars &SC = e.scal[T.cs];
+    const R u1 = (R)SC.umf[1], u2 = (R)SC.umf[2], u3 = (R)SC.umf[3];
+    const bool visc = S.nviscous == 1;
+    const R *t = e.tau;
+    R *F = e.flx;
+    POINT_LOOP(T, g) {
+      const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
+      const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
+      const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+      const R pp = e.p[g];
+      R s1, s2, s3;
+      // freestream split: contravariant velocities of u and of umf apart
+      R su1 = 0, su2 = 0, su3 = 0, sm1 = 0, sm2 = 0, sm3 = 0;
       if constexpr (Freestream<R>::on) {
-        // (rhoE + p) U - p (umf . grad xi) - rhoE_inf (umf . grad xi)
-        const double q5 = e.qa[g + 4 * N];
-        const R d5 = (R)q5 + (R)S.poo + pp, re = (R)(q5 - S.hamm1 * S.poo);
-        a = d5 * su1 + re * sm1;
-        b = d5 * su2 + re * sm2;
-        c = d5 * su3 + re * sm3;
+        const R r1 = e.prim[g], r2 = e.prim[g + N], r3 = e.prim[g + 2 * N];
+        su1 = x1 * r1 + x2 * r2 + x3 * r3; sm1 = x1 * u1 + x2 * u2 + x3 * u3;
+        su2 = e1 * r1 + e2 * r2 + e3 * r3; sm2 = e1 * u1 + e2 * u2 + e3 * u3;
+        su3 = z1 * r1 + z2 * r2 + z3 * r3; sm3 = z1 * u1 + z2 * u2 + z3 * u3;
+        s1 = su1 + sm1; s2 = su2 + sm2; s3 = su3 + sm3;
+        // rho U - rho_inf (umf . grad xi)
+        const double q1 = e.qa[g];
+        const R q = (R)q1, qp = (R)(q1 - S.rhooo);
+        F[g] = q * su1 + qp * sm1; F[g + N] = q * su2 + qp * sm2; F[g + 2 * N] = q * su3 + qp * sm3;
       } else {
-        const R d5 = (R)e.qa[g + 4 * N] + pp;
-        a = d5 * s1 - pp * (u1 * x1 + u2 * x2 + u3 * x3);
-        b = d5 * s2 - pp * (u1 * e1 + u2 * e2 + u3 * e3);
-        c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
+        const R r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
+        s1 = x1 * r1 + x2 * r2 + x3 * r3;
+        s2 = e1 * r1 + e2 * r2 + e3 * r3;
+        s3 = z1 * r1 + z2 * r2 + z3 * r3;
+        const R q = (R)e.qa[g];
+        F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
       }
+      R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
       if (visc) {
-        const R ha = t[g + 6 * N], hb = t[g + 7 * N], hc = t[g + 8 * N];
-        a = a - x1 * ha - x2 * hb - x3 * hc;
-        b = b - e1 * ha - e2 * hb - e3 * hc;
-        c = c - z1 * ha - z2 * hb - z3 * hc;
+        ta[0] = t[g]; tb[0] = t[g + 3 * N]; tc[0] = t[g + 5 * N];
+        ta[1] = t[g + 3 * N]; tb[1] = t[g + N]; tc[1] = t[g + 4 * N];
+        ta[2] = t[g + 5 * N]; tb[2] = t[g + 4 * N]; tc[2] = t[g + 2 * N];
       }
-      F[g + 12 * N] = a; F[g + 13 * N] = b; F[g + 14 * N] = c;
+      const R xm[3] = {x1, x2, x3}, em[3] = {e1, e2, e3}, zm[3] = {z1, z2, z3};
+  #pragma unroll
+      for (int m = 2; m <= 4; m++) {
+        const R q = (R)e.qa[g + (m - 1) * N];
+        R a = q * s1 + xm[m - 2] * pp;
+        R b = q * s2 + em[m - 2] * pp;
+        R c = q * s3 + zm[m - 2] * pp;
+        if (visc) {
+          a = a - x1 * ta[m - 2] - x2 * tb[m - 2] - x3 * tc[m - 2];
+          b = b - e1 * ta[m - 2] - e2 * tb[m - 2] - e3 * tc[m - 2];
+          c = c - z1 * ta[m - 2] - z2 * tb[m - 2] - z3 * tc[m - 2];
+        }
+        F[g + ((m - 1) * 3 + 0) * N] = a;
+        F[g + ((m - 1) * 3 + 1) * N] = b;
+        F[g + ((m - 1) * 3 + 2) * N] = c;
+      }
+      {
+        R a, b, c;
+        if constexpr (Freestream<R>::on) {
+          // (rhoE + p) U - p (umf . grad xi) - rhoE_inf (umf . grad xi)
+          const double q5 = e.qa[g + 4 * N];
+          const R d5 = (R)q5 + (R)S.poo + pp, re = (R)(q5 - S.hamm1 * S.poo);
+          a = d5 * su1 + re * sm1;
+          b = d5 * su2 + re * sm2;
+          c = d5 * su3 + re * sm3;
+        } else {
+          const R d5 = (R)e.qa[g + 4 * N] + pp;
+          a = d5 * s1 - pp * (u1 * x1 + u2 * x2 + u3 * x3);
+          b = d5 * s2 - pp * (u1 * e1 + u2 * e2 + u3 * e3);
+          c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
+        }
+        if (visc) {
+          const R ha = t[g + 6 * N], hb = t[g + 7 * N], hc = t[g + 8 * N];
+          a = a - x1 * ha - x2 * hb - x3 * hc;
+          b = b - e1 * ha - e2 * hb - e3 * hc;
+          c = c - z1 * ha - z2 * hb - z3 * hc;
+        }
+        F[g + 12 * N] = a; F[g + 13 * N] = b; F[g + 14 * N] = c;
+      }
     }
   }
 }
@@ -733,42 +754,45 @@ __global__ void k_flux(Eng<R> e) {
 // spongego (src/SingleTurbulence3D.f90:368-372) on sponge points
 template <typename R>
 __global__ void k_div(Eng<R> e) {
-  const Scheme &S = *e.sc;
   const int64_t N = e.N;
-  const R ham = (R)S.ham;
-  const R *F = e.flx;
-  R u1 = 0, u2 = 0, u3 = 0;
-  if constexpr (Freestream<R>::on) {
-    u1 = (R)e.scal->umf[1]; u2 = (R)e.scal->umf[2]; u3 = (R)e.scal->umf[3];
-  }
-  GRID_STRIDE(g, N) {
-    const R as = e.asz[g], bs = e.bsz[g];
-    const bool sponge = as != (R)0 || bs != (R)0;
-    R fs[5] = {0, 0, 0, 0, 0};
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    Scalars &SC = e.scal[T.cs];
+    const R ham = (R)S.ham;
+    const R *F = e.flx;
+    R u1 = 0, u2 = 0, u3 = 0;
     if constexpr (Freestream<R>::on) {
-      // divergence of the freestream fluxes: rho_inf, p_inf, rhoE_inf times the metric divergence
-      const R g1 = e.gm[g], g2 = e.gm[g + N], g3 = e.gm[g + 2 * N];
-      const R ug = u1 * g1 + u2 * g2 + u3 * g3;
-      fs[0] = (R)S.rhooo * ug;
-      fs[1] = (R)S.poo * g1; fs[2] = (R)S.poo * g2; fs[3] = (R)S.poo * g3;
-      fs[4] = (R)(S.hamm1 * S.poo) * ug;
+      u1 = (R)SC.umf[1]; u2 = (R)SC.umf[2]; u3 = (R)SC.umf[3];
     }
-#pragma unroll
-    for (int m = 1; m <= 5; m++) {
-      R d = F[g + ((m - 1) * 3 + 0) * N] + F[g + ((m - 1) * 3 + 1) * N] + F[g + ((m - 1) * 3 + 2) * N];
-      if constexpr (Freestream<R>::on) d = d + fs[m - 1];
-      if (sponge) {
-        if constexpr (Freestream<R>::on) {  // the pressure plane already holds p - p_inf, p_inf = 1/gamma
-          if (m == 1) d = d + as * (R)(e.qa[g] - 1.0);
-          else if (m <= 4) d = d + as * (R)e.qa[g + (m - 1) * N];
-          else d = d + bs * e.p[g];
-        } else {
-          if (m == 1) d = d + as * ((R)e.qa[g] - (R)1);
-          else if (m <= 4) d = d + as * ((R)e.qa[g + (m - 1) * N] - (R)0);
-          else d = d + bs * (e.p[g] - ham * (R)1);
-        }
+    POINT_LOOP(T, g) {
+      const R as = e.asz[g], bs = e.bsz[g];
+      const bool sponge = as != (R)0 || bs != (R)0;
+      R fs[5] = {0, 0, 0, 0, 0};
+      if constexpr (Freestream<R>::on) {
+        // divergence of the freestream fluxes: rho_inf, p_inf, rhoE_inf times the metric divergence
+        const R g1 = e.gm[g], g2 = e.gm[g + N], g3 = e.gm[g + 2 * N];
+        const R ug = u1 * g1 + u2 * g2 + u3 * g3;
+        fs[0] = (R)S.rhooo * ug;
+        fs[1] = (R)S.poo * g1; fs[2] = (R)S.poo * g2; fs[3] = (R)S.poo * g3;
+        fs[4] = (R)(S.hamm1 * S.poo) * ug;
       }
-      e.de[g + (m - 1) * N] = d;
+  #pragma unroll
+      for (int m = 1; m <= 5; m++) {
+        R d = F[g + ((m - 1) * 3 + 0) * N] + F[g + ((m - 1) * 3 + 1) * N] + F[g + ((m - 1) * 3 + 2) * N];
+        if constexpr (Freestream<R>::on) d = d + fs[m - 1];
+        if (sponge) {
+          if constexpr (Freestream<R>::on) {  // the pressure plane already holds p - p_inf, p_inf = 1/gamma
+            if (m == 1) d = d + as * (R)(e.qa[g] - 1.0);
+            else if (m <= 4) d = d + as * (R)e.qa[g + (m - 1) * N];
+            else d = d + bs * e.p[g];
+          } else {
+            if (m == 1) d = d + as * ((R)e.qa[g] - (R)1);
+            else if (m <= 4) d = d + as * ((R)e.qa[g + (m - 1) * N] - (R)0);
+            else d = d + bs * (e.p[g] - ham * (R)1);
+          }
+        }
+        e.de[g + (m - 1) * N] = d;
+      }
     }
   }
 }
@@ -777,11 +801,15 @@ __global__ void k_div(Eng<R> e) {
 template <typename R>
 __global__ void k_rk(Eng<R> e) {
   const int64_t N = e.N;
-  const double dtk = e.scal->dtk;
-  GRID_STRIDE(g, N) {
-    const double r1 = dtk * e.yacod[g];
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    Scalars &SC = e.scal[T.cs];
+    const double dtk = SC.dtk;
+    POINT_LOOP(T, g) {
+      const double r1 = dtk * e.yacod[g];
 #pragma unroll
-    for (int q = 0; q < 5; q++) e.qa[g + q * N] = e.qo[g + q * N] - r1 * (double)e.de[g + q * N];
+      for (int q = 0; q < 5; q++) e.qa[g + q * N] = e.qo[g + q * N] - r1 * (double)e.de[g + q * N];
+    }
   }
 }
 
@@ -887,8 +915,9 @@ __global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const Scheme &S = *e.sc;
   const BlockDev &B = e.blk[T.b];
+  const Scheme &S = e.sc[B.cs];
+  const Scalars &SC = e.scal[B.cs];
   const int nn = T.nn, ip = T.ip, np = T.bc;
   int i, j, k;
   face_point(B, nn, ip, jk, i, j, k);
@@ -897,7 +926,7 @@ __global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
   R *drva = e.drva + B.face_off[nn] * 10;
   const R *cmv = e.cm + B.face_off[nn] * 6;
   const R cm[3] = {cmv[jk + nbs * (0 + 3 * ip)], cmv[jk + nbs * (1 + 3 * ip)], cmv[jk + nbs * (2 + 3 * ip)]};
-  const R umf[4] = {0, (R)e.scal->umf[1], (R)e.scal->umf[2], (R)e.scal->umf[3]};
+  const R umf[4] = {0, (R)SC.umf[1], (R)SC.umf[2], (R)SC.umf[3]};
   Elem<R> el;
   eleme(S, e, g, cm, umf, el);
   R xt[5][5];
@@ -935,8 +964,9 @@ __global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const Scheme &S = *e.sc;
   const BlockDev &B = e.blk[T.b];
+  const Scheme &S = e.sc[B.cs];
+  const Scalars &SC = e.scal[B.cs];
   const int nn = T.nn, ip = T.ip, np = T.bc, iq = 1 - 2 * ip;
   const R ra0 = (R)iq;
   int i, j, k;
@@ -945,7 +975,7 @@ __global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
   const R *drva = e.drva + B.face_off[nn] * 10;
   const R *cmv = e.cm + B.face_off[nn] * 6;
   const R cm[3] = {cmv[jk + nbs * (0 + 3 * ip)], cmv[jk + nbs * (1 + 3 * ip)], cmv[jk + nbs * (2 + 3 * ip)]};
-  const R umf[4] = {0, (R)e.scal->umf[1], (R)e.scal->umf[2], (R)e.scal->umf[3]};
+  const R umf[4] = {0, (R)SC.umf[1], (R)SC.umf[2], (R)SC.umf[3]};
   Elem<R> el;
   eleme(S, e, g, cm, umf, el);
   R cha[5], d0[5];
@@ -956,7 +986,7 @@ __global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
     if (ra0 * (el.vn + el.vs - el.ao) > (R)0) cha[4] = 0;
   } else if (np == 20 || np == 25) {
     if (e.rpex[T.wall_off + jk] == (R)0) {
-      const R s = cm[0] * (R)e.scal->dudtmf[1] + cm[1] * (R)e.scal->dudtmf[2] + cm[2] * (R)e.scal->dudtmf[3];
+      const R s = cm[0] * (R)SC.dudtmf[1] + cm[1] * (R)SC.dudtmf[2] + cm[2] * (R)SC.dudtmf[3];
       cha[3 + ip] = cha[4 - ip] + (R)2 * ra0 * el.aoi * (R)e.qa[g] * (s + (R)50 * (el.vn + el.vs));
     }
   } else {  // 30: characteristic interface, incoming waves from the neighbour
@@ -999,8 +1029,9 @@ __global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk >= T.nline) return;
-  const Scheme &S = *e.sc;
   const BlockDev &B = e.blk[T.b];
+  const Scheme &S = e.sc[B.cs];
+  const Scalars &SC = e.scal[B.cs];
   int i, j, k;
   face_point(B, T.nn, T.ip, jk, i, j, k);
   const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = e.N;
@@ -1009,9 +1040,9 @@ __global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
   const double rp = e.rpex[T.wall_off + jk];
   const double ra2 = 1.0 - rp, ra3 = 1.0 - ra1 * ra2;
   const double fctr = (1.0 - ra3) * e.qa[g];
-  const double q2 = ra3 * e.qa[g + N] - fctr * e.scal->umf[1];
-  const double q3 = ra3 * e.qa[g + 2 * N] - fctr * e.scal->umf[2];
-  const double q4 = ra3 * e.qa[g + 3 * N] - fctr * e.scal->umf[3];
+  const double q2 = ra3 * e.qa[g + N] - fctr * SC.umf[1];
+  const double q3 = ra3 * e.qa[g + 2 * N] - fctr * SC.umf[2];
+  const double q4 = ra3 * e.qa[g + 3 * N] - fctr * SC.umf[3];
   e.qa[g + N] = q2; e.qa[g + 2 * N] = q3; e.qa[g + 3 * N] = q4;
   const double q1 = e.qa[g];
   e.qa[g + 4 * N] = rp * e.qa[g + 4 * N] + ra2 * (ra0 * q1 + 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
@@ -1119,9 +1150,11 @@ __device__ void d_movef(const Scheme &S, Scalars &s, double dtko, double dtk) {
   }
 }
 
-__global__ void k_scalar(const Scheme *sc, Scalars *scal, int op, int nk) {
-  const Scheme &S = *sc;
-  Scalars &s = *scal;
+__global__ void k_scalar(const Scheme *sc, Scalars *scal, int ncase, int op, int nk) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;  // one thread per case
+  if (c >= ncase) return;
+  const Scheme &S = sc[c];
+  Scalars &s = scal[c];
   const int nkrk = S.nkrk;
   if (op == SC_MOVEF_A) {
     const double dtko = s.dt * min(max(nk - 2, 0), 1) / (nkrk - nk + 3);
@@ -1193,9 +1226,9 @@ __global__ void k_forces(Eng<R> e, const FaceTask *tasks, const double *area, co
     const int64_t g = B.off + ((int64_t)kk * (B.let + 1) + jw) * (B.lxi + 1) + ii;
     const double w1 = wn[ll], w2 = wn[ll + nw], w3 = wn[ll + 2 * nw];
     for (int dir = 0; dir < 2; dir++) {
-      const double pw = Freestream<R>::on ? (double)e.p[g] + e.sc->poo : (double)e.p[g];
+      const double pw = Freestream<R>::on ? (double)e.p[g] + e.sc[B.cs].poo : (double)e.p[g];
       double v = pw * (dir == 0 ? w1 : w2) * ar[ll];
-      if (e.sc->nviscous == 1) {
+      if (e.sc[B.cs].nviscous == 1) {
         const R *t = e.tau;
         double tw;
         if (dir == 0) tw = e.qa[g] * ((double)t[g] * w1 + (double)t[g + 3 * N] * w2 + (double)t[g + 5 * N] * w3);
@@ -1236,11 +1269,11 @@ __global__ void k_metric_div(const double *d3, int64_t N, float *gm) {
 // launchers
 // ---------------------------------------------------------------------------
 template <typename TI, typename TO, typename TC>
-static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const SweepIO<TI, TO> &io, int nblocks,
-                    int maxlines, int maxlen) {
-  (void)maxlen;
+static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const SweepIO<TI, TO> &io) {
+  if (e.nlt[nn] == 0) return;
   SweepArgs<TI, TO, TC> a;
   a.blk = e.blk;
+  a.lt = e.lt[nn];
   a.cf = e.cf;
   a.fac = filt ? e.facf : e.facd;
   a.io = io;
@@ -1249,14 +1282,13 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   a.recv = e.recv;
   a.recv_fs = e.F * 6;
   a.drva = e.drva;
+  const dim3 grid(e.nlt[nn], io.nf);
   if (nn == 1) {
-    dim3 grid((maxlines + XC_NL - 1) / XC_NL, nblocks, io.nf);
     if (filt) k_sweep_xc<true, TI, TO, TC><<<grid, XC_NL, 0, st>>>(a);
     else k_sweep_xc<false, TI, TO, TC><<<grid, XC_NL, 0, st>>>(a);
     return;
   }
-  const int tpb = 128;
-  dim3 grid((maxlines + tpb - 1) / tpb, nblocks, io.nf);
+  const int tpb = SG_LINES;
   if (!filt) {
     if (nn == 2) k_sweep_g<2, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
     else k_sweep_g<3, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
@@ -1266,17 +1298,14 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   }
 }
 
-void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,
-               int nblocks, int maxlines, int maxlen) {
-  sweep_t<double, double, double>(e, st, nn, filt, io, nblocks, maxlines, maxlen);
+void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io) {
+  sweep_t<double, double, double>(e, st, nn, filt, io);
 }
-void sweep_fff(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io,
-               int nblocks, int maxlines, int maxlen) {
-  sweep_t<float, float, float>(e, st, nn, filt, io, nblocks, maxlines, maxlen);
+void sweep_fff(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io) {
+  sweep_t<float, float, float>(e, st, nn, filt, io);
 }
-void sweep_ddf(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,
-               int nblocks, int maxlines, int maxlen) {
-  sweep_t<double, double, float>(e, st, nn, filt, io, nblocks, maxlines, maxlen);
+void sweep_ddf(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io) {
+  sweep_t<double, double, float>(e, st, nn, filt, io);
 }
 
 template <typename TI, typename TC>
@@ -1308,7 +1337,8 @@ static int pw_grid(int64_t N) {
 
 template <typename R>
 static void pointwise_t(const Eng<R> &e, cudaStream_t st, int which) {
-  const int g = pw_grid(e.N), t = 256;
+  if (e.npt == 0) return;
+  const int g = e.npt < 152 * 16 ? e.npt : 152 * 16, t = 256;  // CTAs walk the point tiles
   switch (which) {
     case PW_PRIM: k_prim<R><<<g, t, 0, st>>>(e); break;
     case PW_CFL: k_cfl<R><<<g, t, 0, st>>>(e); break;
@@ -1354,7 +1384,9 @@ void junction(const Eng<double> &e, cudaStream_t st, const JunctionDev *jn, int 
   k_junction<<<dim3((nk + tpb - 1) / tpb, njct), tpb, 0, st>>>(e, jn, njct);
 }
 
-void scalar(const Eng<double> &e, cudaStream_t st, int op, int nk) { k_scalar<<<1, 1, 0, st>>>(e.sc, e.scal, op, nk); }
+void scalar(const Eng<double> &e, cudaStream_t st, int op, int nk) {
+  k_scalar<<<(e.ncase + 63) / 64, 64, 0, st>>>(e.sc, e.scal, e.ncase, op, nk);
+}
 
 void metrics(const Eng<double> &e, cudaStream_t st, const double *xyz) {
   (void)xyz;

@@ -24,13 +24,20 @@ struct Coef {
   T aa, ab, ac;
 };
 
-// Device pointers of one case for intermediates of type R, passed by value.
+// Device pointers of a handle (one case or a batch) for intermediates of
+// type R, passed by value.  Per-case data (sc, scal) is indexed by the case
+// of a block (BlockDev::cs) or of a point tile (PTile::cs).
 template <typename R>
 struct Eng {
   const BlockDev *blk;
-  const Scheme *sc;
-  const Coef<R> *cf;
-  Scalars *scal;
+  const Scheme *sc;     // [ncase]
+  const Coef<R> *cf;    // shared: every case of a batch runs the same scheme
+  Scalars *scal;        // [ncase]
+  int ncase;
+  const PTile *pt;      // pointwise work queue
+  int npt;
+  const LTile *lt[4];   // line-sweep work queue per direction nn = 1..3
+  int nlt[4];
   int64_t N;            // points of all blocks
   double *qa, *qo;      // state (5 planes each), FP64
   const double *yacod;  // Jacobian, FP64 (RK update)
@@ -88,6 +95,12 @@ struct SweepIO {
   TI ofs[5];
 };
 
+// lines per work-queue tile: xi sweeps (shared-memory chunks), eta/zeta sweeps
+constexpr int XC_NL = 64;
+constexpr int SG_LINES = 128;
+// points per pointwise work-queue tile
+constexpr int PT_POINTS = 4096;
+
 // per-field offsets of a closure (mpigo) over a wider input type
 template <typename TI>
 struct FieldOfs {
@@ -99,12 +112,9 @@ struct FieldOfs {
 // launchers exist for (in, out, compute) = (d,d,d), (f,f,f) and (d,d,f).
 #define ATI_DECLARE_LAUNCHERS(NS)                                                                                  \
   namespace NS {                                                                                                   \
-  void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,      \
-                 int nblocks, int maxlines, int maxlen);                                                           \
-  void sweep_fff(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io,         \
-                 int nblocks, int maxlines, int maxlen);                                                           \
-  void sweep_ddf(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io,       \
-                 int nblocks, int maxlines, int maxlen);                                                           \
+  void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io); \
+  void sweep_fff(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<float, float> &io); \
+  void sweep_ddf(const Eng<float> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io); \
   void mpigo_ddd(const Eng<double> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,      \
                  int n45, const double *s1, const double *s2, const double *s3, int64_t fs, int nf);              \
   void mpigo_fff(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,       \

@@ -69,6 +69,14 @@ SIGNATURES = {
     "ati_read_restart": ([_vp, _i32, ctypes.c_char_p], ctypes.c_int),
     "ati_write_plot3d_grid": ([_vp, ctypes.c_char_p], ctypes.c_int),
     "ati_write_plot3d_solution": ([_vp, ctypes.c_char_p], ctypes.c_int),
+    "ati_create_batch": ([_vp, _i32, ctypes.POINTER(_vp)], ctypes.c_int),
+    "ati_case_count": ([_vp, _vp], ctypes.c_int),
+    "ati_case_blocks": ([_vp, _i32, _vp, _vp], ctypes.c_int),
+    "ati_case_time": ([_vp, _i32, _vp], ctypes.c_int),
+    "ati_case_set_time": ([_vp, _i32, _vp], ctypes.c_int),
+    "ati_case_config": ([_vp, _i32, _vp], ctypes.c_int),
+    "ati_case_forces": ([_vp, _i32, _dp], ctypes.c_int),
+    "ati_case_frame": ([_vp, _i32, _dp, _dp], ctypes.c_int),
 }
 
 KERNEL_CLASSES = ["deriv_xi", "deriv_eta", "deriv_zeta", "filter_xi", "filter_eta", "filter_zeta", "mpigo",
@@ -116,8 +124,11 @@ class Case:
         if rc:
             raise AtiError(rc, self.L.ati_last_error(None).decode())
         self.h = h
+        self._dims(cfg.nblocks)
+
+    def _dims(self, nblocks):
         self.dims = []
-        for mb in range(cfg.nblocks):
+        for mb in range(nblocks):
             d = (ctypes.c_int32 * 3)()
             n = ctypes.c_int64()
             self._chk(self.L.ati_block_dims(self.h, mb, d, ctypes.byref(n)))
@@ -274,6 +285,61 @@ class Case:
 
     def write_plot3d_solution(self, path):
         self._chk(self.L.ati_write_plot3d_solution(self.h, os.fsencode(path)))
+
+
+class Batch(Case):
+    """Several independent cases in one handle (ati_create_batch): one launch
+    per kernel and one CUDA graph per step cover every case.  Blocks are
+    numbered across the batch (case c owns blocks 6c..6c+5); ``block(c, mb)``
+    maps a case's own block number."""
+
+    def __init__(self, cfgs, lib_path=LIB_PATH):
+        self.L = load_library(lib_path)
+        self.cfgs = list(cfgs)
+        self.cfg = self.cfgs[0]
+        arr = (type(self.cfg.to_c()) * len(self.cfgs))(*[c.to_c() for c in self.cfgs])
+        self._c = arr
+        h = ctypes.c_void_p()
+        rc = self.L.ati_create_batch(arr, len(self.cfgs), ctypes.byref(h))
+        if rc:
+            raise AtiError(rc, self.L.ati_last_error(None).decode())
+        self.h = h
+        self._dims(sum(c.nblocks for c in self.cfgs))
+
+    @property
+    def ncase(self):
+        return len(self.cfgs)
+
+    def block(self, cs, mb):
+        first, n = ctypes.c_int(), ctypes.c_int()
+        self._chk(self.L.ati_case_blocks(self.h, cs, ctypes.byref(first), ctypes.byref(n)))
+        assert 0 <= mb < n.value
+        return first.value + mb
+
+    def case_state(self, cs):
+        return [self.get_state(self.block(cs, mb)) for mb in range(self.cfgs[cs].nblocks)]
+
+    def case_time(self, cs):
+        t = AtiTime()
+        self._chk(self.L.ati_case_time(self.h, cs, ctypes.byref(t)))
+        return t.as_tuple()
+
+    def case_forces(self, cs):
+        out = np.zeros(2)
+        self._chk(self.L.ati_case_forces(self.h, cs, _dp_of(out)))
+        return out
+
+
+def setup_batch(cfgs, grids=None):
+    """Create a batch, upload every case's aerofoil grid and run the set-up."""
+    from .grid import aerofoil_grid
+    b = Batch(cfgs)
+    for cs, cfg in enumerate(b.cfgs):
+        g = aerofoil_grid(cfg) if grids is None else grids[cs]
+        for mb in range(cfg.nblocks):
+            b.set_grid(b.block(cs, mb), g[mb])
+    b.init()
+    return b
 
 
 def probe_fma_tflops(fp64=True):
