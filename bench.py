@@ -179,6 +179,72 @@ def run_reference(args, cfg, grid):
     return line
 
 
+def batch_leg(args, barrier):
+    """The batched form: 16 independent cases (seed 7; NACA 00tt, t in 8-18 %, AoA 0-8 deg, M 0.2-0.4, 1-6 M
+    points each, spanwise 16-48) in one handle, mixed precision; against the same cases run one handle at a time."""
+    import torch
+    from tandemproject_gb300.solver import Case, setup_batch
+    from tandemproject_gb300.workloads import batch_cases, fold_free_case
+    cases = batch_cases(16, seed=7)
+    cg = []
+    for c, _ in cases:  # fold-free grids (checked on the GPU one case at a time)
+        cfg, g, h = fold_free_case(c)
+        h.close()
+        cg.append((cfg, g))
+    cfgs = [c for c, _ in cg]
+    npts = sum(c.npoints for c in cfgs)
+    b = setup_batch(cfgs, grids=[g for _, g in cg])
+    st = torch.cuda.ExternalStream(b.stream())
+    b.step(args.warmup)
+    barrier()
+    l0 = b.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.step(args.steps)
+    e1.record(st)
+    barrier()
+    t_b = e0.elapsed_time(e1) / 1e3
+    launches = b.launch_count() - l0
+    b.close()
+    # the same cases, one handle at a time, same steps
+    t_seq = 0.0
+    for cfg, (_, g) in zip(cfgs, cg):
+        c = Case(cfg)
+        for mb in range(cfg.nblocks):
+            c.set_grid(mb, g[mb])
+        c.init()
+        c.step(args.warmup)
+        s1 = torch.cuda.ExternalStream(c.stream())
+        barrier()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(s1)
+        c.step(args.steps)
+        a1.record(s1)
+        barrier()
+        t_seq += a0.elapsed_time(a1) / 1e3
+        c.close()
+    return {"workload": "16 cases, seed 7: NACA 00tt t 8-18 %, AoA 0-8 deg, M 0.2-0.4, 1-6 M points (uneven), "
+                        "spanwise 16-48, mixed precision, one handle (ati_create_batch)",
+            "points": npts, "value": npts * 4 * args.steps / t_b, "unit": UNIT, "ms_per_step": t_b / args.steps * 1e3,
+            "gpu_launches_per_step": launches / args.steps,
+            "one_case_at_a_time": {"value": npts * 4 * args.steps / t_seq, "ms_per_step": t_seq / args.steps * 1e3},
+            "batching_speedup": t_seq / t_b,
+            "note": "inflow turbulence intensity is drawn per case but not applied (no inflow-turbulence generator)"}
+
+
+def serve_leg(args):
+    """The serving form: Poisson arrivals (4/s, seed 99), sizes log-uniform 0.5-20 M points, admitted by device
+    footprint under a 150 GB budget, mixed precision; step counts U[200,2000] scaled to keep the run short."""
+    from tandemproject_gb300.serve import Server
+    from tandemproject_gb300.workloads import serving_requests
+    reqs = serving_requests(args.serve_requests, seed=99, rate=4.0, step_scale=args.serve_step_scale)
+    done, summary = Server(budget_bytes=150 << 30).run(reqs)
+    summary["workload"] = (f"{args.serve_requests} requests, seed 99, Poisson 4/s, 0.5-20 M points log-uniform, "
+                           f"steps U[200,2000] x {args.serve_step_scale}, 150 GB budget, mixed precision")
+    summary["unit_latency"] = "s"
+    return summary
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -189,6 +255,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-mixed", dest="mixed", action="store_false")
+    ap.add_argument("--no-batch", dest="batch", action="store_false")
+    ap.add_argument("--no-serve", dest="serve", action="store_false")
+    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-step-scale", type=float, default=0.1)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -372,6 +442,10 @@ def main():
     if mixed is not None:
         line["mixed"] = mixed
     case.close()
+    if args.batch:
+        line["batch"] = batch_leg(args, barrier)
+    if args.serve and rank == 0:
+        line["serving"] = serve_leg(args)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(cfg, grid)
     if rank == 0:

@@ -168,6 +168,13 @@ int ati_set_grid(ati_handle_t *h, int blk, const double *xyz);
  * the initial condition of initialo (:203) with n = 0, dt = 0. */
 int ati_init(ati_handle_t *h);
 
+/* Grid check after ati_init (no counterpart in the reference): flags[b] for
+ * every block b has bit 0 set if some Jacobian J = yaco is positive, bit 1 if
+ * some is negative, bit 2 if some is zero or not finite.  A block whose J
+ * changes sign (flags 3) folds under the compact-derivative metrics, and the
+ * reference's scheme diverges on it within a few dozen steps. */
+int ati_jacobian_sign(ati_handle_t *h, int32_t *flags);
+
 /* State and field copies (block blk, Fortran layout, all components). */
 int ati_set_state(ati_handle_t *h, int blk, const double *q);
 int ati_get_state(ati_handle_t *h, int blk, double *q);
@@ -198,6 +205,14 @@ int ati_rk_stage(ati_handle_t *h, int nk);
 /* nsteps full time steps: filter, nkrk stages, n += 1, timo += dt
  * (src/Main3D.f90:552-965).  Returns ATI_ENONFINITE if the state blew up. */
 int ati_step(ati_handle_t *h, int nsteps);
+/* For a host that drives many handles at once (no counterpart in the
+ * reference): ati_step_async issues the steps and returns without waiting;
+ * ati_query sets *idle = 1 once the handle's stream has finished its work;
+ * ati_check waits for it and returns ati_step's status (ATI_ENONFINITE if
+ * the state blew up). */
+int ati_step_async(ati_handle_t *h, int nsteps);
+int ati_query(ati_handle_t *h, int *idle);
+int ati_check(ati_handle_t *h);
 
 /* ---- instrumentation (no counterpart in the reference) ------------------
  * With profiling enabled every kernel launch of the handle is bracketed by

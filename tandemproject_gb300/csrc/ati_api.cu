@@ -346,6 +346,19 @@ __global__ void k_wall_probe(Eng<double> c, const FaceTask *tasks, int ntask, in
   if (blockIdx.x == 0 && threadIdx.x == 0) tbuf[r] = c.scal->timo;
 }
 
+// sign of the Jacobian over each block: bit 0 some J > 0, bit 1 some J < 0, bit 2 J = 0 or not finite
+__global__ void k_jac_sign(Eng<double> c, int *flags) {
+  const BlockDev &B = c.blk[blockIdx.y];
+  int f = 0;
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < B.npts; l += (int64_t)gridDim.x * blockDim.x) {
+    const double y = c.yaco[B.off + l];
+    if (y > 0.0 && y < 1e300) f |= 1;
+    else if (y < 0.0 && y > -1e300) f |= 2;
+    else f |= 4;
+  }
+  if (f) atomicOr(&flags[blockIdx.y], f);
+}
+
 __global__ void k_to_double(const float *src, double *dst, int64_t n, double add) {
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     dst[g] = (double)src[g] + add;
@@ -901,6 +914,20 @@ extern "C" int ati_set_time(ati_handle_t *h, const ati_time_t *t) {
   return ATI_OK;
 }
 
+extern "C" int ati_jacobian_sign(ati_handle_t *h, int32_t *flags) {
+  if (!h || !flags) return fail(h, ATI_EINVAL, "ati_jacobian_sign: bad argument");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  int *d = reinterpret_cast<int *>(h->fw1);  // the granular scratch plane is free outside granular calls
+  CK(cudaMemsetAsync(d, 0, sizeof(int) * h->nb, h->st));
+  k_jac_sign<<<dim3(64, h->nb), 256, 0, h->st>>>(h->ed, d);
+  CKL();
+  std::vector<int> f(h->nb);
+  CK(cudaMemcpyAsync(f.data(), d, sizeof(int) * h->nb, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int b = 0; b < h->nb; b++) flags[b] = f[b];
+  return ATI_OK;
+}
+
 extern "C" int ati_case_count(ati_handle_t *h, int *ncase) {
   if (!h || !ncase) return fail(h, ATI_EINVAL, "ati_case_count: bad argument");
   *ncase = h->ncase;
@@ -1253,7 +1280,7 @@ static int step_graph(ati_handle *h) {
   return ATI_OK;
 }
 
-extern "C" int ati_step(ati_handle_t *h, int nsteps) {
+static int issue_steps(ati_handle *h, int nsteps) {
   if (!h) return fail(h, ATI_EINVAL, "null handle");
   if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
   if (nsteps < 0) return fail(h, ATI_EINVAL, "nsteps < 0");
@@ -1268,6 +1295,27 @@ extern "C" int ati_step(ati_handle_t *h, int nsteps) {
     h->n_host++;
     h->steps_done++;
   }
+  return ATI_OK;
+}
+
+extern "C" int ati_step(ati_handle_t *h, int nsteps) {
+  int rc = issue_steps(h, nsteps);
+  return rc ? rc : check_flag(h);
+}
+
+extern "C" int ati_step_async(ati_handle_t *h, int nsteps) { return issue_steps(h, nsteps); }
+
+extern "C" int ati_query(ati_handle_t *h, int *idle) {
+  if (!h || !idle) return fail(h, ATI_EINVAL, "ati_query: bad argument");
+  const cudaError_t e = cudaStreamQuery(h->st);
+  if (e == cudaSuccess) *idle = 1;
+  else if (e == cudaErrorNotReady) *idle = 0;
+  else return fail(h, ATI_ECUDA, std::string("cudaStreamQuery: ") + cudaGetErrorString(e));
+  return ATI_OK;
+}
+
+extern "C" int ati_check(ati_handle_t *h) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
   return check_flag(h);
 }
 

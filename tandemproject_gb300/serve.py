@@ -1,0 +1,137 @@
+"""Serving loop: aerofoil solves arrive over time, are admitted by device-
+memory footprint under a budget, stay resident on the GPU while they run, and
+leave when their steps are done.  Admission is continuous: a request that
+arrives while others are running starts as soon as memory is free, and the
+work of all running requests overlaps on the device (one CUDA stream per
+case, steps issued in chunks without waiting).
+
+    python -m tandemproject_gb300.serve --requests 16 --step-scale 0.1
+
+Each request's result (final state, forces) is the same as when it runs
+alone: cases share nothing on the device.
+"""
+import argparse
+import concurrent.futures as cf
+import json
+import time
+
+import numpy as np
+
+from .workloads import fold_free_case, footprint_bytes, relax, serving_requests, valid_grid
+
+
+def _gpu_case(cfg, grid):
+    from .solver import Case
+    c = Case(cfg)
+    for mb in range(cfg.nblocks):
+        c.set_grid(mb, grid[mb])
+    c.init()
+    if c.folded_blocks():  # the grid folds under the compact metrics: take a relaxed grid of the same size
+        c.close()
+        _, _, c = fold_free_case(relax(cfg))
+    return c
+
+
+class Server:
+    def __init__(self, budget_bytes=150 << 30, chunk=10, prefetch=4, keep_state=False, make_case=_gpu_case,
+                 make_grid=valid_grid, footprint=footprint_bytes):
+        self.budget = budget_bytes
+        self.chunk = chunk
+        self.prefetch = prefetch
+        self.keep_state = keep_state
+        self.make_case = make_case
+        self.make_grid = make_grid
+        self.footprint = footprint
+        self.peak_bytes = 0
+
+    def run(self, requests, log=None):
+        """Serve the requests (arrival times in seconds from the start);
+        return one record per request and the run summary."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        waiting, active, done = [], [], []
+        used = 0
+        grids = {}
+        pool = cf.ThreadPoolExecutor(max_workers=self.prefetch)
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        while pending or waiting or active:
+            t = now()
+            while pending and pending[0].arrival <= t:
+                r = pending.pop(0)
+                waiting.append(r)
+                grids[r.rid] = pool.submit(self.make_grid, r.cfg)  # host-side grid, ahead of admission
+            # admit in arrival order while the footprint fits
+            while waiting:
+                r = waiting[0]
+                fp = self.footprint(r.cfg)
+                if used + fp > self.budget and active:
+                    break
+                waiting.pop(0)
+                cfg, grid = grids.pop(r.rid).result()
+                c = self.make_case(cfg, grid)
+                used += fp
+                self.peak_bytes = max(self.peak_bytes, used)
+                active.append({"req": r, "case": c, "left": r.steps, "fp": fp, "admitted": now(), "npts": cfg.npoints})
+                if log:
+                    log(f"t={now():7.2f}s admit #{r.rid} {cfg.npoints / 1e6:.2f} M pts x {r.steps} steps, "
+                        f"{used / 2**30:.1f} GiB in use")
+            # one chunk of steps for every running case, issued without waiting
+            for a in active:
+                if a["left"] > 0 and a["case"].idle():
+                    k = min(self.chunk, a["left"])
+                    a["case"].step_async(k)
+                    a["left"] -= k
+            # retire finished cases
+            for a in list(active):
+                if a["left"] == 0 and a["case"].idle():
+                    c = a["case"]
+                    c.check()
+                    rec = {"id": a["req"].rid, "points": a["npts"], "steps": a["req"].steps,
+                           "arrival": a["req"].arrival, "admitted": a["admitted"], "done": now(),
+                           "forces": c.forces().tolist()}
+                    if self.keep_state:
+                        rec["state"] = [c.get_state(mb) for mb in range(c.cfg.nblocks)]
+                    rec["latency"] = rec["done"] - rec["arrival"]
+                    c.close()
+                    used -= a["fp"]
+                    active.remove(a)
+                    done.append(rec)
+                    if log:
+                        log(f"t={now():7.2f}s done  #{rec['id']} latency {rec['latency']:.2f} s")
+            if not pending and not waiting and active:
+                time.sleep(0.0005)
+            elif pending and not waiting and not active:
+                time.sleep(max(0.0, min(pending[0].arrival - now(), 0.05)))
+        pool.shutdown()
+        makespan = now()
+        lat = np.array([d["latency"] for d in done])
+        work = sum(d["points"] * 4 * d["steps"] for d in done)
+        summary = {"requests": len(done), "makespan_s": makespan,
+                   "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                                 "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+                   "updates_per_s": work / makespan, "peak_resident_gib": self.peak_bytes / 2**30}
+        return done, summary
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--requests", type=int, default=16)
+    ap.add_argument("--rate", type=float, default=4.0)
+    ap.add_argument("--seed", type=int, default=99)
+    ap.add_argument("--step-scale", type=float, default=1.0)
+    ap.add_argument("--budget-gb", type=float, default=150.0)
+    ap.add_argument("--precision", type=int, default=1, help="0 = FP64, 1 = mixed")
+    ap.add_argument("--chunk", type=int, default=10)
+    ap.add_argument("--quiet", action="store_true")
+    args = ap.parse_args()
+    reqs = serving_requests(args.requests, seed=args.seed, rate=args.rate, precision=args.precision,
+                            step_scale=args.step_scale)
+    srv = Server(budget_bytes=int(args.budget_gb * 2**30), chunk=args.chunk)
+    done, summary = srv.run(reqs, log=None if args.quiet else (lambda m: print(m, flush=True)))
+    summary.update({"precision": "mixed" if args.precision == 1 else "fp64", "rate_per_s": args.rate,
+                    "seed": args.seed, "step_scale": args.step_scale, "budget_gb": args.budget_gb})
+    print(json.dumps(summary))
+
+
+if __name__ == "__main__":
+    main()

@@ -70,6 +70,10 @@ SIGNATURES = {
     "ati_write_plot3d_grid": ([_vp, ctypes.c_char_p], ctypes.c_int),
     "ati_write_plot3d_solution": ([_vp, ctypes.c_char_p], ctypes.c_int),
     "ati_create_batch": ([_vp, _i32, ctypes.POINTER(_vp)], ctypes.c_int),
+    "ati_step_async": ([_vp, _i32], ctypes.c_int),
+    "ati_jacobian_sign": ([_vp, _vp], ctypes.c_int),
+    "ati_query": ([_vp, _vp], ctypes.c_int),
+    "ati_check": ([_vp], ctypes.c_int),
     "ati_case_count": ([_vp, _vp], ctypes.c_int),
     "ati_case_blocks": ([_vp, _i32, _vp, _vp], ctypes.c_int),
     "ati_case_time": ([_vp, _i32, _vp], ctypes.c_int),
@@ -219,6 +223,28 @@ class Case:
 
     def step(self, nsteps=1):
         return self._chk(self.L.ati_step(self.h, nsteps))
+
+    def jacobian_sign(self):
+        """Per block: bit 0 some J > 0, bit 1 some J < 0, bit 2 J zero or not finite."""
+        f = (ctypes.c_int32 * len(self.dims))()
+        self._chk(self.L.ati_jacobian_sign(self.h, f))
+        return list(f)
+
+    def folded_blocks(self):
+        return [b for b, f in enumerate(self.jacobian_sign()) if f not in (1, 2)]
+
+    def step_async(self, nsteps=1):
+        """Issue nsteps on the case's stream without waiting."""
+        self._chk(self.L.ati_step_async(self.h, nsteps))
+
+    def idle(self):
+        v = ctypes.c_int()
+        self._chk(self.L.ati_query(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
+    def check(self):
+        """Wait for the issued steps; raise if the state blew up."""
+        self._chk(self.L.ati_check(self.h))
 
     def synchronize(self):
         self._chk(self.L.ati_synchronize(self.h))

@@ -47,3 +47,22 @@ def test_batch_cases_have_own_dt(ati_lib):
     dts = [b.case_time(cs)[2] for cs in range(b.ncase)]
     assert len(set(dts)) == 3 and all(d > 0 for d in dts)
     b.close()
+
+
+def test_jacobian_sign_check(ati_lib):
+    """ati_jacobian_sign: one sign per block on a good grid; the wake-line cells
+    of a coarse-eta grid fold under the compact metrics and are reported."""
+    from tandemproject_gb300.config import PRESETS
+    from tandemproject_gb300.solver import setup_case
+    from tandemproject_gb300.workloads import batch_cases, fold_free_case, valid_grid
+    c = setup_case(PRESETS["naca0012_0p2m"])
+    assert c.folded_blocks() == [] and len(set(c.jacobian_sign())) == 1
+    c.close()
+    coarse = batch_cases(16, seed=7)[5][0].replace(lxibk=(109,) * 3, letbk=(34, 34), lzebk=(45,), smgrid=0.0075)
+    cfg, g = valid_grid(coarse)
+    c = setup_case(cfg, grid=g)
+    assert c.folded_blocks() == [2]
+    c.close()
+    cfg, g, c = fold_free_case(coarse)
+    assert c.folded_blocks() == [] and cfg.letbk[0] > coarse.letbk[0]
+    c.close()
