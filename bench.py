@@ -14,7 +14,10 @@ buffers (pinned host -> device copy of the state and device -> host copy of
 the result inside every step), the roofline of the dominant kernel measured
 live from profiled launches, a CPU baseline (the CPU restatement of the
 reference, all host cores, bounded sample), clocks sampled during the timed
-region and the number of kernel launches.  Under torchrun every rank runs an
+region and the number of kernel launches.  Sub-objects report the same case
+in mixed precision ("mixed"), 16 independent cases in one batched handle
+("batch") and a serving run with Poisson arrivals and p50/p95/p99 latency
+("serving").  Under torchrun every rank runs an
 independent replica of the case (the path has no exchange between GPUs);
 value is the sum over ranks divided by the slowest rank's time.
 

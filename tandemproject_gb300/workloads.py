@@ -49,11 +49,12 @@ def valid_grid(cfg, tries=4):
 
 def relax(cfg):
     """The same case with about the same point count and 25 % more eta lines
-    (a coarse eta resolution is what folds the wake-line cells)."""
-    nx, ny, nz = cfg.lxibk[0] + 1, cfg.letbk[0] + 1, cfg.lzebk[0] + 1
-    ny2 = int(round(ny * 1.25))
-    nx2 = max(24, int(round(nx * ny / ny2)))
-    return cfg.replace(lxibk=(nx2 - 1,) * 3, letbk=(ny2 - 1,) * 2, smgrid=min(0.0075, max(0.002, 1.0 / nx2)))
+    (a coarse eta resolution is what folds the wake-line cells); xi sizes
+    shrink in proportion."""
+    f = 1.25
+    let = tuple(int(round((v + 1) * f)) - 1 for v in cfg.letbk)
+    lxi = tuple(max(23, int(round((v + 1) / f)) - 1) for v in cfg.lxibk)
+    return cfg.replace(lxibk=lxi, letbk=let, smgrid=min(0.0075, max(0.002, 1.0 / (lxi[1] + 1))))
 
 
 def fold_free_case(cfg, tries=4):

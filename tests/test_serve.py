@@ -76,14 +76,15 @@ def test_results_same_alone_and_in_the_mix(ati_lib):
     from tandemproject_gb300.serve import Server
     from tandemproject_gb300.solver import setup_case
     cfgs = [small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), precision=1),
-            small_case(lxibk=(32, 96, 32), letbk=(31, 31), lzebk=(12,), mach=0.3, aoa_deg=4.0, precision=1),
-            small_case(lxibk=(40, 100, 40), letbk=(35, 35), lzebk=(16,), mach=0.2, precision=0)]
+            small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(15,), mach=0.3, aoa_deg=4.0, precision=1),
+            small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), mach=0.2, thick=15.0, precision=0)]
     reqs = [Request(i, c, s, 0.002 * i, {}) for i, (c, s) in enumerate(zip(cfgs, (30, 17, 24)))]
     srv = Server(budget_bytes=8 << 30, chunk=4, keep_state=True)
     done, summary = srv.run(reqs)
     assert summary["requests"] == 3
     for d in done:
         alone = setup_case(cfgs[d["id"]])
+        assert alone.folded_blocks() == []  # the server kept the requested grid
         alone.step(reqs[d["id"]].steps)
         for mb, q in enumerate(d["state"]):
             np.testing.assert_array_equal(q, alone.get_state(mb))
