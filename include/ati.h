@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define ATI_ABI_VERSION 1
+#define ATI_ABI_VERSION 2
 #define ATI_MAX_BK 8 /* max blocks per grid direction */
 
 /* ---- status codes ------------------------------------------------------ */
@@ -108,7 +108,9 @@ typedef struct ati_config {
   int32_t nsmf;               /* 1: frame velocity = freestream at once        */
   int32_t les;                /* 1: Smagorinsky LES branch                     */
   int32_t precision;          /* ATI_FP64 or ATI_MIXED                         */
-  int32_t reserved_i[7];
+  int32_t turb_modes;         /* inflow turbulence: Fourier modes (0: none)    */
+  int32_t turb_seed;          /* seed of the mode directions and phases        */
+  int32_t reserved_i[5];
   double reoo, tempoo;          /* Reynolds number, freestream temperature (K) */
   double amach1, amach2, amach3;/* freestream Mach components                 */
   double wtemp;                 /* wall temperature ratio                      */
@@ -120,7 +122,10 @@ typedef struct ati_config {
   double smago1, smago2;        /* LES constants                               */
   double domlen, span;          /* domain length, span (inputp.dat)            */
   double szth1, szth2, szxt, szco; /* sponge thicknesses and strength         */
-  double reserved_d[8];
+  double turb_intensity;        /* inflow turbulence: rms of each velocity
+                                   component as a fraction of |U_inf|          */
+  double turb_length;           /* von Karman integral length scale            */
+  double reserved_d[6];
 } ati_config_t;
 
 /* Time-marching scalars (src/MainVar3D.f90:121,141), restart header order
@@ -167,6 +172,25 @@ int ati_set_grid(ati_handle_t *h, int blk, const double *xyz);
  * (:443-480), sponge (spongeup, src/SingleTurbulence3D.f90:209-249), and
  * the initial condition of initialo (:203) with n = 0, dt = 0. */
 int ati_init(ati_handle_t *h);
+
+/* Synthetic inflow turbulence (new: the reference's own inflow-eddy generator
+ * is disabled, src/SingleTurbulence3D.f90:260).  With turb_modes > 0 the sponge
+ * of spongego (src/SingleTurbulence3D.f90:332-374) drives the points of the
+ * inflow sponge zone (x < -0.7 domlen + szth1) towards a turbulent target
+ * instead of rest, through the reference's gust form: rho_t = (1 - (gamma-1)/2
+ * |v|^2)^(1/(gamma-1)), momentum target atz rho_t v, pressure target
+ * rho_t^gamma / gamma, atz = sin^2(min(pi (x + domlen) / szth1, pi/2)).  The
+ * velocity is a sum of turb_modes Fourier modes of a von Karman spectrum
+ * (E(k) ~ (k/ke)^4 / (1 + (k/ke)^2)^(17/6), ke = 0.747 / turb_length), with
+ * directions, polarisations and phases uniform from turb_seed, divergence free,
+ * scaled to turb_intensity |U_inf| rms per component and convected with the
+ * freestream: v(x, t) = sum_n 2 a_n s_n cos(k_n . (x - U_inf t) + psi_n).  The
+ * field is evaluated once per time step (at its start time) in FP32.
+ * ati_turbulence_modes copies case cs's table (8 floats per mode: k_x, k_y,
+ * k_z, s_x, s_y, s_z, a, psi) and ati_turbulence_sample evaluates v at n given
+ * points (xyz: x[n], y[n], z[n]; v likewise) at time t on the device. */
+int ati_turbulence_modes(ati_handle_t *h, int cs, float *modes, int32_t *nmodes);
+int ati_turbulence_sample(ati_handle_t *h, int cs, double t, int64_t n, const double *xyz, double *v);
 
 /* Grid check after ati_init (no counterpart in the reference): flags[b] for
  * every block b has bit 0 set if some Jacobian J = yaco is positive, bit 1 if

@@ -29,6 +29,7 @@ SOURCES = [
     ("ati_probe.cu", "ati_probe.o", []),
     ("ati_noalloc.cu", "ati_noalloc.o", ["-fmad=false"]),
     ("ati_io.cpp", "ati_io.o", []),
+    ("ati_turb.cu", "ati_turb.o", []),
 ]
 
 

@@ -26,7 +26,8 @@ class AtiConfig(ctypes.Structure):
         ("lzebk", ctypes.c_int32 * MAX_BK),
         ("nkrk", ctypes.c_int32), ("nviscous", ctypes.c_int32), ("nsmf", ctypes.c_int32),
         ("les", ctypes.c_int32), ("precision", ctypes.c_int32),
-        ("reserved_i", ctypes.c_int32 * 7),
+        ("turb_modes", ctypes.c_int32), ("turb_seed", ctypes.c_int32),
+        ("reserved_i", ctypes.c_int32 * 5),
         ("reoo", ctypes.c_double), ("tempoo", ctypes.c_double),
         ("amach1", ctypes.c_double), ("amach2", ctypes.c_double), ("amach3", ctypes.c_double),
         ("wtemp", ctypes.c_double), ("cfl", ctypes.c_double), ("timf", ctypes.c_double),
@@ -37,7 +38,8 @@ class AtiConfig(ctypes.Structure):
         ("domlen", ctypes.c_double), ("span", ctypes.c_double),
         ("szth1", ctypes.c_double), ("szth2", ctypes.c_double), ("szxt", ctypes.c_double),
         ("szco", ctypes.c_double),
-        ("reserved_d", ctypes.c_double * 8),
+        ("turb_intensity", ctypes.c_double), ("turb_length", ctypes.c_double),
+        ("reserved_d", ctypes.c_double * 6),
     ]
 
 
@@ -91,6 +93,11 @@ class CaseConfig:
     wlea: float = 0.0
     chord: float = 1.0
     delt_deg: float = 0.0
+    # synthetic inflow turbulence (0 intensity: none)
+    turb_intensity: float = 0.0  # rms per velocity component / |U_inf|
+    turb_length: float = 0.1     # von Karman integral length (chord units)
+    turb_modes: int = 2048
+    turb_seed: int = 1234
 
     @property
     def bkx(self):
@@ -144,6 +151,8 @@ class CaseConfig:
         c.smago1, c.smago2 = self.smago1, self.smago2
         c.domlen, c.span = self.domlen, self.span
         c.szth1, c.szth2, c.szxt, c.szco = self.szth1, self.szth2, self.szxt, self.szco
+        c.turb_modes = self.turb_modes if self.turb_intensity > 0 else 0
+        c.turb_seed, c.turb_intensity, c.turb_length = self.turb_seed, self.turb_intensity, self.turb_length
         return c
 
     def replace(self, **kw):
@@ -156,7 +165,10 @@ PRESETS = {
     "naca0012_0p2m": CaseConfig(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,)),
     # smgrid scales the near-wall spacing with resolution so that the quintic
     # grid lines of gridf stay monotone (no folded cells) at these sizes
-    "naca0012_8p8m": CaseConfig(lxibk=(383, 383, 383), letbk=(119, 119), lzebk=(31,), smgrid=0.0025),
+    # the plain-FP64 larger configuration: seeded von Karman inflow turbulence,
+    # 2.5 % of U_inf, integral length 0.1 c, 2048 modes from seed 1234
+    "naca0012_8p8m": CaseConfig(lxibk=(383, 383, 383), letbk=(119, 119), lzebk=(31,), smgrid=0.0025,
+                                turb_intensity=0.025),
     # a 3.5 M-point case (2.4 GB FP64 arena, state larger than L2) for profiler captures
     "naca0012_3p5m": CaseConfig(lxibk=(255, 255, 255), letbk=(95, 95), lzebk=(23,), smgrid=0.004),
     "naca0012_25m": CaseConfig(lxibk=(639, 639, 639), letbk=(199, 199), lzebk=(31,), smgrid=0.002,

@@ -17,11 +17,13 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/ati.h"
 #include "ati_internal.h"
 #include "ati_kernels.h"
+#include "ati_turb.h"
 #include "ati_scheme.h"
 
 using namespace ati;
@@ -89,6 +91,13 @@ struct ati_handle {
   std::vector<Ev> ev_used, ev_free;
   double prof_ms[ATI_K_NSLOTS] = {0};
   int64_t prof_n[ATI_K_NSLOTS] = {0};
+  // synthetic inflow turbulence: mode tables per case, gust points, their target deltas
+  std::vector<float> hmodes;
+  std::vector<TurbCase> htc;
+  float *dmodes = nullptr, *ddelta = nullptr;
+  TurbCase *dtc = nullptr;
+  GustPt *dgust = nullptr;
+  int64_t ngust = 0;
   // surface-pressure recorder (ring buffer of wall pressure on the mid-span lines)
   int probe_cap = 0;
   int64_t probe_npts = 0, probe_n0 = 0;
@@ -595,6 +604,16 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     if (cfgs[c].dto < 0) h->any_cfl = true;
   }
   h->sh = h->shc[0];
+  for (int c = 0; c < ncase; c++) {  // inflow-turbulence modes, concatenated over cases
+    std::vector<float> m;
+    build_modes(cfgs[c], m);
+    TurbCase tc{};
+    tc.off = (int)(h->hmodes.size() / 8);
+    tc.n = (int)(m.size() / 8);
+    for (int q = 0; q < 3; q++) tc.u[q] = h->shc[c].s.uoo[q + 1];
+    h->htc.push_back(tc);
+    h->hmodes.insert(h->hmodes.end(), m.begin(), m.end());
+  }
   std::vector<double> facd, facf, spg;
   int rc = build_tables(h, facd, facf, spg);
   if (rc) {
@@ -778,6 +797,8 @@ extern "C" int ati_destroy(ati_handle_t *h) {
   }
   drop_graphs(h);
   probe_free(h);
+  for (void *p : {(void *)h->dmodes, (void *)h->ddelta, (void *)h->dtc, (void *)h->dgust})
+    if (p) cudaFree(p);
   if (h->arena) cudaFree(h->arena);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
@@ -914,6 +935,36 @@ extern "C" int ati_set_time(ati_handle_t *h, const ati_time_t *t) {
   return ATI_OK;
 }
 
+extern "C" int ati_turbulence_modes(ati_handle_t *h, int cs, float *modes, int32_t *nmodes) {
+  if (!h || !nmodes || cs < 0 || cs >= h->ncase) return fail(h, ATI_EINVAL, "ati_turbulence_modes: bad argument");
+  *nmodes = h->htc[cs].n;
+  if (modes) std::memcpy(modes, h->hmodes.data() + 8 * (size_t)h->htc[cs].off, sizeof(float) * 8 * h->htc[cs].n);
+  return ATI_OK;
+}
+
+extern "C" int ati_turbulence_sample(ati_handle_t *h, int cs, double t, int64_t n, const double *xyz, double *v) {
+  if (!h || cs < 0 || cs >= h->ncase || n < 0 || (n > 0 && (!xyz || !v)))
+    return fail(h, ATI_EINVAL, "ati_turbulence_sample: bad argument");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  if (!h->dtc || h->htc[cs].n == 0) return fail(h, ATI_EINVAL, "ati_turbulence_sample: the case has no inflow turbulence");
+  if (n == 0) return ATI_OK;
+  double *d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * 6 * n) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, ATI_ENOMEM, "ati_turbulence_sample: device allocation failed");
+  }
+  cudaError_t e = cudaMemcpyAsync(d, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->st);
+  if (e == cudaSuccess) {
+    turb_sample(h->st, h->dtc, cs, h->dmodes, t, n, d, d + 3 * n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(v, d + 3 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(h, ATI_ECUDA, std::string("ati_turbulence_sample: ") + cudaGetErrorString(e));
+  return ATI_OK;
+}
+
 extern "C" int ati_jacobian_sign(ati_handle_t *h, int32_t *flags) {
   if (!h || !flags) return fail(h, ATI_EINVAL, "ati_jacobian_sign: bad argument");
   if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
@@ -993,6 +1044,52 @@ static int to_float(ati_handle *h, const double *src, const float *dst, int64_t 
   return ATI_OK;
 }
 
+// gust points of the inflow-turbulence cases: sponge points of the inflow zone
+// (x < -0.7 domlen + szth1, spongeup src/SingleTurbulence3D.f90:252-258), with
+// the streamwise ramp atz = sin^2(min(pi (x + domlen) / szth1, pi / 2)); each
+// case's list is padded to whole CTAs of the evaluation kernel
+static int setup_gust(ati_handle *h) {
+  if (h->hmodes.empty()) return ATI_OK;
+  const int64_t N = h->N;
+  std::vector<double> xyz((size_t)3 * N), asz(N);
+  CK(cudaMemcpyAsync(xyz.data(), h->ss, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(asz.data(), h->ed.asz, sizeof(double) * N, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const double pi = std::acos(-1.0);
+  std::vector<GustPt> pts;
+  const int nbc = h->nb / h->ncase;
+  for (int cs = 0; cs < h->ncase; cs++) {
+    if (h->htc[cs].n == 0) continue;
+    const ati_config_t &cfg = h->cfgs[cs];
+    const double xg = -(double)0.7f * cfg.domlen + cfg.szth1, ra0 = pi / cfg.szth1;
+    const size_t first = pts.size();
+    for (int b = h->case_b0[cs]; b < h->case_b0[cs] + nbc; b++) {
+      const BlockDev &B = h->blk[b];
+      for (int64_t g = B.off; g < B.off + B.npts; g++) {
+        const double x = xyz[g];
+        if (!(asz[g] > 0.0) || !(x < xg)) continue;
+        const double s = std::sin(std::fmin(ra0 * (x + cfg.domlen), 0.5 * pi));
+        pts.push_back(GustPt{g, (float)x, (float)xyz[g + N], (float)xyz[g + 2 * N], (float)(s * s), cs, 0});
+      }
+    }
+    while ((pts.size() - first) % 256) pts.push_back(GustPt{-1, 0.f, 0.f, 0.f, 0.f, cs, 0});
+  }
+  h->ngust = (int64_t)pts.size();
+  if (h->ngust == 0) return ATI_OK;
+  auto alloc = [&](void **p, size_t n) { return cudaMalloc(p, n) == cudaSuccess; };
+  if (!alloc((void **)&h->dgust, sizeof(GustPt) * pts.size()) || !alloc((void **)&h->ddelta, sizeof(float) * 5 * pts.size()) ||
+      !alloc((void **)&h->dmodes, sizeof(float) * h->hmodes.size()) || !alloc((void **)&h->dtc, sizeof(TurbCase) * h->ncase)) {
+    cudaGetLastError();
+    return fail(h, ATI_ENOMEM, "inflow turbulence: device allocation failed");
+  }
+  CK(cudaMemcpyAsync(h->dgust, pts.data(), sizeof(GustPt) * pts.size(), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->dmodes, h->hmodes.data(), sizeof(float) * h->hmodes.size(), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->dtc, h->htc.data(), sizeof(TurbCase) * h->ncase, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemsetAsync(h->ddelta, 0, sizeof(float) * 5 * pts.size(), h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return ATI_OK;
+}
+
 extern "C" int ati_init(ati_handle_t *h) {
   if (!h) return fail(h, ATI_EINVAL, "null handle");
   for (int b = 0; b < h->nb; b++)
@@ -1056,6 +1153,10 @@ extern "C" int ati_init(ati_handle_t *h) {
     strict::metric_divergence(c, h->st, c.flx, const_cast<float *>(m.gm));
     CKL();
     rc = to_float(h, c.drva, const_cast<float *>(m.drvm), 10 * h->F);
+    if (rc) return rc;
+  }
+  {
+    int rc = setup_gust(h);
     if (rc) return rc;
   }
   // initial condition and time scalars (src/Main3D.f90:520-522)
@@ -1192,6 +1293,12 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
     PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io));
   }
   PROF(h, ATI_K_DIV, C::pw(strict, e, st, PW_DIV));
+  if (h->ngust) {  // inflow turbulence: the gust targets of the inflow sponge, evaluated once per step
+    if (nk == 1) PROF(h, ATI_K_DIV, gust_eval(st, h->dgust, h->ngust, h->dtc, h->dmodes, ed.scal, h->ddelta, h->sh.s.gam));
+    if constexpr (std::is_same<R, float>::value)
+      PROF(h, ATI_K_DIV, gust_apply_f(st, h->dgust, h->ngust, h->ddelta, ed.asz, ed.bsz, e.de, N));
+    else PROF(h, ATI_K_DIV, gust_apply_d(st, h->dgust, h->ngust, h->ddelta, ed.asz, ed.bsz, e.de, N));
+  }
   // characteristic boundary conditions (src/Main3D.f90:780-869)
   if (h->tl_gcbc.n) PROF(h, ATI_K_GCBC, C::face(strict, e, st, FK_GCBC_PREP, tp(h, h->tl_gcbc), h->tl_gcbc.n, h->tl_gcbc.maxline));
   for (int d = 1; d <= 3; d++)

@@ -72,6 +72,8 @@ SIGNATURES = {
     "ati_create_batch": ([_vp, _i32, ctypes.POINTER(_vp)], ctypes.c_int),
     "ati_step_async": ([_vp, _i32], ctypes.c_int),
     "ati_jacobian_sign": ([_vp, _vp], ctypes.c_int),
+    "ati_turbulence_modes": ([_vp, _i32, _vp, _vp], ctypes.c_int),
+    "ati_turbulence_sample": ([_vp, _i32, ctypes.c_double, ctypes.c_int64, _dp, _dp], ctypes.c_int),
     "ati_query": ([_vp, _vp], ctypes.c_int),
     "ati_check": ([_vp], ctypes.c_int),
     "ati_case_count": ([_vp, _vp], ctypes.c_int),
@@ -223,6 +225,22 @@ class Case:
 
     def step(self, nsteps=1):
         return self._chk(self.L.ati_step(self.h, nsteps))
+
+    def turbulence_modes(self, cs=0):
+        """(nmodes, 8) float32 table: k_x, k_y, k_z, s_x, s_y, s_z, a, psi."""
+        n = ctypes.c_int32()
+        self._chk(self.L.ati_turbulence_modes(self.h, cs, None, ctypes.byref(n)))
+        out = np.empty((n.value, 8), dtype=np.float32)
+        self._chk(self.L.ati_turbulence_modes(self.h, cs, out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(n)))
+        return out
+
+    def turbulence_sample(self, xyz, t, cs=0):
+        """Inflow-turbulence velocity (3, n) at points xyz (3, n) and time t."""
+        a = np.ascontiguousarray(xyz, dtype=np.float64)
+        n = a.shape[1]
+        v = np.empty((3, n))
+        self._chk(self.L.ati_turbulence_sample(self.h, cs, float(t), n, _dp_of(a), _dp_of(v)))
+        return v
 
     def jacobian_sign(self):
         """Per block: bit 0 some J > 0, bit 1 some J < 0, bit 2 J zero or not finite."""

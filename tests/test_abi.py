@@ -28,13 +28,24 @@ def test_python_binding_covers_header(ati_lib):
     names = set(declared(os.path.join(ROOT, "include", "ati.h")))
     assert names <= set(solver.SIGNATURES), names - set(solver.SIGNATURES)
     lib = solver.load_library(ati_lib)
-    assert lib.ati_abi_version() == 1
+    assert lib.ati_abi_version() == 2
 
 
 def test_oracle_exports_every_declared_symbol(oracle_lib):
     lib = ctypes.CDLL(oracle_lib)
     missing = [n for n in declared(os.path.join(ROOT, "oracle", "ati_oracle.h")) if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_config_struct_matches_header():
+    """The ctypes mirror of ati_config_t has the C layout: 39 int32 (156 B, padded
+    to 160) then 31 doubles; the turbulence fields took reserved slots, so the
+    size is unchanged."""
+    import ctypes as ct
+    from tandemproject_gb300.config import AtiConfig
+    assert ct.sizeof(AtiConfig) == 160 + 31 * 8
+    assert AtiConfig.turb_modes.offset == 32 * 4 and AtiConfig.reoo.offset == 160
+    assert AtiConfig.turb_intensity.offset == 160 + 23 * 8
 
 
 def test_create_fails_loudly_without_gpu(ati_lib):
