@@ -145,7 +145,8 @@ def cpu_baseline(cfg, grid, sample_steps=2, warm_steps=1):
     return {"value": cfg.npoints * cfg.nkrk * sample_steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{sample_steps} time steps ({sample_steps * cfg.nkrk} RK stages) of the full "
                       f"{cfg.npoints}-point case after {warm_steps} warm-up step, CPU restatement (oracle/), "
-                      f"OpenMP over lines, {cores} threads"}
+                      f"OpenMP over lines, {cores} threads; the restatement has no inflow turbulence (new code "
+                      f"without a reference counterpart), so its inflow sponge targets rest"}
 
 
 def run_reference(args, cfg, grid):
@@ -183,8 +184,9 @@ def run_reference(args, cfg, grid):
 
 
 def batch_leg(args, barrier):
-    """The batched form: 16 independent cases (seed 7; NACA 00tt, t in 8-18 %, AoA 0-8 deg, M 0.2-0.4, 1-6 M
-    points each, spanwise 16-48) in one handle, mixed precision; against the same cases run one handle at a time."""
+    """The batched form: 16 independent cases (seed 7; NACA 00tt, t in 8-18 %, AoA 0-8 deg, M 0.2-0.4, inflow
+    turbulence 0-5 %, 1-6 M points each, spanwise 16-48) in one handle, mixed precision; against the same cases run
+    one handle at a time."""
     import torch
     from tandemproject_gb300.solver import Case, setup_batch
     from tandemproject_gb300.workloads import batch_cases, fold_free_case
@@ -232,7 +234,7 @@ def batch_leg(args, barrier):
             "gpu_launches_per_step": launches / args.steps,
             "one_case_at_a_time": {"value": npts * 4 * args.steps / t_seq, "ms_per_step": t_seq / args.steps * 1e3},
             "batching_speedup": t_seq / t_b,
-            "note": "inflow turbulence intensity is drawn per case but not applied (no inflow-turbulence generator)"}
+            "note": "each case has von Karman inflow turbulence of its drawn intensity (2048 modes, L = 0.1 c)"}
 
 
 def serve_leg(args):
@@ -435,7 +437,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: NACA 0012 grid from the reference's grid generator (restated), uniform freestream "
-                    "initial state, impulsive start (nsmf = 1)",
+                    "initial state, impulsive start (nsmf = 1); seeded von Karman inflow turbulence when the "
+                    "preset has it (2.5 % of U_inf, L = 0.1 c, 2048 modes, seed 1234)",
             "config": {"workload": f"{args.preset}: NACA 0012, 6 blocks "
                                    f"{'x'.join(str(v + 1) for v in (cfg.lxibk[0], cfg.letbk[0], cfg.lzebk[0]))}, "
                                    f"{npts} points, FP64, RK4, Re 4e5, M 0.24",

@@ -1067,7 +1067,7 @@ static int setup_gust(ati_handle *h) {
       const BlockDev &B = h->blk[b];
       for (int64_t g = B.off; g < B.off + B.npts; g++) {
         const double x = xyz[g];
-        if (!(asz[g] > 0.0) || !(x < xg)) continue;
+        if (asz[g] == 0.0 || !(x < xg)) continue;  // asz carries the sign of 1/J
         const double s = std::sin(std::fmin(ra0 * (x + cfg.domlen), 0.5 * pi));
         pts.push_back(GustPt{g, (float)x, (float)xyz[g + N], (float)xyz[g + 2 * N], (float)(s * s), cs, 0});
       }

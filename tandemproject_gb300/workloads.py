@@ -2,9 +2,8 @@
 independent cases stepped together) and the serving form (requests arriving
 over time).  Parameters follow the case ranges of those forms: NACA 00tt
 thickness t in U[8,18] %, angle of attack in U[0,8] deg, Mach in U[0.2,0.4],
-inflow turbulence intensity in U[0,5] % (recorded with each case; the
-synthetic inflow-turbulence generator is not part of this package, so the
-cases run without it), uneven grid sizes, spanwise 16-48 points.  Every case
+inflow turbulence intensity in U[0,5] % (von Karman, 2048 modes, integral
+length 0.1 chord), uneven grid sizes, spanwise 16-48 points.  Every case
 starts from rest with the reference deck's smooth frame ramp (nsmf = 0) over
 one time unit: an impulsive start on these grids diverges within a few
 hundred steps for the thicker sections and higher Mach numbers.
@@ -73,8 +72,10 @@ def fold_free_case(cfg, tries=4):
 
 
 def _params(rng):
+    tu = float(rng.uniform(0.0, 5.0))
     return dict(thick=float(rng.uniform(8.0, 18.0)), aoa_deg=float(rng.uniform(0.0, 8.0)),
-                mach=float(rng.uniform(0.2, 0.4))), float(rng.uniform(0.0, 5.0))
+                mach=float(rng.uniform(0.2, 0.4)), turb_intensity=tu / 100.0, turb_length=0.1, turb_modes=2048,
+                turb_seed=int(rng.integers(1, 2**31 - 1))), tu
 
 
 def batch_cases(n=16, seed=7, precision=MIXED, nmin=1.0e6, nmax=6.0e6):
