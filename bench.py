@@ -443,7 +443,9 @@ def main():
                                    f"{'x'.join(str(v + 1) for v in (cfg.lxibk[0], cfg.letbk[0], cfg.lzebk[0]))}, "
                                    f"{npts} points, FP64, RK4, Re 4e5, M 0.24",
                        "points": npts, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                       "l2": "no flush: the state alone (5 x 8 B x points) exceeds the 129 MB L2"},
+                       "l2": "no flush: the state alone (5 x 8 B x points) exceeds the 129 MB L2",
+                       "tiles": dict(zip(("xi_lines_per_cta", "eta_zeta_lines_per_cta", "points_per_tile"),
+                                         case.tiles()))},
             "e2e": e2e, "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches}
     if mixed is not None:
         line["mixed"] = mixed

@@ -185,7 +185,8 @@ int ati_init(ati_handle_t *h);
  * directions, polarisations and phases uniform from turb_seed, divergence free,
  * scaled to turb_intensity |U_inf| rms per component and convected with the
  * freestream: v(x, t) = sum_n 2 a_n s_n cos(k_n . (x - U_inf t) + psi_n).  The
- * field is evaluated once per time step (at its start time) in FP32.
+ * field is evaluated in FP32 at the start time of the first step and of every
+ * step that takes a new dt (n % 10 == 1), and held in between.
  * ati_turbulence_modes copies case cs's table (8 floats per mode: k_x, k_y,
  * k_z, s_x, s_y, s_z, a, psi) and ati_turbulence_sample evaluates v at n given
  * points (xyz: x[n], y[n], z[n]; v likewise) at time t on the device. */
@@ -266,6 +267,11 @@ int ati_check(ati_handle_t *h);
 int ati_profile_enable(ati_handle_t *h, int enable);
 int ati_profile_read(ati_handle_t *h, int nslots, double *ms, int64_t *launches);
 int ati_launch_count(ati_handle_t *h, int64_t *count);
+/* Work-queue tile shapes in use: out[0] xi lines per CTA, out[1] eta/zeta
+ * lines per CTA, out[2] points per pointwise tile.  ati_init picks out[1] and
+ * out[2] by timing candidates on the handle's own grid (results do not depend
+ * on them: every line and point is computed the same way). */
+int ati_tiles(ati_handle_t *h, int32_t out[3]);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events against the solver's. */
 void *ati_stream(ati_handle_t *h);

@@ -55,6 +55,8 @@ struct ati_handle {
   bool any_cfl = false;  // some case takes its dt from the CFL condition (dto < 0)
   std::vector<PTile> hpt;
   std::vector<LTile> hlt[4];
+  size_t max_pt = 0, max_lt[4] = {0, 0, 0, 0};
+  int sg_lines = SG_DEFAULT, pt_points = PT_DEFAULT;  // tile shapes in use (timed at ati_init)
   int64_t N = 0, F = 0, nfac = 0, nsbcc = 0, nwall = 0;
   int maxlen[4] = {0, 0, 0, 0};
   int maxlines[4] = {0, 0, 0, 0};
@@ -103,6 +105,8 @@ struct ati_handle {
   int64_t probe_npts = 0, probe_n0 = 0;
   double *probe_p = nullptr, *probe_t = nullptr;
 };
+
+static int autotune(ati_handle *h);
 
 // error text for calls that have no handle (ati_last_error(NULL))
 void ati_set_thread_error(const char *msg) { g_create_err = msg ? msg : ""; }
@@ -409,6 +413,41 @@ extern "C" int ati_abi_version(void) { return ATI_ABI_VERSION; }
 
 extern "C" const char *ati_last_error(const ati_handle_t *h) { return h ? h->err.c_str() : g_create_err.c_str(); }
 
+// work queues: point tiles of pt points of one case, line tiles of one block
+// (XC_NL xi lines, sg eta or zeta lines)
+static void make_tiles(ati_handle *h, int sg, int pt) {
+  const int nbc = h->nb / h->ncase;
+  h->hpt.clear();
+  for (int cs = 0; cs < h->ncase; cs++) {
+    const int64_t g0 = h->blk[h->case_b0[cs]].off;
+    const BlockDev &Bl = h->blk[h->case_b0[cs] + nbc - 1];
+    const int64_t g1 = Bl.off + Bl.npts;
+    for (int64_t g = g0; g < g1; g += pt) h->hpt.push_back(PTile{cs, 0, g, std::min(g + pt, g1)});
+  }
+  for (int nn = 1; nn <= 3; nn++) {
+    h->hlt[nn].clear();
+    const int step = nn == 1 ? XC_NL : sg;
+    for (int gb = 0; gb < h->nb; gb++)
+      for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += step) h->hlt[nn].push_back(LTile{gb, t0});
+  }
+  h->sg_lines = sg;
+  h->pt_points = pt;
+}
+
+// copy the host work queues into the device arrays and point both engines at them
+static int upload_tiles(ati_handle *h) {
+  CK(cudaMemcpyAsync(const_cast<PTile *>(h->ed.pt), h->hpt.data(), sizeof(PTile) * h->hpt.size(), cudaMemcpyHostToDevice,
+                     h->st));
+  for (int nn = 1; nn <= 3; nn++)
+    CK(cudaMemcpyAsync(const_cast<LTile *>(h->ed.lt[nn]), h->hlt[nn].data(), sizeof(LTile) * h->hlt[nn].size(),
+                       cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  h->ed.npt = h->ef.npt = (int)h->hpt.size();
+  for (int nn = 1; nn <= 3; nn++) h->ed.nlt[nn] = h->ef.nlt[nn] = (int)h->hlt[nn].size();
+  h->ed.sg_lines = h->ef.sg_lines = h->sg_lines;
+  return ATI_OK;
+}
+
 static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<double> &facf, std::vector<double> &spg) {
   int64_t off = 0, face = 0, fac = 0;
   spg.assign((size_t)SPG_PER_BLOCK * h->nb, 0.0);
@@ -532,20 +571,11 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
     r.n++;
     r.maxline = std::max(r.maxline, T[h->tl_force.off + q].nline);
   }
-  // work queues: point tiles of one case, line tiles of one block
-  h->hpt.clear();
-  for (int cs = 0; cs < h->ncase; cs++) {
-    const int64_t g0 = h->blk[h->case_b0[cs]].off;
-    const BlockDev &Bl = h->blk[h->case_b0[cs] + nbc - 1];
-    const int64_t g1 = Bl.off + Bl.npts;
-    for (int64_t g = g0; g < g1; g += PT_POINTS) h->hpt.push_back(PTile{cs, 0, g, std::min(g + PT_POINTS, g1)});
-  }
-  for (int nn = 1; nn <= 3; nn++) {
-    h->hlt[nn].clear();
-    const int step = nn == 1 ? XC_NL : SG_LINES;
-    for (int gb = 0; gb < h->nb; gb++)
-      for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += step) h->hlt[nn].push_back(LTile{gb, t0});
-  }
+  // work queues, at their finest tiles (the device arrays are sized for these)
+  make_tiles(h, SG_MIN, PT_MIN);
+  h->max_pt = h->hpt.size();
+  for (int nn = 1; nn <= 3; nn++) h->max_lt[nn] = h->hlt[nn].size();
+  make_tiles(h, SG_DEFAULT, PT_DEFAULT);
   return ATI_OK;
 }
 
@@ -642,8 +672,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_sc = take(sizeof(Scheme) * ncase), o_cfd = take(sizeof(Coef<double>)),
                o_scal = take(sizeof(Scalars) * ncase), o_task = take(sizeof(FaceTask) * h->htasks.size()),
                o_jn = take(sizeof(JunctionDev) * 2 * ncase), o_woff = take(nforce * sizeof(int64_t)),
-               o_pt = take(sizeof(PTile) * h->hpt.size()), o_lt1 = take(sizeof(LTile) * h->hlt[1].size()),
-               o_lt2 = take(sizeof(LTile) * h->hlt[2].size()), o_lt3 = take(sizeof(LTile) * h->hlt[3].size());
+               o_pt = take(sizeof(PTile) * h->max_pt), o_lt1 = take(sizeof(LTile) * h->max_lt[1]),
+               o_lt2 = take(sizeof(LTile) * h->max_lt[2]), o_lt3 = take(sizeof(LTile) * h->max_lt[3]);
   // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
          o_frpex = 0, o_cff = 0, o_fdrvm = 0;
@@ -674,7 +704,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   Eng<double> &d = h->ed;
   double *f = D(o_f);
   d.blk = dblk; d.sc = dsc; d.cf = (Coef<double> *)(h->arena + o_cfd); d.scal = dscal; d.N = N; d.F = F;
-  d.ncase = ncase; d.pt = dpt; d.npt = (int)h->hpt.size();
+  d.ncase = ncase; d.pt = dpt; d.npt = (int)h->hpt.size(); d.sg_lines = h->sg_lines;
   for (int nn = 1; nn <= 3; nn++) { d.lt[nn] = dlt[nn]; d.nlt[nn] = (int)h->hlt[nn].size(); }
   d.qa = f; f += 5 * N; d.qo = f; f += 5 * N; d.de = f; f += 5 * N;
   h->rr = f; f += 3 * N; h->ss = f; f += 3 * N;
@@ -692,7 +722,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     Eng<float> &m = h->ef;
     float *g = Fp(o_ff);
     m.blk = dblk; m.sc = dsc; m.cf = (Coef<float> *)(h->arena + o_cff); m.scal = dscal; m.N = N; m.F = F;
-    m.ncase = ncase; m.pt = dpt; m.npt = d.npt;
+    m.ncase = ncase; m.pt = dpt; m.npt = d.npt; m.sg_lines = d.sg_lines;
     for (int nn = 1; nn <= 3; nn++) { m.lt[nn] = dlt[nn]; m.nlt[nn] = d.nlt[nn]; }
     m.qa = d.qa; m.qo = d.qo; m.yacod = d.yacod; m.cnt = d.cnt;
     m.de = g; g += 5 * N; m.prim = g; g += 4 * N; m.mu = g; g += N; m.p = g; g += N; m.dv = g; g += 12 * N;
@@ -979,6 +1009,14 @@ extern "C" int ati_jacobian_sign(ati_handle_t *h, int32_t *flags) {
   return ATI_OK;
 }
 
+extern "C" int ati_tiles(ati_handle_t *h, int32_t out[3]) {
+  if (!h || !out) return fail(h, ATI_EINVAL, "ati_tiles: bad argument");
+  out[0] = XC_NL;
+  out[1] = h->sg_lines;
+  out[2] = h->pt_points;
+  return ATI_OK;
+}
+
 extern "C" int ati_case_count(ati_handle_t *h, int *ncase) {
   if (!h || !ncase) return fail(h, ATI_EINVAL, "ati_case_count: bad argument");
   *ncase = h->ncase;
@@ -1166,6 +1204,7 @@ extern "C" int ati_init(ati_handle_t *h) {
   strict::scalar(c, h->st, SC_INIT, 0);
   CKL();
   CK(cudaStreamSynchronize(h->st));
+  if (int rc = autotune(h)) return rc;
   h->n_host = 0;
   h->steps_done = 0;
   h->inited = true;
@@ -1230,6 +1269,68 @@ struct EngineCalls<float> {
   }
 };
 
+// Tile shapes timed on the handle's own grid: lines per CTA of the eta/zeta
+// sweeps (a 5-field derivative sweep of each direction, into scratch planes)
+// and points per pointwise tile (the flux kernel).  Every line and every point
+// is computed the same way whatever the tiles, so the choice changes timings only.
+template <typename R>
+static int autotune_t(ati_handle *h, Eng<R> &e) {
+  using C = EngineCalls<R>;
+  const bool strict = h->cfg.precision == ATI_FP64_STRICT;
+  const int64_t N = h->N;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  auto time_it = [&](auto &&fn) {
+    cudaEventRecord(a, h->st);
+    fn();
+    cudaEventRecord(b, h->st);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  };
+  // candidates are timed in turn, five rounds, best of each; a candidate replaces
+  // the default only when it is at least 3 % faster (timings of one launch are noisy)
+  auto pick = [&](const std::vector<int> &cand, int dflt, auto &&setup, auto &&run) -> int {
+    std::vector<float> best(cand.size(), 1e30f);
+    for (int round = 0; round < 5; round++)
+      for (size_t q = 0; q < cand.size(); q++) {
+        setup(cand[q]);
+        run();  // warm
+        best[q] = std::min(best[q], time_it(run));
+      }
+    size_t qd = 0, qb = 0;
+    for (size_t q = 0; q < cand.size(); q++) {
+      if (cand[q] == dflt) qd = q;
+      if (best[q] < best[qb]) qb = q;
+    }
+    return best[qb] < 0.97f * best[qd] ? cand[qb] : dflt;
+  };
+  auto set_tiles = [&](int sg, int pt) {
+    make_tiles(h, sg, pt);
+    upload_tiles(h);
+    e.npt = h->ed.npt;
+    e.sg_lines = sg;
+    for (int nn = 1; nn <= 3; nn++) e.nlt[nn] = h->ed.nlt[nn];
+  };
+  const int sg = pick({SG_MIN, SG_DEFAULT, SG_MAX}, SG_DEFAULT, [&](int v) { set_tiles(v, PT_DEFAULT); }, [&] {
+    for (int nn = 2; nn <= 3; nn++) {
+      SweepIO<R, R> io{e.flx, 3 * N, e.dv, 3 * N, nullptr, 5, 1, false};
+      C::sweep(strict, e, h->st, nn, false, io);
+    }
+  });
+  const int pt = pick({PT_MIN, 4 * PT_MIN, PT_MAX}, PT_DEFAULT, [&](int v) { set_tiles(sg, v); },
+                      [&] { C::pw(strict, e, h->st, PW_FLUX); });
+  set_tiles(sg, pt);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CKL();
+  return ATI_OK;
+}
+
+static int autotune(ati_handle *h) { return h->mixed ? autotune_t<float>(h, h->ef) : autotune_t<double>(h, h->ed); }
+
 template <typename R>
 static int filter_step_t(ati_handle *h, const Eng<R> &e) {
   using C = EngineCalls<R>;
@@ -1293,8 +1394,12 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
     PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io));
   }
   PROF(h, ATI_K_DIV, C::pw(strict, e, st, PW_DIV));
-  if (h->ngust) {  // inflow turbulence: the gust targets of the inflow sponge, evaluated once per step
-    if (nk == 1) PROF(h, ATI_K_DIV, gust_eval(st, h->dgust, h->ngust, h->dtc, h->dmodes, ed.scal, h->ddelta, h->sh.s.gam));
+  if (h->ngust) {
+    // inflow turbulence: the gust targets of the inflow sponge, evaluated on the steps that take a new dt
+    // (n % 10 == 1, and the first step) and held in between: 10 steps are a few thousandths of the eddies'
+    // convective time L / U_inf, and the 2048-mode synthesis would otherwise cost more than the sponge it feeds
+    if (nk == 1 && (h->n_host % 10 == 1 || h->steps_done == 0))
+      PROF(h, ATI_K_DIV, gust_eval(st, h->dgust, h->ngust, h->dtc, h->dmodes, ed.scal, h->ddelta, h->sh.s.gam));
     if constexpr (std::is_same<R, float>::value)
       PROF(h, ATI_K_DIV, gust_apply_f(st, h->dgust, h->ngust, h->ddelta, ed.asz, ed.bsz, e.de, N));
     else PROF(h, ATI_K_DIV, gust_apply_d(st, h->dgust, h->ngust, h->ddelta, ed.asz, ed.bsz, e.de, N));

@@ -272,9 +272,10 @@ struct SweepArgs {
 
 // eta and zeta lines: one thread per line; consecutive threads own
 // consecutive xi positions, so each warp access of an eta or zeta sweep is one
-// contiguous row.  A CTA takes SG_LINES lines of one block (one work-queue tile).
+// contiguous row.  A CTA takes the lines of one work-queue tile of one block
+// (sg_lines of them, one per thread).
 template <int NN, bool FILT, typename TI, typename TO, typename TC>
-__global__ void __launch_bounds__(SG_LINES) k_sweep_g(SweepArgs<TI, TO, TC> a) {
+__global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
   const LTile LT = a.lt[blockIdx.x];
   const BlockDev &B = a.blk[LT.b];
   const int f = blockIdx.y;
@@ -556,11 +557,43 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long *a, double v) 
 template <typename R>
 __global__ void k_cfl(Eng<R> e) {
   const int64_t N = e.N;
+  __shared__ double s1[32], s2v[32];
+  // maxima of the CTA's tiles of one case, folded into the case's slot when the case changes
+  auto flush = [&](int cs, R m1, R m2) {
+    double dm1 = (double)m1, dm2 = (double)m2;
+    for (int o = 16; o > 0; o >>= 1) {
+      dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
+      dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
+    }
+    const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    __syncthreads();  // s1/s2v of an earlier flush are read
+    if (ln == 0) { s1[w] = dm1; s2v[w] = dm2; }
+    __syncthreads();
+    if (w == 0) {
+      const int nw = blockDim.x >> 5;
+      dm1 = ln < nw ? s1[ln] : 0.0;
+      dm2 = ln < nw ? s2v[ln] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) {
+        dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
+        dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
+      }
+      if (ln == 0) {
+        atomic_max_pos(&e.scal[cs].cflmax[0], dm1);
+        atomic_max_pos(&e.scal[cs].cflmax[1], dm2);
+      }
+    }
+  };
+  int cur = -1;
+  R m1 = 0, m2 = 0;
   TILE_LOOP(e, T) {
-    const Scheme &S = e.sc[T.cs];
+    if (T.cs != cur) {  // uniform over the CTA: every thread walks the same tiles
+      if (cur >= 0) flush(cur, m1, m2);
+      cur = T.cs;
+      m1 = 0;
+      m2 = 0;
+    }
     Scalars &SC = e.scal[T.cs];
     const R u1 = (R)SC.umf[1], u2 = (R)SC.umf[2], u3 = (R)SC.umf[3];
-    R m1 = 0, m2 = 0;
     POINT_LOOP(T, g) {
       const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
       const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
@@ -576,30 +609,8 @@ __global__ void k_cfl(Eng<R> e) {
       m2 = fmax(m2, v2);
       if (v1 != v1 || v2 != v2) atomicOr(&SC.flag, 4);
     }
-    double dm1 = (double)m1, dm2 = (double)m2;
-    for (int o = 16; o > 0; o >>= 1) {
-      dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
-      dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
-    }
-    __shared__ double s1[32], s2v[32];
-    const int w = threadIdx.x >> 5, ln = threadIdx.x & 31;
-    if (ln == 0) { s1[w] = dm1; s2v[w] = dm2; }
-    __syncthreads();
-    if (w == 0) {
-      const int nw = blockDim.x >> 5;
-      dm1 = ln < nw ? s1[ln] : 0.0;
-      dm2 = ln < nw ? s2v[ln] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) {
-        dm1 = fmax(dm1, __shfl_xor_sync(0xffffffffu, dm1, o));
-        dm2 = fmax(dm2, __shfl_xor_sync(0xffffffffu, dm2, o));
-      }
-      if (ln == 0) {
-        atomic_max_pos(&SC.cflmax[0], dm1);
-        atomic_max_pos(&SC.cflmax[1], dm2);
-      }
-    }
-    __syncthreads();  // s1/s2v are reused by the next tile
   }
+  if (cur >= 0) flush(cur, m1, m2);
 }
 
 // physical gradients of u, v, w, T and the viscous stresses and heat fluxes
@@ -1288,7 +1299,7 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
     else k_sweep_xc<false, TI, TO, TC><<<grid, XC_NL, 0, st>>>(a);
     return;
   }
-  const int tpb = SG_LINES;
+  const int tpb = e.sg_lines;
   if (!filt) {
     if (nn == 2) k_sweep_g<2, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
     else k_sweep_g<3, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
@@ -1338,7 +1349,7 @@ static int pw_grid(int64_t N) {
 template <typename R>
 static void pointwise_t(const Eng<R> &e, cudaStream_t st, int which) {
   if (e.npt == 0) return;
-  const int g = e.npt < 152 * 16 ? e.npt : 152 * 16, t = 256;  // CTAs walk the point tiles
+  const int g = e.npt < 152 * 16 ? e.npt : 152 * 16, t = 256;  // CTAs walk the point tiles, stride gridDim.x
   switch (which) {
     case PW_PRIM: k_prim<R><<<g, t, 0, st>>>(e); break;
     case PW_CFL: k_cfl<R><<<g, t, 0, st>>>(e); break;

@@ -38,6 +38,7 @@ struct Eng {
   int npt;
   const LTile *lt[4];   // line-sweep work queue per direction nn = 1..3
   int nlt[4];
+  int sg_lines;         // lines per CTA of the eta/zeta sweeps (the tiles of lt[2], lt[3])
   int64_t N;            // points of all blocks
   double *qa, *qo;      // state (5 planes each), FP64
   const double *yacod;  // Jacobian, FP64 (RK update)
@@ -95,11 +96,14 @@ struct SweepIO {
   TI ofs[5];
 };
 
-// lines per work-queue tile: xi sweeps (shared-memory chunks), eta/zeta sweeps
+// lines per work-queue tile of the xi sweeps (shared-memory chunks); the
+// eta/zeta sweeps take SG_MIN..SG_MAX lines per CTA and the pointwise kernels
+// PT_MIN..PT_MAX points per tile, chosen per handle by timing (ati_init)
 constexpr int XC_NL = 64;
-constexpr int SG_LINES = 128;
-// points per pointwise work-queue tile
-constexpr int PT_POINTS = 4096;
+constexpr int SG_MIN = 64, SG_MAX = 256, SG_DEFAULT = 128;
+// (a tile of 256 points is one point per thread: consecutive CTAs then sweep
+// consecutive memory, the access order of a plain grid-stride loop)
+constexpr int PT_MIN = 256, PT_MAX = 4096, PT_DEFAULT = 256;
 
 // per-field offsets of a closure (mpigo) over a wider input type
 template <typename TI>

@@ -72,6 +72,7 @@ SIGNATURES = {
     "ati_create_batch": ([_vp, _i32, ctypes.POINTER(_vp)], ctypes.c_int),
     "ati_step_async": ([_vp, _i32], ctypes.c_int),
     "ati_jacobian_sign": ([_vp, _vp], ctypes.c_int),
+    "ati_tiles": ([_vp, _vp], ctypes.c_int),
     "ati_turbulence_modes": ([_vp, _i32, _vp, _vp], ctypes.c_int),
     "ati_turbulence_sample": ([_vp, _i32, ctypes.c_double, ctypes.c_int64, _dp, _dp], ctypes.c_int),
     "ati_query": ([_vp, _vp], ctypes.c_int),
@@ -241,6 +242,12 @@ class Case:
         v = np.empty((3, n))
         self._chk(self.L.ati_turbulence_sample(self.h, cs, float(t), n, _dp_of(a), _dp_of(v)))
         return v
+
+    def tiles(self):
+        """(xi lines per CTA, eta/zeta lines per CTA, points per pointwise tile) chosen at init."""
+        t = (ctypes.c_int32 * 3)()
+        self._chk(self.L.ati_tiles(self.h, t))
+        return tuple(t)
 
     def jacobian_sign(self):
         """Per block: bit 0 some J > 0, bit 1 some J < 0, bit 2 J zero or not finite."""

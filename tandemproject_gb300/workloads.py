@@ -71,19 +71,21 @@ def fold_free_case(cfg, tries=4):
     raise ValueError(f"no fold-free grid for {cfg}")
 
 
-def _params(rng):
+def _params(rng, index, seed):
+    p = dict(thick=float(rng.uniform(8.0, 18.0)), aoa_deg=float(rng.uniform(0.0, 8.0)),
+             mach=float(rng.uniform(0.2, 0.4)))
     tu = float(rng.uniform(0.0, 5.0))
-    return dict(thick=float(rng.uniform(8.0, 18.0)), aoa_deg=float(rng.uniform(0.0, 8.0)),
-                mach=float(rng.uniform(0.2, 0.4)), turb_intensity=tu / 100.0, turb_length=0.1, turb_modes=2048,
-                turb_seed=int(rng.integers(1, 2**31 - 1))), tu
+    # the turbulence seed is derived, not drawn, so the size and step draws keep their sequence
+    p.update(turb_intensity=tu / 100.0, turb_length=0.1, turb_modes=2048, turb_seed=1000 * seed + index)
+    return p, tu
 
 
 def batch_cases(n=16, seed=7, precision=MIXED, nmin=1.0e6, nmax=6.0e6):
     """n cases with sizes spread unevenly over [nmin, nmax] points."""
     rng = np.random.default_rng(seed)
     out = []
-    for _ in range(n):
-        p, tu = _params(rng)
+    for i in range(n):
+        p, tu = _params(rng, i, seed)
         npts = float(rng.uniform(nmin, nmax))
         nz = int(rng.integers(16, 49))
         out.append((sized_case(npts, nz, rng, precision=precision, **p), {"turbulence_intensity_pct": tu}))
@@ -108,7 +110,7 @@ def serving_requests(n, seed=99, rate=4.0, nmin=0.5e6, nmax=20.0e6, smin=200, sm
     out = []
     for i in range(n):
         t += float(rng.exponential(1.0 / rate))
-        p, tu = _params(rng)
+        p, tu = _params(rng, i, seed)
         npts = float(math.exp(rng.uniform(math.log(nmin), math.log(nmax))))
         nz = int(rng.integers(16, 49))
         steps = max(3, int(round(int(rng.integers(smin, smax + 1)) * step_scale)))

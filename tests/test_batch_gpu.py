@@ -66,3 +66,12 @@ def test_jacobian_sign_check(ati_lib):
     cfg, g, c = fold_free_case(coarse)
     assert c.folded_blocks() == [] and cfg.letbk[0] > coarse.letbk[0]
     c.close()
+
+
+def test_autotuned_tiles_are_candidates(ati_lib):
+    from tandemproject_gb300.config import PRESETS
+    from tandemproject_gb300.solver import setup_case
+    c = setup_case(PRESETS["naca0012_0p2m"])
+    xi, sg, pt = c.tiles()
+    assert xi == 64 and sg in (64, 128, 256) and pt in (256, 1024, 4096)
+    c.close()
