@@ -356,6 +356,7 @@ def main():
         cm.step(2)
         mprof = cm.profile_read()
         cm.profile(False)
+        mtiles = cm.tiles()
         cm.close()
         mtot = sum(v[0] for v in mprof.values())
         mdom = max(mprof, key=lambda k: mprof[k][0])
@@ -379,6 +380,7 @@ def main():
                  "stage_hbm_frac_728B": STAGE_BYTES_MIXED * (npts * cfg.nkrk * args.steps / t_mix) / 1e9
                  / measured_peaks()[0],
                  "roofline": mroof,
+                 "tiles": list(mtiles),
                  "kernel_share": {k: round(v[0] / mtot, 4) for k, v in mprof.items() if v[1]}}
 
     # end to end through the C ABI: pinned host state in, step, state out
@@ -444,7 +446,8 @@ def main():
                                    f"{npts} points, FP64, RK4, Re 4e5, M 0.24",
                        "points": npts, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                        "l2": "no flush: the state alone (5 x 8 B x points) exceeds the 129 MB L2",
-                       "tiles": dict(zip(("xi_lines_per_cta", "eta_zeta_lines_per_cta", "points_per_tile"),
+                       "tiles": dict(zip(("xi_lines_per_cta", "eta_lines_per_cta", "zeta_lines_per_cta",
+                                          "points_per_tile"),
                                          case.tiles()))},
             "e2e": e2e, "roofline": roofline, "clocks": clk.summary(), "gpu_launches": launches}
     if mixed is not None:

@@ -267,11 +267,11 @@ int ati_check(ati_handle_t *h);
 int ati_profile_enable(ati_handle_t *h, int enable);
 int ati_profile_read(ati_handle_t *h, int nslots, double *ms, int64_t *launches);
 int ati_launch_count(ati_handle_t *h, int64_t *count);
-/* Work-queue tile shapes in use: out[0] xi lines per CTA, out[1] eta/zeta
- * lines per CTA, out[2] points per pointwise tile.  ati_init picks out[1] and
- * out[2] by timing candidates on the handle's own grid (results do not depend
- * on them: every line and point is computed the same way). */
-int ati_tiles(ati_handle_t *h, int32_t out[3]);
+/* Work-queue tile shapes in use: out[0] xi lines per CTA, out[1] eta and
+ * out[2] zeta lines per CTA, out[3] points per pointwise tile.  ati_init picks
+ * out[1..3] by timing candidates on the handle's own grid (results do not
+ * depend on them: every line and point is computed the same way). */
+int ati_tiles(ati_handle_t *h, int32_t out[4]);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events against the solver's. */
 void *ati_stream(ati_handle_t *h);

@@ -56,7 +56,7 @@ struct ati_handle {
   std::vector<PTile> hpt;
   std::vector<LTile> hlt[4];
   size_t max_pt = 0, max_lt[4] = {0, 0, 0, 0};
-  int sg_lines = SG_DEFAULT, pt_points = PT_DEFAULT;  // tile shapes in use (timed at ati_init)
+  int sg_lines[4] = {XC_NL, XC_NL, SG_DEFAULT, SG_DEFAULT}, pt_points = PT_DEFAULT;  // tile shapes (timed at ati_init)
   int64_t N = 0, F = 0, nfac = 0, nsbcc = 0, nwall = 0;
   int maxlen[4] = {0, 0, 0, 0};
   int maxlines[4] = {0, 0, 0, 0};
@@ -414,8 +414,8 @@ extern "C" int ati_abi_version(void) { return ATI_ABI_VERSION; }
 extern "C" const char *ati_last_error(const ati_handle_t *h) { return h ? h->err.c_str() : g_create_err.c_str(); }
 
 // work queues: point tiles of pt points of one case, line tiles of one block
-// (XC_NL xi lines, sg eta or zeta lines)
-static void make_tiles(ati_handle *h, int sg, int pt) {
+// (XC_NL xi lines, sg2 eta lines, sg3 zeta lines)
+static void make_tiles(ati_handle *h, int sg2, int sg3, int pt) {
   const int nbc = h->nb / h->ncase;
   h->hpt.clear();
   for (int cs = 0; cs < h->ncase; cs++) {
@@ -426,11 +426,12 @@ static void make_tiles(ati_handle *h, int sg, int pt) {
   }
   for (int nn = 1; nn <= 3; nn++) {
     h->hlt[nn].clear();
-    const int step = nn == 1 ? XC_NL : sg;
+    const int step = nn == 1 ? XC_NL : (nn == 2 ? sg2 : sg3);
     for (int gb = 0; gb < h->nb; gb++)
       for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += step) h->hlt[nn].push_back(LTile{gb, t0});
   }
-  h->sg_lines = sg;
+  h->sg_lines[2] = sg2;
+  h->sg_lines[3] = sg3;
   h->pt_points = pt;
 }
 
@@ -444,7 +445,7 @@ static int upload_tiles(ati_handle *h) {
   CK(cudaStreamSynchronize(h->st));
   h->ed.npt = h->ef.npt = (int)h->hpt.size();
   for (int nn = 1; nn <= 3; nn++) h->ed.nlt[nn] = h->ef.nlt[nn] = (int)h->hlt[nn].size();
-  h->ed.sg_lines = h->ef.sg_lines = h->sg_lines;
+  for (int nn = 0; nn < 4; nn++) h->ed.sg_lines[nn] = h->ef.sg_lines[nn] = h->sg_lines[nn];
   return ATI_OK;
 }
 
@@ -572,10 +573,10 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
     r.maxline = std::max(r.maxline, T[h->tl_force.off + q].nline);
   }
   // work queues, at their finest tiles (the device arrays are sized for these)
-  make_tiles(h, SG_MIN, PT_MIN);
+  make_tiles(h, SG_MIN, SG_MIN, PT_MIN);
   h->max_pt = h->hpt.size();
   for (int nn = 1; nn <= 3; nn++) h->max_lt[nn] = h->hlt[nn].size();
-  make_tiles(h, SG_DEFAULT, PT_DEFAULT);
+  make_tiles(h, SG_DEFAULT, SG_DEFAULT, PT_DEFAULT);
   return ATI_OK;
 }
 
@@ -704,7 +705,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   Eng<double> &d = h->ed;
   double *f = D(o_f);
   d.blk = dblk; d.sc = dsc; d.cf = (Coef<double> *)(h->arena + o_cfd); d.scal = dscal; d.N = N; d.F = F;
-  d.ncase = ncase; d.pt = dpt; d.npt = (int)h->hpt.size(); d.sg_lines = h->sg_lines;
+  d.ncase = ncase; d.pt = dpt; d.npt = (int)h->hpt.size();
+  for (int nn = 0; nn < 4; nn++) d.sg_lines[nn] = h->sg_lines[nn];
+  for (int nn = 0; nn < 4; nn++) d.maxlen[nn] = h->maxlen[nn];
   for (int nn = 1; nn <= 3; nn++) { d.lt[nn] = dlt[nn]; d.nlt[nn] = (int)h->hlt[nn].size(); }
   d.qa = f; f += 5 * N; d.qo = f; f += 5 * N; d.de = f; f += 5 * N;
   h->rr = f; f += 3 * N; h->ss = f; f += 3 * N;
@@ -722,7 +725,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     Eng<float> &m = h->ef;
     float *g = Fp(o_ff);
     m.blk = dblk; m.sc = dsc; m.cf = (Coef<float> *)(h->arena + o_cff); m.scal = dscal; m.N = N; m.F = F;
-    m.ncase = ncase; m.pt = dpt; m.npt = d.npt; m.sg_lines = d.sg_lines;
+    m.ncase = ncase; m.pt = dpt; m.npt = d.npt;
+    for (int nn = 0; nn < 4; nn++) m.sg_lines[nn] = d.sg_lines[nn];
+    for (int nn = 0; nn < 4; nn++) m.maxlen[nn] = h->maxlen[nn];
     for (int nn = 1; nn <= 3; nn++) { m.lt[nn] = dlt[nn]; m.nlt[nn] = d.nlt[nn]; }
     m.qa = d.qa; m.qo = d.qo; m.yacod = d.yacod; m.cnt = d.cnt;
     m.de = g; g += 5 * N; m.prim = g; g += 4 * N; m.mu = g; g += N; m.p = g; g += N; m.dv = g; g += 12 * N;
@@ -1009,11 +1014,12 @@ extern "C" int ati_jacobian_sign(ati_handle_t *h, int32_t *flags) {
   return ATI_OK;
 }
 
-extern "C" int ati_tiles(ati_handle_t *h, int32_t out[3]) {
+extern "C" int ati_tiles(ati_handle_t *h, int32_t out[4]) {
   if (!h || !out) return fail(h, ATI_EINVAL, "ati_tiles: bad argument");
   out[0] = XC_NL;
-  out[1] = h->sg_lines;
-  out[2] = h->pt_points;
+  out[1] = h->sg_lines[2];
+  out[2] = h->sg_lines[3];
+  out[3] = h->pt_points;
   return ATI_OK;
 }
 
@@ -1307,22 +1313,26 @@ static int autotune_t(ati_handle *h, Eng<R> &e) {
     }
     return best[qb] < 0.97f * best[qd] ? cand[qb] : dflt;
   };
-  auto set_tiles = [&](int sg, int pt) {
-    make_tiles(h, sg, pt);
+  auto set_tiles = [&](int sg2, int sg3, int pt) {
+    make_tiles(h, sg2, sg3, pt);
     upload_tiles(h);
     e.npt = h->ed.npt;
-    e.sg_lines = sg;
+    for (int nn = 0; nn < 4; nn++) e.sg_lines[nn] = h->sg_lines[nn];
     for (int nn = 1; nn <= 3; nn++) e.nlt[nn] = h->ed.nlt[nn];
   };
-  const int sg = pick({SG_MIN, SG_DEFAULT, SG_MAX}, SG_DEFAULT, [&](int v) { set_tiles(v, PT_DEFAULT); }, [&] {
-    for (int nn = 2; nn <= 3; nn++) {
+  // eta and zeta apart: the line length decides whether the forward values fit shared memory
+  auto sweep_of = [&](int nn) {
+    return [&, nn] {
       SweepIO<R, R> io{e.flx, 3 * N, e.dv, 3 * N, nullptr, 5, 1, false};
       C::sweep(strict, e, h->st, nn, false, io);
-    }
-  });
-  const int pt = pick({PT_MIN, 4 * PT_MIN, PT_MAX}, PT_DEFAULT, [&](int v) { set_tiles(sg, v); },
+    };
+  };
+  const std::vector<int> sgc{SG_MIN, 2 * SG_MIN, SG_DEFAULT, SG_MAX};
+  const int sg2 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(v, SG_DEFAULT, PT_DEFAULT); }, sweep_of(2));
+  const int sg3 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(sg2, v, PT_DEFAULT); }, sweep_of(3));
+  const int pt = pick({PT_MIN, 4 * PT_MIN, PT_MAX}, PT_DEFAULT, [&](int v) { set_tiles(sg2, sg3, v); },
                       [&] { C::pw(strict, e, h->st, PW_FLUX); });
-  set_tiles(sg, pt);
+  set_tiles(sg2, sg3, pt);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   CKL();

@@ -167,6 +167,8 @@ __device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int
     fw.st(2, v);
     f2 = f1; f1 = v;
   }
+  // unrolled so that several independent loads are in flight per thread (the recurrence is latency-bound)
+#pragma unroll 4
   for (int i = 3; i <= L - 4; i++) {
     const TC a6 = ld(i + 3);
     const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
@@ -194,6 +196,7 @@ __device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int
   last = b0;
   put(L - 1, b0);
   put(L - 2, b1);
+#pragma unroll 4
   for (int i = L - 3; i >= 0; i--) {
     const TC v = fac[i * 5 + 2] * fw.ld(i) - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
     put(i, v);
@@ -241,6 +244,14 @@ struct GlobalFw {
   __device__ __forceinline__ void st(int i, TC v) { p[(int64_t)i * s] = v; }
   __device__ __forceinline__ TC ld(int i) const { return p[(int64_t)i * s]; }
 };
+// forward values of one line in shared memory, column threadIdx.x of a [i][line] tile
+template <typename TC>
+struct SmemFw {
+  TC *p;
+  int s;
+  __device__ __forceinline__ void st(int i, TC v) { p[i * s] = v; }
+  __device__ __forceinline__ TC ld(int i) const { return p[i * s]; }
+};
 template <bool FILT, typename TI, typename TO, typename TC>
 struct GlobalSink {
   const TI *in;
@@ -273,9 +284,12 @@ struct SweepArgs {
 // eta and zeta lines: one thread per line; consecutive threads own
 // consecutive xi positions, so each warp access of an eta or zeta sweep is one
 // contiguous row.  A CTA takes the lines of one work-queue tile of one block
-// (sg_lines of them, one per thread).
-template <int NN, bool FILT, typename TI, typename TO, typename TC>
+// (sg_lines[NN] of them, one per thread).
+// SFW: the forward values stay in shared memory (lines short enough that a
+// CTA's lines fit 48 KB), which saves their round trip through DRAM
+template <int NN, bool FILT, bool SFW, typename TI, typename TO, typename TC>
 __global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
+  extern __shared__ __align__(16) unsigned char sg_smem[];
   const LTile LT = a.lt[blockIdx.x];
   const BlockDev &B = a.blk[LT.b];
   const int f = blockIdx.y;
@@ -289,11 +303,16 @@ __global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
   const TC *fac = a.fac + B.fac_off[NN] * 5;
   const TI *pin = a.io.in + f * a.io.in_fs + base;
   GlobalSrc<TI, TC> ld{pin, stride, a.io.ofs[f]};
-  GlobalFw<TC> fw{a.fw + f * a.fw_fs + base, stride};
   TO *o2 = a.io.out2 ? a.io.out2 + f * a.io.out_fs + base : nullptr;
   GlobalSink<FILT, TI, TO, TC> put{pin, a.io.out + f * a.io.out_fs + base, o2, stride};
   TC first, last;
-  solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
+  if constexpr (SFW) {
+    SmemFw<TC> fw{reinterpret_cast<TC *>(sg_smem) + threadIdx.x, (int)blockDim.x};
+    solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
+  } else {
+    GlobalFw<TC> fw{a.fw + f * a.fw_fs + base, stride};
+    solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
+  }
   if (!FILT && a.io.drva) {
     TC *d = a.drva + B.face_off[NN] * 10;
     const int m = a.io.m0 + f;
@@ -1299,13 +1318,21 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
     else k_sweep_xc<false, TI, TO, TC><<<grid, XC_NL, 0, st>>>(a);
     return;
   }
-  const int tpb = e.sg_lines;
+  const int tpb = e.sg_lines[nn];
+  const size_t smem = (size_t)e.maxlen[nn] * tpb * sizeof(TC);
+  if (smem <= SG_SMEM_FW) {  // short lines: forward values in shared memory
+#define ATI_SG(D, F) k_sweep_g<D, F, true, TI, TO, TC><<<grid, tpb, smem, st>>>(a)
+    if (!filt) { if (nn == 2) ATI_SG(2, false); else ATI_SG(3, false); }
+    else { if (nn == 2) ATI_SG(2, true); else ATI_SG(3, true); }
+#undef ATI_SG
+    return;
+  }
   if (!filt) {
-    if (nn == 2) k_sweep_g<2, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
-    else k_sweep_g<3, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
+    if (nn == 2) k_sweep_g<2, false, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
+    else k_sweep_g<3, false, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
   } else {
-    if (nn == 2) k_sweep_g<2, true, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
-    else k_sweep_g<3, true, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
+    if (nn == 2) k_sweep_g<2, true, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
+    else k_sweep_g<3, true, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
   }
 }
 

@@ -38,7 +38,8 @@ struct Eng {
   int npt;
   const LTile *lt[4];   // line-sweep work queue per direction nn = 1..3
   int nlt[4];
-  int sg_lines;         // lines per CTA of the eta/zeta sweeps (the tiles of lt[2], lt[3])
+  int sg_lines[4];      // lines per CTA of the eta (2) and zeta (3) sweeps: the tiles of lt[2], lt[3]
+  int maxlen[4];        // longest line per direction
   int64_t N;            // points of all blocks
   double *qa, *qo;      // state (5 planes each), FP64
   const double *yacod;  // Jacobian, FP64 (RK update)
@@ -100,10 +101,12 @@ struct SweepIO {
 // eta/zeta sweeps take SG_MIN..SG_MAX lines per CTA and the pointwise kernels
 // PT_MIN..PT_MAX points per tile, chosen per handle by timing (ati_init)
 constexpr int XC_NL = 64;
-constexpr int SG_MIN = 64, SG_MAX = 256, SG_DEFAULT = 128;
+constexpr int SG_MIN = 32, SG_MAX = 256, SG_DEFAULT = 128;
 // (a tile of 256 points is one point per thread: consecutive CTAs then sweep
 // consecutive memory, the access order of a plain grid-stride loop)
 constexpr int PT_MIN = 256, PT_MAX = 4096, PT_DEFAULT = 256;
+// eta/zeta sweeps keep their forward values in shared memory up to this many bytes per CTA
+constexpr size_t SG_SMEM_FW = 48 * 1024;
 
 // per-field offsets of a closure (mpigo) over a wider input type
 template <typename TI>

@@ -244,8 +244,8 @@ class Case:
         return v
 
     def tiles(self):
-        """(xi lines per CTA, eta/zeta lines per CTA, points per pointwise tile) chosen at init."""
-        t = (ctypes.c_int32 * 3)()
+        """(xi, eta, zeta lines per CTA, points per pointwise tile) chosen at init."""
+        t = (ctypes.c_int32 * 4)()
         self._chk(self.L.ati_tiles(self.h, t))
         return tuple(t)
 

@@ -72,6 +72,6 @@ def test_autotuned_tiles_are_candidates(ati_lib):
     from tandemproject_gb300.config import PRESETS
     from tandemproject_gb300.solver import setup_case
     c = setup_case(PRESETS["naca0012_0p2m"])
-    xi, sg, pt = c.tiles()
-    assert xi == 64 and sg in (64, 128, 256) and pt in (256, 1024, 4096)
+    xi, s2, s3, pt = c.tiles()
+    assert xi == 64 and s2 in (32, 64, 128, 256) and s3 in (32, 64, 128, 256) and pt in (256, 1024, 4096)
     c.close()
