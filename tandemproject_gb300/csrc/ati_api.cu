@@ -1287,7 +1287,16 @@ static int autotune_t(ati_handle *h, Eng<R> &e) {
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
+  // a buffer larger than L2, written before every timed run so that each candidate reads its inputs from DRAM
+  // as it does inside a step (timed back to back on the same arrays, L2 would favour low occupancy)
+  const size_t flush_bytes = 256u << 20;
+  void *flush = nullptr;
+  if (cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    flush = nullptr;
+  }
   auto time_it = [&](auto &&fn) {
+    if (flush) cudaMemsetAsync(flush, 0, flush_bytes, h->st);
     cudaEventRecord(a, h->st);
     fn();
     cudaEventRecord(b, h->st);
@@ -1333,6 +1342,7 @@ static int autotune_t(ati_handle *h, Eng<R> &e) {
   const int pt = pick({PT_MIN, 4 * PT_MIN, PT_MAX}, PT_DEFAULT, [&](int v) { set_tiles(sg2, sg3, v); },
                       [&] { C::pw(strict, e, h->st, PW_FLUX); });
   set_tiles(sg2, sg3, pt);
+  if (flush) cudaFree(flush);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   CKL();

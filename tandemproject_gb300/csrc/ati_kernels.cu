@@ -497,10 +497,15 @@ __global__ void k_mpigo(const BlockDev *blk, const Coef<TC> *cf, const FaceTask 
   const int isB = ipp * b1, ieB = 1 - 2 * ipp;
   const int mp = nt == 0 ? LMD : LMF;
   const TI ofs = fo.v[fld];
-  const TC res = ra0 * cvt_in<TI, TC>(src[Bn.off + idx3(Bn.lxi, Bn.let, isB, j, k, nn)], ofs);
+  // the neighbour's line: point index linear in the line position (indx3, src/Subroutineso.f90:364-375)
+  const int64_t b0 = Bn.off + idx3(Bn.lxi, Bn.let, 0, j, k, nn);
+  const int64_t bs = nn == 1 ? 1 : (nn == 2 ? (int64_t)(Bn.lxi + 1) : (int64_t)(Bn.lxi + 1) * (Bn.let + 1));
+  const TI *line = src + b0 + isB * bs;
+  const int64_t step = ieB * bs;
+  const TC res = ra0 * cvt_in<TI, TC>(line[0], ofs);
   TC s0 = 0, s1 = 0, sap0 = 0;
   for (int i = 0; i <= mp; i++) {
-    const TC v = cvt_in<TI, TC>(src[Bn.off + idx3(Bn.lxi, Bn.let, isB + ieB * (i + ii), j, k, nn)], ofs);
+    const TC v = cvt_in<TI, TC>(line[(i + ii) * step], ofs);
     if (i == 0) sap0 = v;
     s0 += C.pbco[nt][0][i] * v;
     s1 += C.pbco[nt][1][i] * v;
