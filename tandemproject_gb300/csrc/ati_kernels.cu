@@ -159,11 +159,11 @@ __device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int
   TC a0 = ld(0), a1 = ld(1), a2 = ld(2), a3 = ld(3), a4 = ld(4), a5 = ld(5);
   // forward elimination (src/Subroutines3D.f90:124-128 / 190-194)
   TC f2 = sbs0;
-  TC f1 = sbs1 - fac[1 * 5 + 1] * f2;
+  TC f1 = sbs1 - __ldg(fac + (1 * 5 + 1)) * f2;
   fw.st(0, f2);
   fw.st(1, f1);
   {
-    const TC v = sbs2 - fac[2 * 5 + 0] * f2 - fac[2 * 5 + 1] * f1;
+    const TC v = sbs2 - __ldg(fac + (2 * 5 + 0)) * f2 - __ldg(fac + (2 * 5 + 1)) * f1;
     fw.st(2, v);
     f2 = f1; f1 = v;
   }
@@ -172,33 +172,33 @@ __device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int
   for (int i = 3; i <= L - 4; i++) {
     const TC a6 = ld(i + 3);
     const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
-    const TC v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    const TC v = sb - __ldg(fac + (i * 5 + 0)) * f2 - __ldg(fac + (i * 5 + 1)) * f1;
     fw.st(i, v);
     f2 = f1; f1 = v;
     a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
   }
   {
     int i = L - 3;
-    TC v = sbe2 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    TC v = sbe2 - __ldg(fac + (i * 5 + 0)) * f2 - __ldg(fac + (i * 5 + 1)) * f1;
     fw.st(i, v);
     f2 = f1; f1 = v;
     i = L - 2;
-    v = sbe1 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    v = sbe1 - __ldg(fac + (i * 5 + 0)) * f2 - __ldg(fac + (i * 5 + 1)) * f1;
     fw.st(i, v);
     f2 = f1; f1 = v;
     i = L - 1;
-    v = sbe0 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    v = sbe0 - __ldg(fac + (i * 5 + 0)) * f2 - __ldg(fac + (i * 5 + 1)) * f1;
     f2 = f1; f1 = v;  // f1 = fw(L-1), f2 = fw(L-2)
   }
   // back substitution (src/Subroutines3D.f90:129-136 / 195-202)
-  TC b0 = fac[(L - 1) * 5 + 2] * f1;
-  TC b1 = fac[(L - 2) * 5 + 2] * f2 - fac[(L - 2) * 5 + 3] * b0;
+  TC b0 = __ldg(fac + ((L - 1) * 5 + 2)) * f1;
+  TC b1 = __ldg(fac + ((L - 2) * 5 + 2)) * f2 - __ldg(fac + ((L - 2) * 5 + 3)) * b0;
   last = b0;
   put(L - 1, b0);
   put(L - 2, b1);
 #pragma unroll 4
   for (int i = L - 3; i >= 0; i--) {
-    const TC v = fac[i * 5 + 2] * fw.ld(i) - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
+    const TC v = __ldg(fac + (i * 5 + 2)) * fw.ld(i) - __ldg(fac + (i * 5 + 3)) * b1 - __ldg(fac + (i * 5 + 4)) * b0;
     put(i, v);
     b0 = b1; b1 = v;
   }
@@ -235,7 +235,9 @@ struct GlobalSrc {
   const TI *p;
   int64_t s;
   TI ofs;
-  __device__ __forceinline__ TC operator()(int i) const { return cvt_in<TI, TC>(p[(int64_t)i * s], ofs); }
+  // read-only-path loads: every element of a line is read before the line's first result is
+  // stored, so the loads may be scheduled ahead of the forward-value stores
+  __device__ __forceinline__ TC operator()(int i) const { return cvt_in<TI, TC>(__ldg(p + (int64_t)i * s), ofs); }
 };
 template <typename TC>
 struct GlobalFw {
