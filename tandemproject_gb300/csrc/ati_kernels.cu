@@ -287,8 +287,9 @@ struct SweepArgs {
 // consecutive xi positions, so each warp access of an eta or zeta sweep is one
 // contiguous row.  A CTA takes the lines of one work-queue tile of one block
 // (sg_lines[NN] of them, one per thread).
-// SFW: the forward values stay in shared memory (lines short enough that a
-// CTA's lines fit 48 KB), which saves their round trip through DRAM
+// SFW: lines short enough that a CTA's lines fit 48 KB are staged whole in
+// shared memory (one column per thread) and solved there: all loads of a line
+// are in flight at once, and the forward values skip their round trip through DRAM
 template <int NN, bool FILT, bool SFW, typename TI, typename TO, typename TC>
 __global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
   extern __shared__ __align__(16) unsigned char sg_smem[];
@@ -309,8 +310,16 @@ __global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
   GlobalSink<FILT, TI, TO, TC> put{pin, a.io.out + f * a.io.out_fs + base, o2, stride};
   TC first, last;
   if constexpr (SFW) {
-    SmemFw<TC> fw{reinterpret_cast<TC *>(sg_smem) + threadIdx.x, (int)blockDim.x};
-    solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
+    // the whole line first, every load issued back to back, then the recurrences on shared memory
+    // (the forward values overwrite inputs already consumed, as solve_line allows)
+    TC *col = reinterpret_cast<TC *>(sg_smem) + threadIdx.x;
+    const int P = (int)blockDim.x;
+#pragma unroll 8
+    for (int i = 0; i < L; i++) col[i * P] = ld(i);
+    SmemFw<TC> fw{col, P};
+    const SmemFw<TC> lds{col, P};
+    auto sld = [&](int i) { return lds.ld(i); };
+    solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, sld, fw, put, first, last);
   } else {
     GlobalFw<TC> fw{a.fw + f * a.fw_fs + base, stride};
     solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
