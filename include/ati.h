@@ -279,6 +279,12 @@ void *ati_stream(ati_handle_t *h);
  * traffic) in TFLOP/s, FP64 when fp64 != 0 else FP32: the compute roofline
  * denominator of the FP64 path. */
 int ati_probe_fma_tflops(int fp64, double *tflops);
+/* The mixed path widens FP32 to FP64 with integer and bit operations (the
+ * FP64 pipe that runs the conversion instruction is GB300's slowest); this
+ * runs both forms on n device-generated bit patterns covering every exponent,
+ * zeros, subnormals, infinities and NaNs, and returns how many results differ
+ * (0 expected). */
+int ati_check_conversions(int64_t n, int64_t *mismatches);
 
 /* ---- allocation-free derivative (no counterpart in the reference) -------
  * For callers that must not allocate GPU memory when they call in: codes

@@ -30,6 +30,7 @@ SOURCES = [
     ("ati_noalloc.cu", "ati_noalloc.o", ["-fmad=false"]),
     ("ati_io.cpp", "ati_io.o", []),
     ("ati_turb.cu", "ati_turb.o", []),
+    ("ati_convert.cu", "ati_convert.o", []),
 ]
 
 

@@ -1,0 +1,38 @@
+// ati_convert.h — FP32 -> FP64 conversion on the integer pipes.
+//
+// On GB300 the FP64 pipe does 1/55 of the FP32 work per clock and also executes
+// the F2F conversion instructions, so the mixed path's RK update and filter,
+// which add FP32 increments to the FP64 state, spend much of their time there.
+// widen() does the exact conversion with integer and bit operations, straight
+// from the IEEE-754 binary32/binary64 layouts; zero is handled, and subnormals,
+// infinities and NaNs fall back to the instruction.  It gives the instruction's
+// result bit for bit (checked on the device by ati_check_conversions).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+namespace ati {
+
+// float -> double, exact: re-bias the exponent (127 -> 1023) and pad the significand
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu, s = u & 0x80000000u;
+  if (e - 1u < 254u) return __hiloint2double((int)(s | ((e + 896u) << 20) | (m >> 3)), (int)(m << 29));
+  if ((u << 1) == 0u) return __hiloint2double((int)s, 0);  // signed zero
+  return (double)f;  // subnormal, infinity, NaN
+}
+
+// conversion between the engine types: FP32 -> FP64 on the integer pipes.  The
+// other direction stays with the conversion instruction: rounding takes some
+// 15 integer operations and branches, slower in the line sweeps' load loops than
+// the FP64 pipe it would spare (measured on the mixed filter sweeps)
+template <typename TO, typename TI>
+__device__ __forceinline__ TO cvt(TI v) {
+  if constexpr (std::is_same<TO, TI>::value) return v;
+  else if constexpr (std::is_same<TO, double>::value && std::is_same<TI, float>::value) return widen(v);
+  else return (TO)v;
+}
+
+}  // namespace ati

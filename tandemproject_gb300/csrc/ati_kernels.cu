@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <type_traits>
 
+#include "ati_convert.h"
 #include "ati_kernels.h"
 
 #ifndef ATI_KNS
@@ -227,7 +228,7 @@ __device__ __forceinline__ bool line_geom(const BlockDev &B, int t, int64_t &bas
 template <typename TI, typename TC>
 __device__ __forceinline__ TC cvt_in(TI v, TI ofs) {
   if constexpr (std::is_same<TI, TC>::value) return v;
-  else return (TC)(v - ofs);
+  else return cvt<TC>(ofs == (TI)0 ? v : v - ofs);  // x - 0 is x: no subtraction for offset-free fields
 }
 
 template <typename TI, typename TC>
@@ -262,7 +263,7 @@ struct GlobalSink {
   __device__ __forceinline__ void operator()(int i, TC v) {
     const int64_t o = (int64_t)i * s;
     TO r;
-    if (FILT) r = (TO)(in[o] + (TI)v);  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+    if (FILT) r = (TO)(in[o] + cvt<TI>(v));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
     else r = (TO)v;
     out[o] = r;
     if (out2) out2[o] = r;
@@ -435,7 +436,7 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
     for (int q = 0; q < 3; q++) {
       const int64_t p = o + L - 3 + q;
       TO r;
-      if (FILT) r = (TO)(in[p] + (TI)rv[q]);  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+      if (FILT) r = (TO)(in[p] + cvt<TI>(rv[q]));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
       else r = (TO)rv[q];
       out[p] = r;
       if (out2) out2[p] = r;
@@ -466,7 +467,7 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
         const int64_t p = (int64_t)ln * L + c0 + lane - 3;
         const TC v = tile[lane][ln];
         TO r;
-        if (FILT) r = (TO)(in[p] + (TI)v);
+        if (FILT) r = (TO)(in[p] + cvt<TI>(v));
         else r = (TO)v;
         out[p] = r;
         if (out2) out2[p] = r;
@@ -559,16 +560,16 @@ __global__ void k_prim(Eng<R> e) {
     int bad = 0;
     const double rhoE_inf = S.hamm1 * S.poo;
     POINT_LOOP(T, g) {
-      const R q1 = (R)e.qa[g], q2 = (R)e.qa[g + N], q3 = (R)e.qa[g + 2 * N], q4 = (R)e.qa[g + 3 * N];
+      const R q1 = cvt<R>(e.qa[g]), q2 = cvt<R>(e.qa[g + N]), q3 = cvt<R>(e.qa[g + 2 * N]), q4 = cvt<R>(e.qa[g + 3 * N]);
       const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
       R pp, d5;
       if constexpr (Freestream<R>::on) {
         // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
-        const R re = (R)(e.qa[g + 4 * N] - rhoE_inf);
+        const R re = cvt<R>(e.qa[g + 4 * N] - rhoE_inf);
         pp = gamm1 * (re - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
         d5 = gam * ((R)S.poo + pp) * d1;
       } else {
-        const R q5 = (R)e.qa[g + 4 * N];
+        const R q5 = cvt<R>(e.qa[g + 4 * N]);
         pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
         d5 = gam * pp * d1;
       }
@@ -578,7 +579,10 @@ __global__ void k_prim(Eng<R> e) {
       e.p[g] = pp;
       e.mu[g] = mu;
       const R pabs = Freestream<R>::on ? (R)S.poo + pp : pp;
-      if (!(q1 > (R)0) || !(pabs > (R)0) || !(fabs((double)e.qa[g + 4 * N]) < 1e300)) bad = 1;
+      bool finite;
+      if constexpr (Freestream<R>::on) finite = ((__double2hiint(e.qa[g + 4 * N]) >> 20) & 0x7ff) != 0x7ff;
+      else finite = fabs((double)e.qa[g + 4 * N]) < 1e300;
+      if (!(q1 > (R)0) || !(pabs > (R)0) || !finite) bad = 1;
     }
     if (bad) atomicOr(&SC.flag, 1);
   }
@@ -638,7 +642,7 @@ __global__ void k_cfl(Eng<R> e) {
       const R r2 = fabs(x1 * d2 + x2 * d3 + x3 * d4) + fabs(e1 * d2 + e2 * d3 + e3 * d4) + fabs(z1 * d2 + z2 * d3 + z3 * d4);
       const R s2 = fabs(e.yaco[g]);
       const R v1 = (sqrt(e.prim[g + 3 * N] * r1) + r2) * s2;
-      const R d1 = (R)1 / (R)e.qa[g];
+      const R d1 = (R)1 / cvt<R>(e.qa[g]);
       const R v2 = d1 * e.mu[g] * r1 * s2 * s2;
       m1 = fmax(m1, v1);
       m2 = fmax(m2, v2);
@@ -683,7 +687,7 @@ __global__ void k_visc(Eng<R> e) {
         const R d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
                      (hxx + tyz) * (hxx + tyz);
         const R varr = (R)pow(-1.0 / (double)yac, 1.5);
-        const R q1 = (R)e.qa[g];
+        const R q1 = cvt<R>(e.qa[g]);
         r3 = q1 * (sm1 * sm1) * varr * sqrt((R)2 * d1);
         r1 = r1 + r3 * yac;
         r2 = r2 + tgp * r3 * yac;
@@ -737,14 +741,14 @@ __global__ void k_flux(Eng<R> e) {
         s1 = su1 + sm1; s2 = su2 + sm2; s3 = su3 + sm3;
         // rho U - rho_inf (umf . grad xi)
         const double q1 = e.qa[g];
-        const R q = (R)q1, qp = (R)(q1 - S.rhooo);
+        const R q = cvt<R>(q1), qp = cvt<R>(q1 - S.rhooo);
         F[g] = q * su1 + qp * sm1; F[g + N] = q * su2 + qp * sm2; F[g + 2 * N] = q * su3 + qp * sm3;
       } else {
         const R r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
         s1 = x1 * r1 + x2 * r2 + x3 * r3;
         s2 = e1 * r1 + e2 * r2 + e3 * r3;
         s3 = z1 * r1 + z2 * r2 + z3 * r3;
-        const R q = (R)e.qa[g];
+        const R q = cvt<R>(e.qa[g]);
         F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
       }
       R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
@@ -756,7 +760,7 @@ __global__ void k_flux(Eng<R> e) {
       const R xm[3] = {x1, x2, x3}, em[3] = {e1, e2, e3}, zm[3] = {z1, z2, z3};
   #pragma unroll
       for (int m = 2; m <= 4; m++) {
-        const R q = (R)e.qa[g + (m - 1) * N];
+        const R q = cvt<R>(e.qa[g + (m - 1) * N]);
         R a = q * s1 + xm[m - 2] * pp;
         R b = q * s2 + em[m - 2] * pp;
         R c = q * s3 + zm[m - 2] * pp;
@@ -774,12 +778,12 @@ __global__ void k_flux(Eng<R> e) {
         if constexpr (Freestream<R>::on) {
           // (rhoE + p) U - p (umf . grad xi) - rhoE_inf (umf . grad xi)
           const double q5 = e.qa[g + 4 * N];
-          const R d5 = (R)q5 + (R)S.poo + pp, re = (R)(q5 - S.hamm1 * S.poo);
+          const R d5 = cvt<R>(q5) + (R)S.poo + pp, re = cvt<R>(q5 - S.hamm1 * S.poo);
           a = d5 * su1 + re * sm1;
           b = d5 * su2 + re * sm2;
           c = d5 * su3 + re * sm3;
         } else {
-          const R d5 = (R)e.qa[g + 4 * N] + pp;
+          const R d5 = cvt<R>(e.qa[g + 4 * N]) + pp;
           a = d5 * s1 - pp * (u1 * x1 + u2 * x2 + u3 * x3);
           b = d5 * s2 - pp * (u1 * e1 + u2 * e2 + u3 * e3);
           c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
@@ -828,12 +832,12 @@ __global__ void k_div(Eng<R> e) {
         if constexpr (Freestream<R>::on) d = d + fs[m - 1];
         if (sponge) {
           if constexpr (Freestream<R>::on) {  // the pressure plane already holds p - p_inf, p_inf = 1/gamma
-            if (m == 1) d = d + as * (R)(e.qa[g] - 1.0);
-            else if (m <= 4) d = d + as * (R)e.qa[g + (m - 1) * N];
+            if (m == 1) d = d + as * cvt<R>(e.qa[g] - 1.0);
+            else if (m <= 4) d = d + as * cvt<R>(e.qa[g + (m - 1) * N]);
             else d = d + bs * e.p[g];
           } else {
-            if (m == 1) d = d + as * ((R)e.qa[g] - (R)1);
-            else if (m <= 4) d = d + as * ((R)e.qa[g + (m - 1) * N] - (R)0);
+            if (m == 1) d = d + as * (cvt<R>(e.qa[g]) - (R)1);
+            else if (m <= 4) d = d + as * (cvt<R>(e.qa[g + (m - 1) * N]) - (R)0);
             else d = d + bs * (e.p[g] - ham * (R)1);
           }
         }
@@ -854,7 +858,7 @@ __global__ void k_rk(Eng<R> e) {
     POINT_LOOP(T, g) {
       const double r1 = dtk * e.yacod[g];
 #pragma unroll
-      for (int q = 0; q < 5; q++) e.qa[g + q * N] = e.qo[g + q * N] - r1 * (double)e.de[g + q * N];
+      for (int q = 0; q < 5; q++) e.qa[g + q * N] = e.qo[g + q * N] - r1 * cvt<double>(e.de[g + q * N]);
     }
   }
 }
@@ -873,13 +877,13 @@ template <typename R>
 __device__ __forceinline__ void eleme(const Scheme &S, const Eng<R> &e, int64_t g, const R cm[3], const R umf[4],
                                       Elem<R> &el) {
   const int64_t N = e.N;
-  el.rhoi = (R)1 / (R)e.qa[g];
+  el.rhoi = (R)1 / cvt<R>(e.qa[g]);
   const R pabs = Freestream<R>::on ? (R)S.poo + e.p[g] : e.p[g];
   el.ao = sqrt((R)S.gam * el.rhoi * pabs);
   el.aoi = (R)1 / el.ao;
-  el.ve[0] = el.rhoi * (R)e.qa[g + N];
-  el.ve[1] = el.rhoi * (R)e.qa[g + 2 * N];
-  el.ve[2] = el.rhoi * (R)e.qa[g + 3 * N];
+  el.ve[0] = el.rhoi * cvt<R>(e.qa[g + N]);
+  el.ve[1] = el.rhoi * cvt<R>(e.qa[g + 2 * N]);
+  el.ve[2] = el.rhoi * cvt<R>(e.qa[g + 3 * N]);
   el.hv2 = (R)0.5 * (el.ve[0] * el.ve[0] + el.ve[1] * el.ve[1] + el.ve[2] * el.ve[2]);
   el.vn = cm[0] * el.ve[0] + cm[1] * el.ve[1] + cm[2] * el.ve[2];
   el.vs = cm[0] * umf[1] + cm[1] * umf[2] + cm[2] * umf[3];
@@ -1033,7 +1037,7 @@ __global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
   } else if (np == 20 || np == 25) {
     if (e.rpex[T.wall_off + jk] == (R)0) {
       const R s = cm[0] * (R)SC.dudtmf[1] + cm[1] * (R)SC.dudtmf[2] + cm[2] * (R)SC.dudtmf[3];
-      cha[3 + ip] = cha[4 - ip] + (R)2 * ra0 * el.aoi * (R)e.qa[g] * (s + (R)50 * (el.vn + el.vs));
+      cha[3 + ip] = cha[4 - ip] + (R)2 * ra0 * el.aoi * cvt<R>(e.qa[g]) * (s + (R)50 * (el.vn + el.vs));
     }
   } else {  // 30: characteristic interface, incoming waves from the neighbour
     const BlockDev &Bn = e.blk[T.nb_b];

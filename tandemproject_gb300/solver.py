@@ -73,6 +73,7 @@ SIGNATURES = {
     "ati_step_async": ([_vp, _i32], ctypes.c_int),
     "ati_jacobian_sign": ([_vp, _vp], ctypes.c_int),
     "ati_tiles": ([_vp, _vp], ctypes.c_int),
+    "ati_check_conversions": ([ctypes.c_int64, _vp], ctypes.c_int),
     "ati_turbulence_modes": ([_vp, _i32, _vp, _vp], ctypes.c_int),
     "ati_turbulence_sample": ([_vp, _i32, ctypes.c_double, ctypes.c_int64, _dp, _dp], ctypes.c_int),
     "ati_query": ([_vp, _vp], ctypes.c_int),

@@ -94,3 +94,14 @@ def test_mixed_pressure_field_is_absolute(ati_lib):
     from tandemproject_gb300.solver import F_P
     pd, pm = d.get_field(0, F_P), m.get_field(0, F_P)
     assert np.allclose(pd, pm, rtol=1e-6, atol=0)
+
+
+def test_integer_pipe_conversions_match_the_instructions(ati_lib):
+    """The mixed kernels widen FP32 to FP64 with integer operations; that must
+    give the conversion instruction's results bit for bit."""
+    import ctypes
+    from tandemproject_gb300.solver import load_library
+    L = load_library(ati_lib)
+    bad = ctypes.c_int64(-1)
+    assert L.ati_check_conversions(1 << 24, ctypes.byref(bad)) == 0
+    assert bad.value == 0
