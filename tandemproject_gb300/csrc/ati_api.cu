@@ -61,6 +61,9 @@ struct ati_handle {
   int maxlen[4] = {0, 0, 0, 0};
   int maxlines[4] = {0, 0, 0, 0};
   cudaStream_t st = nullptr;
+  // side streams and events for the three directions' sweeps, which are independent within a stage
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
   char *arena = nullptr;
   size_t arena_bytes = 0;
   Eng<double> ed{};  // FP64 arrays: set-up, granular calls, FP64 stage
@@ -662,8 +665,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   const size_t D8 = sizeof(double), F4 = sizeof(float);
   const size_t nforce = std::max<size_t>(h->tl_force.n, 1);
   // FP64 set: qa qo de(5) rr ss(3) xim etm zem(3) yaco p mu(1) tau(9) asz bsz(1) cnt(2) prim(4) dv(12) flx(15)
-  // fw(5) fw1(1)
-  const int np64 = 5 + 5 + 5 + 3 + 3 + 9 + 1 + 1 + 1 + 9 + 2 + 2 + 4 + 12 + 15 + 5 + 1;
+  // fw(3 x 5) fw1(1)
+  const int np64 = 5 + 5 + 5 + 3 + 3 + 9 + 1 + 1 + 1 + 9 + 2 + 2 + 4 + 12 + 15 + 15 + 1;
   const size_t o_f = take((size_t)np64 * N * D8), o_drva = take(10 * F * D8), o_drvb = take(10 * F * D8),
                o_recv = take(30 * F * D8), o_cm = take(6 * F * D8), o_facd = take(facd.size() * D8),
                o_facf = take(facf.size() * D8), o_sbcc = take(std::max<int64_t>(h->nsbcc, 1) * D8),
@@ -675,10 +678,10 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_jn = take(sizeof(JunctionDev) * 2 * ncase), o_woff = take(nforce * sizeof(int64_t)),
                o_pt = take(sizeof(PTile) * h->max_pt), o_lt1 = take(sizeof(LTile) * h->max_lt[1]),
                o_lt2 = take(sizeof(LTile) * h->max_lt[2]), o_lt3 = take(sizeof(LTile) * h->max_lt[3]);
-  // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(5) xim etm zem(3) yaco asz bsz(1) gm(3)
+  // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(3 x 5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
          o_frpex = 0, o_cff = 0, o_fdrvm = 0;
-  const int np32 = 5 + 4 + 1 + 1 + 12 + 9 + 15 + 5 + 9 + 1 + 1 + 1 + 3;
+  const int np32 = 5 + 4 + 1 + 1 + 12 + 9 + 15 + 15 + 9 + 1 + 1 + 1 + 3;
   if (h->mixed) {
     o_ff = take((size_t)np32 * N * F4);
     o_fdrva = take(10 * F * F4); o_fdrvb = take(10 * F * F4); o_frecv = take(30 * F * F4); o_fcm = take(6 * F * F4);
@@ -713,7 +716,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   h->rr = f; f += 3 * N; h->ss = f; f += 3 * N;
   d.xim = f; f += 3 * N; d.etm = f; f += 3 * N; d.zem = f; f += 3 * N; d.yaco = f; d.yacod = f; f += N;
   d.p = f; f += N; d.mu = f; f += N; d.tau = f; f += 9 * N; d.asz = f; f += N; d.bsz = f; f += N;
-  d.cnt = f; f += 2 * N; d.prim = f; f += 4 * N; d.dv = f; f += 12 * N; d.flx = f; f += 15 * N; d.fw = f; f += 5 * N;
+  d.cnt = f; f += 2 * N; d.prim = f; f += 4 * N; d.dv = f; f += 12 * N; d.flx = f; f += 15 * N; d.fw = f; f += 15 * N;
+  d.fw_dir = 5 * N;
   h->fw1 = f; f += N;
   d.drva = D(o_drva); d.drvb = D(o_drvb); d.recv = D(o_recv); d.cm = D(o_cm);
   d.facd = D(o_facd); d.facf = D(o_facf); d.sbcc = D(o_sbcc); d.rpex = D(o_rpex);
@@ -731,7 +735,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     for (int nn = 1; nn <= 3; nn++) { m.lt[nn] = dlt[nn]; m.nlt[nn] = d.nlt[nn]; }
     m.qa = d.qa; m.qo = d.qo; m.yacod = d.yacod; m.cnt = d.cnt;
     m.de = g; g += 5 * N; m.prim = g; g += 4 * N; m.mu = g; g += N; m.p = g; g += N; m.dv = g; g += 12 * N;
-    m.tau = g; g += 9 * N; m.flx = g; g += 15 * N; m.fw = g; g += 5 * N;
+    m.tau = g; g += 9 * N; m.flx = g; g += 15 * N; m.fw = g; g += 15 * N;
+    m.fw_dir = 5 * N;
     m.xim = g; g += 3 * N; m.etm = g; g += 3 * N; m.zem = g; g += 3 * N; m.yaco = g; g += N;
     m.asz = g; g += N; m.bsz = g; g += N; m.gm = g; g += 3 * N;
     m.drvm = Fp(o_fdrvm);
@@ -770,6 +775,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   for (int c = 0; c < ncase; c++) schemes.push_back(h->shc[c].s);
   std::vector<float> facd32(facd.begin(), facd.end()), facf32(facf.begin(), facf.end());
   e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaStreamCreateWithFlags(&h->side[q], cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+  for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaEventCreateWithFlags(&h->ev_join[q], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->arena, 0, bytes, h->st);
   auto up = [&](const void *dst, const void *src, size_t n) {
     if (e == cudaSuccess && n) e = cudaMemcpyAsync(const_cast<void *>(dst), src, n, cudaMemcpyHostToDevice, h->st);
@@ -836,6 +844,11 @@ extern "C" int ati_destroy(ati_handle_t *h) {
     if (p) cudaFree(p);
   if (h->arena) cudaFree(h->arena);
   if (h->st) cudaStreamDestroy(h->st);
+  for (int q = 0; q < 2; q++) {
+    if (h->side[q]) cudaStreamDestroy(h->side[q]);
+    if (h->ev_join[q]) cudaEventDestroy(h->ev_join[q]);
+  }
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   delete h;
   return ATI_OK;
 }
@@ -1049,6 +1062,7 @@ extern "C" int ati_set_grid(ati_handle_t *h, int blk, const double *xyz) {
 static int granular_sweep(ati_handle *h, int nn, bool filt, const double *in, double *out, int m) {
   Eng<double> e = h->ed;
   e.fw = h->fw1;
+  e.fw_dir = 0;
   SweepIO<double, double> io{in, 0, out, 0, nullptr, 1, m, !filt};
   PROF(h, (filt ? ATI_K_FILTER_XI : ATI_K_DERIV_XI) + nn - 1,
        strict::sweep_ddd(e, h->st, nn, filt, io));
@@ -1351,6 +1365,28 @@ static int autotune_t(ati_handle *h, Eng<R> &e) {
 
 static int autotune(ati_handle *h) { return h->mixed ? autotune_t<float>(h, h->ef) : autotune_t<double>(h, h->ed); }
 
+// The derivative sweeps of the three directions within a stage read and write
+// disjoint planes and face buffers, so xi runs on the handle's stream and eta,
+// zeta on two side streams forked from and joined back into it (inside the step
+// graph too): each direction alone leaves the GPU under-occupied.  With
+// profiling on they run one after another, so each launch is timed alone.
+template <typename F>
+static void three_directions(ati_handle *h, F &&sweep) {
+  if (h->profiling) {
+    for (int nn = 3; nn >= 1; nn--) sweep(nn, h->st);
+    return;
+  }
+  cudaEventRecord(h->ev_fork, h->st);
+  for (int q = 0; q < 2; q++) cudaStreamWaitEvent(h->side[q], h->ev_fork, 0);
+  sweep(1, h->st);
+  sweep(2, h->side[0]);
+  sweep(3, h->side[1]);
+  for (int q = 0; q < 2; q++) {
+    cudaEventRecord(h->ev_join[q], h->side[q]);
+    cudaStreamWaitEvent(h->st, h->ev_join[q], 0);
+  }
+}
+
 template <typename R>
 static int filter_step_t(ati_handle *h, const Eng<R> &e) {
   using C = EngineCalls<R>;
@@ -1399,20 +1435,20 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
     // d(u,v,w,T)/d(zeta,eta,xi) (src/Main3D.f90:629-651): four fields per launch
     PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, 0, e.prim,
                                   e.prim, e.prim, N, 4));
-    for (int nn = 3; nn >= 1; nn--) {
+    three_directions(h, [&](int nn, cudaStream_t s) {
       SweepIO<R, R> io{e.prim, N, e.dv + (nn - 1) * N, 3 * N, nullptr, 4, 2, true};
-      PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io));
-    }
+      PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, s, nn, false, io));
+    });
     PROF(h, ATI_K_VISC, C::pw(strict, e, st, PW_VISC));
   }
   // fluxes and their derivatives (src/Main3D.f90:710-768): five fields per launch
   PROF(h, ATI_K_FLUX, C::pw(strict, e, st, PW_FLUX));
   PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, 0, e.flx,
                                 e.flx + N, e.flx + 2 * N, 3 * N, 5));
-  for (int nn = 1; nn <= 3; nn++) {
+  three_directions(h, [&](int nn, cudaStream_t s) {
     SweepIO<R, R> io{e.flx + (nn - 1) * N, 3 * N, e.flx + (nn - 1) * N, 3 * N, nullptr, 5, 1, true};
-    PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, st, nn, false, io));
-  }
+    PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, s, nn, false, io));
+  });
   PROF(h, ATI_K_DIV, C::pw(strict, e, st, PW_DIV));
   if (h->ngust) {
     // inflow turbulence: the gust targets of the inflow sponge, evaluated on the steps that take a new dt

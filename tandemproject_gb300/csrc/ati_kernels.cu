@@ -1327,7 +1327,7 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   a.cf = e.cf;
   a.fac = filt ? e.facf : e.facd;
   a.io = io;
-  a.fw = e.fw;
+  a.fw = e.fw + (nn - 1) * e.fw_dir;  // sweeps of different directions may run at once
   a.fw_fs = e.N;
   a.recv = e.recv;
   a.recv_fs = e.F * 6;

@@ -51,6 +51,7 @@ struct Eng {
   R *tau;               // txx,tyy,tzz,txy,tyz,tzx,hxx,hyy,hzz
   R *flx;               // fluxes: plane (m-1)*3 + (nn-1)
   R *fw;                // forward-elimination scratch, one plane per field in flight
+  int64_t fw_dir;       // offset between the scratch of the three directions (0: one shared scratch)
   const R *xim, *etm, *zem, *yaco;
   const R *asz, *bsz;
   R *drva, *drvb, *recv;
