@@ -120,8 +120,8 @@ def serving_requests(n, seed=99, rate=4.0, nmin=0.5e6, nmax=20.0e6, smin=200, sm
 
 
 def footprint_bytes(cfg):
-    """Device memory of one case handle: the FP64 arena (83 planes of 8 B) and,
-    for the mixed path, the FP32 planes (67 of 4 B), plus face buffers."""
+    """Device memory of one case handle: the FP64 arena (93 planes of 8 B) and,
+    for the mixed path, the FP32 planes (77 of 4 B), plus face buffers."""
     n = cfg.npoints
-    per = 83 * 8 + (67 * 4 if cfg.precision == MIXED else 0)
+    per = 93 * 8 + (77 * 4 if cfg.precision == MIXED else 0)
     return int(n * per * 1.03) + (64 << 20)
