@@ -50,6 +50,10 @@ SWEEP_FLOPS = {"deriv": 17, "filter": 22}
 # the mixed path: FP32 derivative sweeps (4 B in, 4 B out); the filter reads
 # and writes the FP64 state
 SWEEP_BYTES_MIXED = {"deriv": 8, "filter": 16}
+# algorithmic bytes per point of the mixed path's pointwise kernels: k_flux<float>
+# reads the FP64 state (40 B), the FP32 metrics (36 B), velocity (12 B),
+# pressure (4 B) and stresses/heat fluxes (36 B) and writes 15 FP32 fluxes (60 B)
+POINTWISE_BYTES_MIXED = {"flux": 188}
 # fields swept per direction per time step: 4 viscous gradients + 5 fluxes in
 # each of the 4 stages, or the 5 variables once for the filter
 FIELD_SWEEPS_PER_STEP = {"deriv": 4 * (4 + 5), "filter": 5}
@@ -368,8 +372,14 @@ def main():
             mroof = {"bound": "hbm", "kernel": f"k_sweep<{mdom}> in FP32, {SWEEP_BYTES_MIXED[mkind]} B per point-field",
                      "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
                      "frac": mach / measured_peaks()[0]}
+        elif mdom in POINTWISE_BYTES_MIXED:
+            mt = mprof[mdom][0] / max(mprof[mdom][1], 1) / 1e3
+            mach = POINTWISE_BYTES_MIXED[mdom] * npts / mt / 1e9
+            mroof = {"bound": "hbm", "kernel": f"k_{mdom}<float>, {POINTWISE_BYTES_MIXED[mdom]} B per point",
+                     "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
+                     "frac": mach / measured_peaks()[0]}
         else:
-            mroof = {"kernel": mdom, "note": "dominant class is not a line sweep"}
+            mroof = {"kernel": mdom, "note": "no algorithmic byte count for this kernel class"}
         mixed = {"value": npts * cfg.nkrk * args.steps * ws / t_mix, "ms_per_step": t_mix / args.steps * 1e3,
                  "dtype": "f32 line solves/filters/fluxes, f64 metrics, Jacobian and RK state",
                  "speedup_vs_fp64": (npts * cfg.nkrk * args.steps * ws / t_mix) / value,

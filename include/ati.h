@@ -272,6 +272,11 @@ int ati_launch_count(ati_handle_t *h, int64_t *count);
  * out[1..3] by timing candidates on the handle's own grid (results do not
  * depend on them: every line and point is computed the same way). */
 int ati_tiles(ati_handle_t *h, int32_t out[4]);
+/* Pins the tile shapes (same meaning as ati_tiles; 0 keeps the current value):
+ * in[0] must be 0 or the fixed xi tile, in[1] and in[2] multiples of 32 in
+ * [32, 256], in[3] a multiple of 256 in [256, 4096].  Waits for the steps in
+ * flight and re-captures the step graphs at the next step. */
+int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events against the solver's. */
 void *ati_stream(ati_handle_t *h);

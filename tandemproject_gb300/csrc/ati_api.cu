@@ -55,6 +55,7 @@ struct ati_handle {
   bool any_cfl = false;  // some case takes its dt from the CFL condition (dto < 0)
   std::vector<PTile> hpt;
   std::vector<LTile> hlt[4];
+  std::vector<LTile> hlts[4];  // tiles of the segmented sweeps (mixed path), SEG_LINES lines each
   size_t max_pt = 0, max_lt[4] = {0, 0, 0, 0};
   int sg_lines[4] = {XC_NL, XC_NL, SG_DEFAULT, SG_DEFAULT}, pt_points = PT_DEFAULT;  // tile shapes (timed at ati_init)
   int64_t N = 0, F = 0, nfac = 0, nsbcc = 0, nwall = 0;
@@ -580,7 +581,63 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
   h->max_pt = h->hpt.size();
   for (int nn = 1; nn <= 3; nn++) h->max_lt[nn] = h->hlt[nn].size();
   make_tiles(h, SG_DEFAULT, SG_DEFAULT, PT_DEFAULT);
+  for (int nn = 1; nn <= 3; nn++) {
+    h->hlts[nn].clear();
+    for (int gb = 0; gb < h->nb; gb++)
+      for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += SEG_LINES) h->hlts[nn].push_back(LTile{gb, t0});
+    if (h->mixed && h->maxlen[nn] > SEG_LMAX)
+      return fail(h, ATI_EINVAL, "mixed precision: lines of up to " + std::to_string(SEG_LMAX) + " points");
+  }
   return ATI_OK;
+}
+
+// Row tables of the segmented solves (k_sweep_seg), SEG_RT floats per row of
+// one table of LU factors: the factors with the entries a row does not have
+// set to zero, and the responses (g, h) = forward values of the row's segment
+// from incoming v(s0-2) = 1 and from v(s0-1) = 1, (G, H) = its back-substituted
+// values from b(s1) = 1 and from b(s1+1) = 1.  The first segment receives no
+// forward values and the last no backward ones: their responses stay zero.
+static void seg_tables(const ati_handle *h, const std::vector<double> &fac, std::vector<float> &out) {
+  out.assign((size_t)h->nfac * SEG_RT, 0.f);
+  for (int gb = 0; gb < h->nb; gb++) {
+    const BlockDev &B = h->blk[gb];
+    for (int nn = 1; nn <= 3; nn++) {
+      const int L = nn == 1 ? B.lxi + 1 : (nn == 2 ? B.let + 1 : B.lze + 1);
+      const double *fc = &fac[(size_t)B.fac_off[nn] * 5];
+      float *o = &out[(size_t)B.fac_off[nn] * SEG_RT];
+      auto l0 = [&](int i) { return i >= 2 ? fc[i * 5 + 0] : 0.0; };
+      auto l1 = [&](int i) { return i >= 1 ? fc[i * 5 + 1] : 0.0; };
+      auto c3 = [&](int i) { return i <= L - 2 ? fc[i * 5 + 3] : 0.0; };
+      auto c4 = [&](int i) { return i <= L - 3 ? fc[i * 5 + 4] : 0.0; };
+      for (int i = 0; i < L; i++) {
+        float *r = o + (size_t)i * SEG_RT;
+        r[0] = (float)l0(i); r[1] = (float)l1(i);
+        r[6] = (float)fc[i * 5 + 2]; r[7] = (float)c3(i); r[10] = (float)c4(i);
+      }
+      const int S = seg_count(L);
+      for (int k = 0; k < S; k++) {
+        const int s0 = seg_start(k, L, S), s1 = seg_start(k + 1, L, S);
+        if (k > 0) {
+          double g2 = 1, g1 = 0, h2 = 0, h1 = 1;  // rows i-2, i-1
+          for (int i = s0; i < s1; i++) {
+            const double g = -l0(i) * g2 - l1(i) * g1, hh = -l0(i) * h2 - l1(i) * h1;
+            o[(size_t)i * SEG_RT + 4] = (float)g;
+            o[(size_t)i * SEG_RT + 5] = (float)hh;
+            g2 = g1; g1 = g; h2 = h1; h1 = hh;
+          }
+        }
+        if (k < S - 1) {
+          double G1 = 1, G2 = 0, H1 = 0, H2 = 1;  // rows i+1, i+2
+          for (int i = s1 - 1; i >= s0; i--) {
+            const double G = -c3(i) * G1 - c4(i) * G2, H = -c3(i) * H1 - c4(i) * H2;
+            o[(size_t)i * SEG_RT + 8] = (float)G;
+            o[(size_t)i * SEG_RT + 9] = (float)H;
+            G2 = G1; G1 = G; H2 = H1; H1 = H;
+          }
+        }
+      }
+    }
+  }
 }
 
 template <typename T>
@@ -680,7 +737,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_lt2 = take(sizeof(LTile) * h->max_lt[2]), o_lt3 = take(sizeof(LTile) * h->max_lt[3]);
   // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(3 x 5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
-         o_frpex = 0, o_cff = 0, o_fdrvm = 0;
+         o_frpex = 0, o_cff = 0, o_fdrvm = 0, o_lts[4] = {0, 0, 0, 0}, o_segd = 0, o_segf = 0;
   const int np32 = 5 + 4 + 1 + 1 + 12 + 9 + 15 + 15 + 9 + 1 + 1 + 1 + 3;
   if (h->mixed) {
     o_ff = take((size_t)np32 * N * F4);
@@ -689,6 +746,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     o_ffacd = take(facd.size() * F4); o_ffacf = take(facf.size() * F4);
     o_fsbcc = take(std::max<int64_t>(h->nsbcc, 1) * F4); o_frpex = take(std::max<int64_t>(h->nwall, 1) * F4);
     o_cff = take(sizeof(Coef<float>));
+    for (int nn = 1; nn <= 3; nn++) o_lts[nn] = take(sizeof(LTile) * std::max<size_t>(h->hlts[nn].size(), 1));
+    o_segd = take((size_t)h->nfac * SEG_RT * F4); o_segf = take((size_t)h->nfac * SEG_RT * F4);
   }
   cudaError_t e = cudaMalloc(&h->arena, bytes);
   if (e != cudaSuccess) {
@@ -742,6 +801,11 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     m.drvm = Fp(o_fdrvm);
     m.drva = Fp(o_fdrva); m.drvb = Fp(o_fdrvb); m.recv = Fp(o_frecv); m.cm = Fp(o_fcm);
     m.facd = Fp(o_ffacd); m.facf = Fp(o_ffacf); m.sbcc = Fp(o_fsbcc); m.rpex = Fp(o_frpex);
+    for (int nn = 1; nn <= 3; nn++) {
+      m.lts[nn] = (const LTile *)(h->arena + o_lts[nn]);
+      m.nlts[nn] = (int)h->hlts[nn].size();
+    }
+    m.segd = Fp(o_segd); m.segf = Fp(o_segf);
   }
   // junctions (src/SingleTurbulence3D.f90:386-398), bkx = 3, bky = 2, per case
   std::vector<JunctionDev> jn;
@@ -773,7 +837,11 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   const Coef<float> cff = make_coef<float>(h->sh.s);
   std::vector<Scheme> schemes;
   for (int c = 0; c < ncase; c++) schemes.push_back(h->shc[c].s);
-  std::vector<float> facd32(facd.begin(), facd.end()), facf32(facf.begin(), facf.end());
+  std::vector<float> facd32(facd.begin(), facd.end()), facf32(facf.begin(), facf.end()), segd32, segf32;
+  if (h->mixed) {
+    seg_tables(h, facd, segd32);
+    seg_tables(h, facf, segf32);
+  }
   e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaStreamCreateWithFlags(&h->side[q], cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
@@ -797,6 +865,10 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     up(h->ef.cf, &cff, sizeof(cff));
     up(h->ef.facd, facd32.data(), facd32.size() * F4);
     up(h->ef.facf, facf32.data(), facf32.size() * F4);
+    up(h->ef.segd, segd32.data(), segd32.size() * F4);
+    up(h->ef.segf, segf32.data(), segf32.size() * F4);
+    for (int nn = 1; nn <= 3; nn++) up(h->ef.lts[nn], h->hlts[nn].data(), sizeof(LTile) * h->hlts[nn].size());
+    if (e == cudaSuccess) e = fast::seg_init();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) {
@@ -1033,6 +1105,22 @@ extern "C" int ati_tiles(ati_handle_t *h, int32_t out[4]) {
   out[1] = h->sg_lines[2];
   out[2] = h->sg_lines[3];
   out[3] = h->pt_points;
+  return ATI_OK;
+}
+
+extern "C" int ati_set_tiles(ati_handle_t *h, const int32_t in[4]) {
+  if (!h || !in) return fail(h, ATI_EINVAL, "ati_set_tiles: bad argument");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_set_tiles: handle not initialised");
+  const int sg2 = in[1] ? in[1] : h->sg_lines[2], sg3 = in[2] ? in[2] : h->sg_lines[3];
+  const int pt = in[3] ? in[3] : h->pt_points;
+  auto sg_ok = [](int v) { return v >= SG_MIN && v <= SG_MAX && v % 32 == 0; };
+  if ((in[0] && in[0] != XC_NL) || !sg_ok(sg2) || !sg_ok(sg3) || pt < PT_MIN || pt > PT_MAX || pt % PT_MIN)
+    return fail(h, ATI_EINVAL, "ati_set_tiles: xi lines per CTA are fixed; eta/zeta lines per CTA must be multiples "
+                               "of 32 in [32, 256] and points per tile multiples of 256 in [256, 4096]");
+  CK(cudaStreamSynchronize(h->st));  // steps in flight read the queues
+  make_tiles(h, sg2, sg3, pt);
+  if (int rc = upload_tiles(h)) return rc;
+  drop_graphs(h);  // the step graphs hold the old grid shapes
   return ATI_OK;
 }
 
@@ -1350,9 +1438,13 @@ static int autotune_t(ati_handle *h, Eng<R> &e) {
       C::sweep(strict, e, h->st, nn, false, io);
     };
   };
+  // (the mixed path solves every line in segmented tiles of fixed shape: only its point tiles are timed)
   const std::vector<int> sgc{SG_MIN, 2 * SG_MIN, SG_DEFAULT, SG_MAX};
-  const int sg2 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(v, SG_DEFAULT, PT_DEFAULT); }, sweep_of(2));
-  const int sg3 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(sg2, v, PT_DEFAULT); }, sweep_of(3));
+  int sg2 = SG_DEFAULT, sg3 = SG_DEFAULT;
+  if (!h->mixed) {
+    sg2 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(v, SG_DEFAULT, PT_DEFAULT); }, sweep_of(2));
+    sg3 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(sg2, v, PT_DEFAULT); }, sweep_of(3));
+  }
   const int pt = pick({PT_MIN, 4 * PT_MIN, PT_MAX}, PT_DEFAULT, [&](int v) { set_tiles(sg2, sg3, v); },
                       [&] { C::pw(strict, e, h->st, PW_FLUX); });
   set_tiles(sg2, sg3, pt);

@@ -38,6 +38,22 @@ __device__ __forceinline__ void ijk_of(const BlockDev &B, int nn, int &i1, int &
   else { i1 = B.lze; i2 = B.lxi; i3 = B.let; }
 }
 
+// asynchronous global-to-shared copies (cp.async, sm_80 and later): the copy
+// holds no register while in flight, so a thread can have a whole line's
+// loads outstanding at once.  A thread's own copies are complete after
+// cp_async_wait; other threads see them after a barrier that follows the wait.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+  static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async.ca copies 4, 8 or 16 bytes");
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Compact derivative / filter of one line: deriv (src/Subroutines3D.f90:84-141)
 // and filte (src/Subroutines3D.f90:145-206).  ld(i) gives the original value at
@@ -168,16 +184,31 @@ __device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int
     fw.st(2, v);
     f2 = f1; f1 = v;
   }
-  // unrolled so that several independent loads are in flight per thread (the recurrence is latency-bound)
-#pragma unroll 4
-  for (int i = 3; i <= L - 4; i++) {
-    const TC a6 = ld(i + 3);
+  // interior rows in blocks of four, software-pipelined: the next block's
+  // inputs are read before this block's forward values are stored, so the
+  // loads are in flight during the recurrence even where the compiler cannot
+  // tell the forward store from the input (both in one shared-memory column)
+  auto fstep = [&](int i, TC a6) {
     const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
     const TC v = sb - __ldg(fac + (i * 5 + 0)) * f2 - __ldg(fac + (i * 5 + 1)) * f1;
     fw.st(i, v);
     f2 = f1; f1 = v;
     a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
+  };
+  const int iend = L - 4;  // last interior row
+  int i = 3;
+  if (i + 3 <= iend) {
+    TC n0 = ld(i + 3), n1 = ld(i + 4), n2 = ld(i + 5), n3 = ld(i + 6);
+    for (; i + 3 <= iend; i += 4) {
+      const TC c0 = n0, c1 = n1, c2 = n2, c3 = n3;
+      if (i + 7 <= iend) { n0 = ld(i + 7); n1 = ld(i + 8); n2 = ld(i + 9); n3 = ld(i + 10); }
+      fstep(i, c0);
+      fstep(i + 1, c1);
+      fstep(i + 2, c2);
+      fstep(i + 3, c3);
+    }
   }
+  for (; i <= iend; i++) fstep(i, ld(i + 3));
   {
     int i = L - 3;
     TC v = sbe2 - __ldg(fac + (i * 5 + 0)) * f2 - __ldg(fac + (i * 5 + 1)) * f1;
@@ -197,12 +228,25 @@ __device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int
   last = b0;
   put(L - 1, b0);
   put(L - 2, b1);
-#pragma unroll 4
-  for (int i = L - 3; i >= 0; i--) {
-    const TC v = __ldg(fac + (i * 5 + 2)) * fw.ld(i) - __ldg(fac + (i * 5 + 3)) * b1 - __ldg(fac + (i * 5 + 4)) * b0;
+  // blocks of four rows, the next block's forward values read before this block's results are stored
+  auto bstep = [&](int i, TC w) {
+    const TC v = __ldg(fac + (i * 5 + 2)) * w - __ldg(fac + (i * 5 + 3)) * b1 - __ldg(fac + (i * 5 + 4)) * b0;
     put(i, v);
     b0 = b1; b1 = v;
+  };
+  int k = L - 3;
+  if (k >= 3) {
+    TC m0 = fw.ld(k), m1 = fw.ld(k - 1), m2 = fw.ld(k - 2), m3 = fw.ld(k - 3);
+    for (; k >= 3; k -= 4) {
+      const TC c0 = m0, c1 = m1, c2 = m2, c3 = m3;
+      if (k >= 7) { m0 = fw.ld(k - 4); m1 = fw.ld(k - 5); m2 = fw.ld(k - 6); m3 = fw.ld(k - 7); }
+      bstep(k, c0);
+      bstep(k - 1, c1);
+      bstep(k - 2, c2);
+      bstep(k - 3, c3);
+    }
   }
+  for (; k >= 0; k--) bstep(k, fw.ld(k));
   first = b1;
 }
 
@@ -315,8 +359,16 @@ __global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
     // (the forward values overwrite inputs already consumed, as solve_line allows)
     TC *col = reinterpret_cast<TC *>(sg_smem) + threadIdx.x;
     const int P = (int)blockDim.x;
+    if constexpr (std::is_same<TI, TC>::value) {
+      // same type in and out: asynchronous copies, the whole line outstanding at once
 #pragma unroll 8
-    for (int i = 0; i < L; i++) col[i * P] = ld(i);
+      for (int i = 0; i < L; i++) cp_async<sizeof(TC)>(col + i * P, pin + (int64_t)i * stride);
+      cp_async_commit();
+      cp_async_wait<0>();
+    } else {
+#pragma unroll 8
+      for (int i = 0; i < L; i++) col[i * P] = ld(i);
+    }
     SmemFw<TC> fw{col, P};
     const SmemFw<TC> lds{col, P};
     auto sld = [&](int i) { return lds.ld(i); };
@@ -347,7 +399,11 @@ constexpr int XC_C = 32;
 
 template <bool FILT, typename TI, typename TO, typename TC>
 __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
-  __shared__ TC tile[XC_C][XC_NL + 1];
+  // FP32 lines of one type in and out: two tiles, the next chunk's asynchronous
+  // copies in flight while the recurrences run through the current one
+  constexpr bool AS = std::is_same<TI, TC>::value && sizeof(TC) == 4;
+  constexpr int NBUF = AS ? 2 : 1;
+  __shared__ TC tile[NBUF][XC_C][XC_NL + 1];
   const LTile LT = a.lt[blockIdx.x];
   const BlockDev &B = a.blk[LT.b];
   const int f = blockIdx.y;
@@ -384,31 +440,49 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
   }
   // forward elimination, chunk by chunk
   const TI ofs = a.io.ofs[f];
-  for (int c0 = 0; c0 < L; c0 += XC_C) {
-    const int cl = min(XC_C, L - c0);
-    __syncthreads();
+  const int nch = (L + XC_C - 1) / XC_C;
+  // asynchronous copies of chunk c of the CTA's lines of src into tile bf, one group
+  auto issue = [&](const TC *src, int c, int bf) {
+    const int c0 = c * XC_C, cl = min(XC_C, L - c0);
     if (lane < cl)
-      for (int ln = warp; ln < nl; ln += NW) tile[lane][ln] = cvt_in<TI, TC>(in[(int64_t)ln * L + c0 + lane], ofs);
+      for (int ln = warp; ln < nl; ln += NW)
+        cp_async<sizeof(TC)>(&tile[bf][lane][ln], src + (int64_t)ln * L + c0 + lane);
+    cp_async_commit();
+  };
+  if constexpr (AS) issue(reinterpret_cast<const TC *>(in), 0, 0);
+  for (int c = 0; c < nch; c++) {
+    const int c0 = c * XC_C, cl = min(XC_C, L - c0), bf = AS ? (c & 1) : 0;
+    __syncthreads();  // the previous chunk's write-back has read the tile about to be refilled
+    if constexpr (AS) {
+      if (c + 1 < nch) {
+        issue(reinterpret_cast<const TC *>(in), c + 1, (c + 1) & 1);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+    } else if (lane < cl) {
+      for (int ln = warp; ln < nl; ln += NW) tile[0][lane][ln] = cvt_in<TI, TC>(in[(int64_t)ln * L + c0 + lane], ofs);
+    }
     __syncthreads();
     if (act) {
       int s0 = 0;
       if (c0 == 0) {  // fw(0..2) go to positions 3..5
-        tile[3][t] = w0; tile[4][t] = w1; tile[5][t] = w2;
+        tile[bf][3][t] = w0; tile[bf][4][t] = w1; tile[bf][5][t] = w2;
         s0 = 6;
       }
       for (int s = s0; s < cl; s++) {
         const int i = c0 + s - 3;
-        const TC a6 = tile[s][t];
+        const TC a6 = tile[bf][s][t];
         const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
         const TC v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
-        tile[s][t] = v;
+        tile[bf][s][t] = v;
         f2 = f1; f1 = v;
         a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
       }
     }
     __syncthreads();
     if (lane < cl)
-      for (int ln = warp; ln < nl; ln += NW) fwg[(int64_t)ln * L + c0 + lane] = tile[lane][ln];
+      for (int ln = warp; ln < nl; ln += NW) fwg[(int64_t)ln * L + c0 + lane] = tile[bf][lane][ln];
   }
   // the last three rows and the first three results, in registers
   TC b0 = 0, b1 = 0;
@@ -444,19 +518,28 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
     b0 = b1; b1 = r3;
   }
   // back substitution, chunks in reverse: position j holds fw(j-3)
-  const int clast = ((L - 1) / XC_C) * XC_C;
-  for (int c0 = clast; c0 >= 0; c0 -= XC_C) {
-    const int cl = min(XC_C, L - c0);
+  __syncthreads();  // the forward pass's last write-back is complete and has read its tile
+  if constexpr (AS) issue(fwg, nch - 1, 0);
+  for (int r = 0; r < nch; r++) {
+    const int c = nch - 1 - r, c0 = c * XC_C, cl = min(XC_C, L - c0), bf = AS ? (r & 1) : 0;
     __syncthreads();
-    if (lane < cl)
-      for (int ln = warp; ln < nl; ln += NW) tile[lane][ln] = fwg[(int64_t)ln * L + c0 + lane];
+    if constexpr (AS) {
+      if (r + 1 < nch) {
+        issue(fwg, c - 1, (r + 1) & 1);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+    } else if (lane < cl) {
+      for (int ln = warp; ln < nl; ln += NW) tile[0][lane][ln] = fwg[(int64_t)ln * L + c0 + lane];
+    }
     __syncthreads();
     if (act) {
       const int se = c0 == 0 ? 3 : 0;
       for (int s = cl - 1; s >= se; s--) {
         const int i = c0 + s - 3;
-        const TC v = fac[i * 5 + 2] * tile[s][t] - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
-        tile[s][t] = v;
+        const TC v = fac[i * 5 + 2] * tile[bf][s][t] - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
+        tile[bf][s][t] = v;
         b0 = b1; b1 = v;
       }
     }
@@ -465,7 +548,7 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
     if (lane < cl && lane >= sw)
       for (int ln = warp; ln < nl; ln += NW) {
         const int64_t p = (int64_t)ln * L + c0 + lane - 3;
-        const TC v = tile[lane][ln];
+        const TC v = tile[bf][lane][ln];
         TO r;
         if (FILT) r = (TO)(in[p] + cvt<TI>(v));
         else r = (TO)v;
@@ -476,6 +559,311 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
   if (act && !FILT && a.io.drva) {
     TC *d = a.drva + B.face_off[1] * 10;
     d[jk + nbs * ((a.io.m0 + f - 1) + 5 * 0)] = b1;  // drva(jk,m,0) = sb(is)
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Segmented line solves (mixed path, FP32 arithmetic).  A CTA takes SEG_LINES
+// consecutive lines of one block and one field and stages them whole in
+// shared memory as a [point][line] tile.  Each line is cut into S =
+// seg_count(L) segments: warp w solves segment w, lane l line l.  The LU
+// solve (src/Subroutines3D.f90:124-136) is linear, so a segment's forward
+// values are its particular solution (zero incoming values) plus
+// g(i) v(s0-2) + h(i) v(s0-1), where g and h, the responses to the incoming
+// values, depend only on the LU factors that every line of the block shares.
+// They come precomputed per row (FP64 on the host, rounded once; G and H are
+// the same for the back substitution), packed with the row's LU factors.  One warp carries the incoming values
+// from segment to segment (a 2x2 update per segment), then every segment adds
+// its correction and back-substitutes the same way.  A thread's serial chain
+// is L/S rows instead of L, and every line is read from and written to DRAM
+// once, with no forward-value scratch.  The results differ from the
+// sequential solve by rounding only, and depend on the line length alone.
+// ---------------------------------------------------------------------------
+template <int NN, bool FILT, typename TI, typename TO>
+__global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, TO, float> a, const float *rtab) {
+  extern __shared__ __align__(16) unsigned char seg_smem[];
+  constexpr int RS = SEG_LINES + 1;  // tile row stride in words: a warp's column reads and row reads are conflict-free
+  constexpr bool ASYNC = std::is_same<TI, float>::value;
+  const int nwarp = (int)(blockDim.x >> 5);
+  float2 *cf = reinterpret_cast<float2 *>(seg_smem);  // [segment][line] values a segment passes on
+  float2 *cx = cf + nwarp * SEG_LINES;                 // [segment][line] values a segment receives
+  float *tile = reinterpret_cast<float *>(cx + nwarp * SEG_LINES);
+  const LTile LT = a.lt[blockIdx.x];
+  const BlockDev &B = a.blk[LT.b];
+  const int f = blockIdx.y;
+  const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
+  const int nl = min(SEG_LINES, (int)B.nbsize[NN] - LT.t0);
+  const int L = NN == 1 ? B.lxi + 1 : (NN == 2 ? B.let + 1 : B.lze + 1);
+  int64_t base = 0, stride = 1;
+  int jk = 0, Lg = 0;
+  line_geom<NN>(B, LT.t0 + lane, base, stride, jk, Lg);
+  const TI *in = a.io.in + f * a.io.in_fs;
+  const TI ofs = a.io.ofs[f];
+
+  // 1. stage the lines (inputs wider than FP32 lose their offset and are rounded on the way in);
+  // source and destination pointers walk by constant steps
+  auto stage = [&](float *dst, const TI *src) {
+    if constexpr (ASYNC) cp_async<4>(dst, src);
+    else *dst = cvt_in<TI, float>(__ldg(src), ofs);
+  };
+  if constexpr (NN == 1) {
+    // xi lines are contiguous: a warp copies one line at a time, lanes along the line
+    const TI *src0 = in + B.off + (int64_t)LT.t0 * L;
+    for (int ln = w; ln < nl; ln += nwarp) {
+      const TI *src = src0 + (int64_t)ln * L + lane;
+      float *dst = tile + lane * RS + ln;
+#pragma unroll 4
+      for (int i = lane; i < L; i += 32, src += 32, dst += 32 * RS) stage(dst, src);
+    }
+  } else {
+    // consecutive eta/zeta lines are consecutive points of a row: a warp copies one row at a time
+    if (lane < nl) {
+      const TI *src = in + base + (int64_t)w * stride;
+      const int64_t step = (int64_t)nwarp * stride;
+      float *dst = tile + w * RS + lane;
+#pragma unroll 4
+      for (int i = w; i < L; i += nwarp, src += step, dst += nwarp * RS) stage(dst, src);
+    }
+  }
+  if constexpr (ASYNC) {
+    cp_async_commit();
+    cp_async_wait<0>();
+  }
+  __syncthreads();
+
+  const int S = seg_count(L);
+  const bool act = w < S && lane < nl;
+  const int s0 = seg_start(w, L, S), s1 = seg_start(w + 1, L, S);
+  float *col = tile + lane;
+  // the block's row table, SEG_RT floats per row (layout at SEG_RT)
+  const float *rt = rtab + (int64_t)B.fac_off[NN] * SEG_RT;
+  auto row = [&](int i) { return rt + i * SEG_RT; };
+  // interior stencil weights in registers (loads from the coefficient struct could not move past the stores)
+  const Coef<float> &C = *a.cf;
+  const float k1 = FILT ? C.fa : C.aa, k2 = FILT ? C.fb : C.ab, k3 = FILT ? C.fc : C.ac;
+  auto rhs = [&](float x0, float x1, float x2, float x3, float x4, float x5, float x6) {
+    if (!FILT) return k1 * (x4 - x2) + k2 * (x5 - x1) + k3 * (x6 - x0);
+    const float r = 2.f * x3;
+    return k1 * (x2 + x4 - r) + k2 * (x1 + x5 - r) + k3 * (x0 + x6 - r);
+  };
+  const int ilo = max(s0, 3), ihi = min(s1, L - 3);  // interior rows [ilo, ihi) of the segment
+  // 2. what a segment reads outside its own rows, before any row is overwritten:
+  // the boundary-closure rows, the first window and the three rows after it
+  float sbs0 = 0, sbs1 = 0, sbs2 = 0, sbe0 = 0, sbe1 = 0, sbe2 = 0;
+  float a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, h0 = 0, h1 = 0, h2 = 0;
+  if (act) {
+    auto sld = [&](int i) { return col[i * RS]; };
+    if (w == 0 || w == S - 1) {
+      const float *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
+      line_ends<FILT, float>(C, L, B.ndf[0][NN], B.ndf[1][NN], rcv, B.nbsize[NN], jk, sld, sbs0, sbs1, sbs2, sbe0,
+                             sbe1, sbe2);
+    }
+    if (ilo < ihi) {
+      a0 = sld(ilo - 3); a1 = sld(ilo - 2); a2 = sld(ilo - 1); a3 = sld(ilo); a4 = sld(ilo + 1); a5 = sld(ilo + 2);
+    }
+    if (w < S - 1) { h0 = sld(s1); h1 = sld(s1 + 1); h2 = sld(s1 + 2); }
+  }
+  __syncthreads();
+
+  // 3. forward elimination of the segment from zero incoming values (the particular solution), in place
+  float pm2 = 0, pm1 = 0;
+  if (act) {
+    auto fwd = [&](int i, float r) {
+      const float2 l = __ldg(reinterpret_cast<const float2 *>(row(i)));  // masked l0, l1
+      const float p = r - l.x * pm2 - l.y * pm1;
+      col[i * RS] = p;
+      pm2 = pm1; pm1 = p;
+    };
+    int i = s0;
+    for (; i < min(s1, 3); i++) fwd(i, i == 0 ? sbs0 : (i == 1 ? sbs1 : sbs2));
+    const int iown = min(ihi, s1 - 3);  // windows inside the segment
+    {
+      // four rows per pass, walking a shared and a table pointer: the loop body is
+      // the arithmetic itself (the loads of a pass come before its stores)
+      float *pc = col + i * RS;
+      const float *tr = row(i);
+      for (; i + 3 < iown; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
+        const float b0 = pc[3 * RS], b1 = pc[4 * RS], b2 = pc[5 * RS], b3 = pc[6 * RS];
+        const float2 m0 = __ldg(reinterpret_cast<const float2 *>(tr));
+        const float2 m1 = __ldg(reinterpret_cast<const float2 *>(tr + SEG_RT));
+        const float2 m2 = __ldg(reinterpret_cast<const float2 *>(tr + 2 * SEG_RT));
+        const float2 m3 = __ldg(reinterpret_cast<const float2 *>(tr + 3 * SEG_RT));
+        float p;
+        p = rhs(a0, a1, a2, a3, a4, a5, b0) - m0.x * pm2 - m0.y * pm1; pc[0] = p; pm2 = pm1; pm1 = p;
+        p = rhs(a1, a2, a3, a4, a5, b0, b1) - m1.x * pm2 - m1.y * pm1; pc[RS] = p; pm2 = pm1; pm1 = p;
+        p = rhs(a2, a3, a4, a5, b0, b1, b2) - m2.x * pm2 - m2.y * pm1; pc[2 * RS] = p; pm2 = pm1; pm1 = p;
+        p = rhs(a3, a4, a5, b0, b1, b2, b3) - m3.x * pm2 - m3.y * pm1; pc[3 * RS] = p; pm2 = pm1; pm1 = p;
+        a0 = a4; a1 = a5; a2 = b0; a3 = b1; a4 = b2; a5 = b3;
+      }
+    }
+    for (; i < iown; i++) {
+      const float a6 = col[(i + 3) * RS];
+      fwd(i, rhs(a0, a1, a2, a3, a4, a5, a6));
+      a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
+    }
+    for (; i < ihi; i++) {  // windows reaching into the next segment: its first rows, read before the barrier
+      const int d = i + 3 - s1;
+      const float a6 = d == 0 ? h0 : (d == 1 ? h1 : h2);
+      fwd(i, rhs(a0, a1, a2, a3, a4, a5, a6));
+      a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
+    }
+    for (; i < s1; i++) fwd(i, i == L - 1 ? sbe0 : (i == L - 2 ? sbe1 : sbe2));
+    cf[w * SEG_LINES + lane] = make_float2(pm2, pm1);  // rows s1-2, s1-1
+  }
+  // lines of one segment (S = 1, the same for the whole CTA) need neither carries nor corrections
+  const bool multi = S > 1;
+  if (multi) {
+    __syncthreads();
+    // 4. incoming values of every segment, carried by warp 0 (segment 0 receives zeros)
+    if (w == 0 && lane < nl) {
+      float2 x = make_float2(0.f, 0.f);
+      cx[lane] = x;
+      for (int k = 1; k < S; k++) {
+        const int e = seg_start(k, L, S);
+        const float2 c = cf[(k - 1) * SEG_LINES + lane];
+        const float2 t2 = __ldg(reinterpret_cast<const float2 *>(row(e - 2) + 4));  // g, h
+        const float2 t1 = __ldg(reinterpret_cast<const float2 *>(row(e - 1) + 4));
+        x = make_float2(c.x + t2.x * x.x + t2.y * x.y, c.y + t1.x * x.x + t1.y * x.y);
+        cx[k * SEG_LINES + lane] = x;
+      }
+    }
+    __syncthreads();
+  }
+  TO *out = a.io.out + f * a.io.out_fs;
+  TO *out2 = FILT && a.io.out2 ? a.io.out2 + f * a.io.out_fs : nullptr;  // (a derivative has one output)
+  float *drv = (!FILT && a.io.drva) ? a.drva + B.face_off[NN] * 10 : nullptr;
+  const int64_t nbs = B.nbsize[NN];
+  const int m = a.io.m0 + f;
+  // 5. the segment's forward values, then its back substitution from zero values beyond its end; with one
+  // segment that gives the results, which eta/zeta lines write straight to DRAM (a warp writes a row)
+  if (act) {
+    const float2 x = multi ? cx[w * SEG_LINES + lane] : make_float2(0.f, 0.f);
+    float q1 = 0, q2 = 0;  // rows i+1, i+2
+    int i = s1 - 1;
+    float *pc = col + i * RS;
+    const float *tr = row(i);
+    const int64_t o = base + (int64_t)i * stride;
+    TO *po = out + o;
+    TO *po2 = out2 ? out2 + o : nullptr;
+    const TI *pi = in + o;
+    auto sweep = [&](auto direct) {
+      constexpr bool D = decltype(direct)::value;
+      // one row: t = (g, h, c2, masked c3) and the masked c4 of the row
+      auto bwd = [&](float *c, const float *t) {
+        const float4 g = __ldg(reinterpret_cast<const float4 *>(t + 4));
+        const float c4 = __ldg(t + 10);
+        const float v = *c + g.x * x.x + g.y * x.y;
+        const float q = g.z * v - g.w * q1 - c4 * q2;
+        if constexpr (D) {
+          TO r;
+          if (FILT) r = (TO)(*pi + cvt<TI>(q));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+          else r = (TO)q;
+          *po = r;
+          po -= stride;
+          if (out2) { *po2 = r; po2 -= stride; }
+          if (FILT) pi -= stride;
+        } else {
+          *c = q;
+        }
+        q2 = q1; q1 = q;
+      };
+      for (; i - 3 >= s0; i -= 4, pc -= 4 * RS, tr -= 4 * SEG_RT) {
+        bwd(pc, tr);
+        bwd(pc - RS, tr - SEG_RT);
+        bwd(pc - 2 * RS, tr - 2 * SEG_RT);
+        bwd(pc - 3 * RS, tr - 3 * SEG_RT);
+      }
+      for (; i >= s0; i--, pc -= RS, tr -= SEG_RT) bwd(pc, tr);
+    };
+    if (!multi && NN != 1) {
+      sweep(std::true_type{});
+      if (drv) {
+        drv[jk + nbs * ((m - 1) + 5 * 0)] = q1;  // drva(jk,m,0) = sb(is): row 0, the last one solved
+        drv[jk + nbs * ((m - 1) + 5 * 1)] = (float)out[base + (int64_t)(L - 1) * stride];  // drva(jk,m,1) = sb(ie)
+      }
+    } else {
+      sweep(std::false_type{});
+      if (multi) cf[w * SEG_LINES + lane] = make_float2(q1, q2);  // rows s0, s0+1
+      else if (drv) {
+        drv[jk + nbs * ((m - 1) + 5 * 0)] = col[0];
+        drv[jk + nbs * ((m - 1) + 5 * 1)] = col[(L - 1) * RS];
+      }
+    }
+  }
+  if (multi) {
+    __syncthreads();
+    // 6. values beyond every segment's end, carried backwards by warp 0 (the last segment receives zeros)
+    if (w == 0 && lane < nl) {
+      float2 y = make_float2(0.f, 0.f);
+      cx[(S - 1) * SEG_LINES + lane] = y;
+      for (int k = S - 2; k >= 0; k--) {
+        const int e = seg_start(k + 1, L, S);
+        const float2 c = cf[(k + 1) * SEG_LINES + lane];
+        const float2 t0 = __ldg(reinterpret_cast<const float2 *>(row(e) + 8));  // G, H
+        const float2 t1 = __ldg(reinterpret_cast<const float2 *>(row(e + 1) + 8));
+        y = make_float2(c.x + t0.x * y.x + t0.y * y.y, c.y + t1.x * y.x + t1.y * y.y);
+        cx[k * SEG_LINES + lane] = y;
+      }
+    }
+    __syncthreads();
+    // 7. results: eta/zeta rows go straight to DRAM (a warp writes a contiguous row), xi lines through the tile
+    if (act) {
+      const float2 y = cx[w * SEG_LINES + lane];
+      auto fv = [&](const float *c, const float *t) {
+        const float2 g = __ldg(reinterpret_cast<const float2 *>(t));
+        return *c + g.x * y.x + g.y * y.y;
+      };
+      if (drv) {
+        if (w == 0) drv[jk + nbs * ((m - 1) + 5 * 0)] = fv(col, row(0) + 8);  // drva(jk,m,0) = sb(is)
+        if (w == S - 1) drv[jk + nbs * ((m - 1) + 5 * 1)] = fv(col + (L - 1) * RS, row(L - 1) + 8);
+      }
+      int i = s0;
+      float *pc = col + i * RS;
+      const float *tr = row(i) + 8;
+      if constexpr (NN == 1) {
+        for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
+          const float r0 = fv(pc, tr), r1 = fv(pc + RS, tr + SEG_RT);
+          const float r2 = fv(pc + 2 * RS, tr + 2 * SEG_RT), r3 = fv(pc + 3 * RS, tr + 3 * SEG_RT);
+          pc[0] = r0; pc[RS] = r1; pc[2 * RS] = r2; pc[3 * RS] = r3;
+        }
+        for (; i < s1; i++, pc += RS, tr += SEG_RT) *pc = fv(pc, tr);
+      } else {
+        // a walking output pointer: one 64-bit add per row
+        const int64_t o = base + (int64_t)i * stride;
+        TO *po = out + o;
+        TO *po2 = out2 ? out2 + o : nullptr;
+        const TI *pi = in + o;
+        auto put = [&](float v) {
+          TO r;
+          if (FILT) r = (TO)(*pi + cvt<TI>(v));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+          else r = (TO)v;
+          *po = r;
+          po += stride;
+          if (out2) { *po2 = r; po2 += stride; }
+          if (FILT) pi += stride;
+        };
+        for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
+          const float r0 = fv(pc, tr), r1 = fv(pc + RS, tr + SEG_RT);
+          const float r2 = fv(pc + 2 * RS, tr + 2 * SEG_RT), r3 = fv(pc + 3 * RS, tr + 3 * SEG_RT);
+          put(r0); put(r1); put(r2); put(r3);
+        }
+        for (; i < s1; i++, pc += RS, tr += SEG_RT) put(fv(pc, tr));
+      }
+    }
+  }
+  if constexpr (NN == 1) {
+    __syncthreads();
+    const int64_t o0 = B.off + (int64_t)LT.t0 * L;
+    for (int ln = w; ln < nl; ln += nwarp)
+      for (int i = lane; i < L; i += 32) {
+        const int64_t p = o0 + (int64_t)ln * L + i;
+        const float v = tile[i * RS + ln];
+        TO r;
+        if (FILT) r = (TO)(in[p] + cvt<TI>(v));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+        else r = (TO)v;
+        out[p] = r;
+        if (out2) out2[p] = r;
+      }
   }
 }
 
@@ -1332,6 +1720,21 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   a.recv = e.recv;
   a.recv_fs = e.F * 6;
   a.drva = e.drva;
+  if constexpr (std::is_same<TC, float>::value) {
+    // the mixed path: segmented solves over tiles of SEG_LINES lines
+    const float *seg = filt ? e.segf : e.segd;
+    if (seg && e.nlts[nn] > 0) {
+      a.lt = e.lts[nn];
+      const int nt = SEG_LINES * seg_count(e.maxlen[nn]);
+      const size_t smem = seg_smem_bytes(e.maxlen[nn]);
+      const dim3 g(e.nlts[nn], io.nf);
+#define ATI_SEG(D, F) k_sweep_seg<D, F, TI, TO><<<g, nt, smem, st>>>(a, seg)
+      if (!filt) { if (nn == 1) ATI_SEG(1, false); else if (nn == 2) ATI_SEG(2, false); else ATI_SEG(3, false); }
+      else { if (nn == 1) ATI_SEG(1, true); else if (nn == 2) ATI_SEG(2, true); else ATI_SEG(3, true); }
+#undef ATI_SEG
+      return;
+    }
+  }
   const dim3 grid(e.nlt[nn], io.nf);
   if (nn == 1) {
     if (filt) k_sweep_xc<true, TI, TO, TC><<<grid, XC_NL, 0, st>>>(a);
@@ -1354,6 +1757,24 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
     if (nn == 2) k_sweep_g<2, true, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
     else k_sweep_g<3, true, false, TI, TO, TC><<<grid, tpb, 0, st>>>(a);
   }
+}
+
+// the segmented sweeps may take more than the default 48 KB of dynamic shared memory
+template <typename TI, typename TO>
+static cudaError_t seg_attr() {
+  const int v = (int)SEG_SMEM_MAX;
+  const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(k_sweep_seg<1, false, TI, TO>, A, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<2, false, TI, TO>, A, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<3, false, TI, TO>, A, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<1, true, TI, TO>, A, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<2, true, TI, TO>, A, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<3, true, TI, TO>, A, v);
+  return e;
+}
+cudaError_t seg_init() {
+  cudaError_t e = seg_attr<float, float>();
+  return e == cudaSuccess ? seg_attr<double, double>() : e;
 }
 
 void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io) {

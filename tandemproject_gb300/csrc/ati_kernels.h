@@ -38,6 +38,9 @@ struct Eng {
   int npt;
   const LTile *lt[4];   // line-sweep work queue per direction nn = 1..3
   int nlt[4];
+  const LTile *lts[4];  // segmented sweeps (mixed path): SEG_LINES lines per tile, per direction
+  int nlts[4];
+  const float *segd, *segf;  // their row tables (SEG_RT floats per factor row; derivative, filter)
   int sg_lines[4];      // lines per CTA of the eta (2) and zeta (3) sweeps: the tiles of lt[2], lt[3]
   int maxlen[4];        // longest line per direction
   int64_t N;            // points of all blocks
@@ -109,6 +112,34 @@ constexpr int PT_MIN = 256, PT_MAX = 4096, PT_DEFAULT = 256;
 // eta/zeta sweeps keep their forward values in shared memory up to this many bytes per CTA
 constexpr size_t SG_SMEM_FW = 48 * 1024;
 
+// Segmented line solves of the mixed path: SEG_LINES lines per CTA staged
+// whole in shared memory, each line cut into seg_count(L) segments of about
+// SEG_ROWS points (one warp per segment).  The segmentation is a function of
+// the line length alone, so a block's results do not depend on the other
+// blocks or cases of a handle.  Lines up to SEG_LMAX points fit the tile.
+constexpr int SEG_LINES = 32, SEG_ROWS = 48, SEG_MAX = 16, SEG_LMAX = 1600;
+constexpr size_t SEG_SMEM_MAX = 227 * 1024;
+__host__ __device__ inline int seg_count(int L) {
+  const int s = (L + SEG_ROWS - 1) / SEG_ROWS;
+  return s < 1 ? 1 : (s > SEG_MAX ? SEG_MAX : s);
+}
+// Row table of the segmented sweeps, SEG_RT floats per LU-factor row:
+//   [0] l0, [1] l1   forward-elimination factors (zero where the row has none)
+//   [4] g, [5] h     the row's forward values from incoming v(s0-2) = 1, v(s0-1) = 1
+//   [6] c2, [7] c3   back-substitution factors (c3 zero on the last row)
+//   [8] G, [9] H     the row's back-substituted values from b(s1) = 1, b(s1+1) = 1
+//   [10] c4          (zero on the last two rows); [2], [3], [11] unused
+constexpr int SEG_RT = 12;
+// first row of segment k of S on a line of L points (the first L % S segments hold one row more)
+__host__ __device__ inline int seg_start(int k, int L, int S) {
+  const int q = L / S, r = L % S;
+  return k * q + (k < r ? k : r);
+}
+// dynamic shared memory of a segmented sweep over lines of up to maxlen points
+inline size_t seg_smem_bytes(int maxlen) {
+  return (size_t)seg_count(maxlen) * SEG_LINES * 2 * 2 * sizeof(float) + (size_t)maxlen * (SEG_LINES + 1) * sizeof(float);
+}
+
 // per-field offsets of a closure (mpigo) over a wider input type
 template <typename TI>
 struct FieldOfs {
@@ -130,6 +161,7 @@ struct FieldOfs {
   void mpigo_ddf(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, int maxline, int nt,       \
                  int n45, const double *s1, const double *s2, const double *s3, int64_t fs, int nf,               \
                  const FieldOfs<double> &ofs);                                                                     \
+  cudaError_t seg_init();                                                                                          \
   void metric_divergence(const Eng<double> &e, cudaStream_t st, const double *d3, float *gm);                     \
   void pointwise_d(const Eng<double> &e, cudaStream_t st, int which);                                             \
   void pointwise_f(const Eng<float> &e, cudaStream_t st, int which);                                              \

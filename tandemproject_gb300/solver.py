@@ -73,6 +73,7 @@ SIGNATURES = {
     "ati_step_async": ([_vp, _i32], ctypes.c_int),
     "ati_jacobian_sign": ([_vp, _vp], ctypes.c_int),
     "ati_tiles": ([_vp, _vp], ctypes.c_int),
+    "ati_set_tiles": ([_vp, _vp], ctypes.c_int),
     "ati_check_conversions": ([ctypes.c_int64, _vp], ctypes.c_int),
     "ati_turbulence_modes": ([_vp, _i32, _vp, _vp], ctypes.c_int),
     "ati_turbulence_sample": ([_vp, _i32, ctypes.c_double, ctypes.c_int64, _dp, _dp], ctypes.c_int),
@@ -249,6 +250,11 @@ class Case:
         t = (ctypes.c_int32 * 4)()
         self._chk(self.L.ati_tiles(self.h, t))
         return tuple(t)
+
+    def set_tiles(self, eta=0, zeta=0, points=0):
+        """Pin the eta/zeta lines per CTA and points per tile (0 keeps the current one)."""
+        t = (ctypes.c_int32 * 4)(0, eta, zeta, points)
+        self._chk(self.L.ati_set_tiles(self.h, t))
 
     def jacobian_sign(self):
         """Per block: bit 0 some J > 0, bit 1 some J < 0, bit 2 J zero or not finite."""

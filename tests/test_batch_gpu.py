@@ -75,3 +75,26 @@ def test_autotuned_tiles_are_candidates(ati_lib):
     xi, s2, s3, pt = c.tiles()
     assert xi == 64 and s2 in (32, 64, 128, 256) and s3 in (32, 64, 128, 256) and pt in (256, 1024, 4096)
     c.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_pinned_tiles_give_identical_states(ati_lib, precision):
+    """Tile shapes (and with them the shared-memory or global forward values of
+    the eta/zeta sweeps) change timings only: states agree bit for bit."""
+    from tandemproject_gb300.config import small_case
+    from tandemproject_gb300.solver import AtiError, setup_case
+    cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), precision=precision)
+    a, b = setup_case(cfg), setup_case(cfg)
+    a.set_tiles(eta=32, zeta=256, points=256)
+    b.set_tiles(eta=256, zeta=32, points=4096)
+    assert a.tiles() == (64, 32, 256, 256) and b.tiles() == (64, 256, 32, 4096)
+    a.step(6)
+    b.step(6)
+    for mb in range(6):
+        np.testing.assert_array_equal(a.get_state(mb), b.get_state(mb))
+    with pytest.raises(AtiError):
+        a.set_tiles(eta=48)
+    with pytest.raises(AtiError):
+        a.set_tiles(points=300)
+    a.close()
+    b.close()
