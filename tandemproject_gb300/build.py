@@ -22,8 +22,8 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contrac
 # (source, object, extra flags): the kernels are compiled twice, with and
 # without FMA contraction; set-up kernels never contract
 SOURCES = [
-    ("ati_kernels.cu", "ati_kernels_fast.o", ["-DATI_KNS=fast", "-fmad=true"]),
-    ("ati_kernels.cu", "ati_kernels_strict.o", ["-DATI_KNS=strict", "-fmad=false"]),
+    ("ati_kernels.cu", "ati_kernels_fast.o", ["-DATI_KNS=fast", "-DATI_KFAST=1", "-fmad=true"]),
+    ("ati_kernels.cu", "ati_kernels_strict.o", ["-DATI_KNS=strict", "-DATI_KFAST=0", "-fmad=false"]),
     ("ati_api.cu", "ati_api.o", ["-fmad=false"]),
     ("ati_scheme.cpp", "ati_scheme.o", []),
     ("ati_probe.cu", "ati_probe.o", []),

@@ -640,6 +640,33 @@ static void seg_tables(const ati_handle *h, const std::vector<double> &fac, std:
   }
 }
 
+// Scaled-factor row tables of the FP64 fast path's line solves (solve_line_u,
+// layout at FU_RT): forward factors rescaled to carry u = c2 v, the stencil
+// weights k1..k3 times c2, the back-substitution factors with the entries past
+// the line end set to zero, and c2 itself.
+static void fu_tables(const ati_handle *h, const std::vector<double> &fac, double k1, double k2, double k3,
+                      std::vector<double> &out) {
+  out.assign((size_t)h->nfac * FU_RT, 0.0);
+  for (int gb = 0; gb < h->nb; gb++) {
+    const BlockDev &B = h->blk[gb];
+    for (int nn = 1; nn <= 3; nn++) {
+      const int L = nn == 1 ? B.lxi + 1 : (nn == 2 ? B.let + 1 : B.lze + 1);
+      const double *fc = &fac[(size_t)B.fac_off[nn] * 5];
+      double *o = &out[(size_t)B.fac_off[nn] * FU_RT];
+      for (int i = 0; i < L; i++) {
+        const double c2 = fc[i * 5 + 2];
+        double *r = o + (size_t)i * FU_RT;
+        r[0] = i >= 2 ? c2 * fc[i * 5 + 0] / fc[(i - 2) * 5 + 2] : 0.0;
+        r[1] = i >= 1 ? c2 * fc[i * 5 + 1] / fc[(i - 1) * 5 + 2] : 0.0;
+        r[2] = c2 * k1; r[3] = c2 * k2; r[4] = c2 * k3;
+        r[5] = i <= L - 2 ? fc[i * 5 + 3] : 0.0;
+        r[6] = i <= L - 3 ? fc[i * 5 + 4] : 0.0;
+        r[7] = c2;
+      }
+    }
+  }
+}
+
 template <typename T>
 static Coef<T> make_coef(const Scheme &S) {
   Coef<T> c;
@@ -734,7 +761,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_scal = take(sizeof(Scalars) * ncase), o_task = take(sizeof(FaceTask) * h->htasks.size()),
                o_jn = take(sizeof(JunctionDev) * 2 * ncase), o_woff = take(nforce * sizeof(int64_t)),
                o_pt = take(sizeof(PTile) * h->max_pt), o_lt1 = take(sizeof(LTile) * h->max_lt[1]),
-               o_lt2 = take(sizeof(LTile) * h->max_lt[2]), o_lt3 = take(sizeof(LTile) * h->max_lt[3]);
+               o_lt2 = take(sizeof(LTile) * h->max_lt[2]), o_lt3 = take(sizeof(LTile) * h->max_lt[3]),
+               o_facud = take((size_t)h->nfac * FU_RT * D8), o_facuf = take((size_t)h->nfac * FU_RT * D8);
   // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(3 x 5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
          o_frpex = 0, o_cff = 0, o_fdrvm = 0, o_lts[4] = {0, 0, 0, 0}, o_segd = 0, o_segf = 0;
@@ -780,6 +808,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   h->fw1 = f; f += N;
   d.drva = D(o_drva); d.drvb = D(o_drvb); d.recv = D(o_recv); d.cm = D(o_cm);
   d.facd = D(o_facd); d.facf = D(o_facf); d.sbcc = D(o_sbcc); d.rpex = D(o_rpex);
+  d.facud = D(o_facud); d.facuf = D(o_facuf);
   h->area = D(o_area); h->wnor = D(o_wnor); h->dforce = D(o_frc); h->dspg = D(o_spg);
   h->dtasks = (FaceTask *)(h->arena + o_task);
   h->djn = (JunctionDev *)(h->arena + o_jn);
@@ -852,6 +881,11 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   };
   up(d.facd, facd.data(), facd.size() * D8);
   up(d.facf, facf.data(), facf.size() * D8);
+  std::vector<double> facud, facuf;
+  fu_tables(h, facd, h->sh.s.aa, h->sh.s.ab, h->sh.s.ac, facud);
+  fu_tables(h, facf, h->sh.s.fa, h->sh.s.fb, h->sh.s.fc, facuf);
+  up(d.facud, facud.data(), facud.size() * D8);
+  up(d.facuf, facuf.data(), facuf.size() * D8);
   up(h->dspg, spg.data(), spg.size() * D8);
   up(dblk, h->blk.data(), sizeof(BlockDev) * h->nb);
   up(dsc, schemes.data(), sizeof(Scheme) * ncase);

@@ -20,9 +20,16 @@
 #ifndef ATI_KNS
 #error "compile with -DATI_KNS=fast or -DATI_KNS=strict"
 #endif
+#ifndef ATI_KFAST
+#error "compile with -DATI_KFAST=1 (fast) or -DATI_KFAST=0 (strict)"
+#endif
 
 namespace ati {
 namespace ATI_KNS {
+
+// the fast build may reorder the FP64 line solves (scaled-factor tables);
+// the strict build keeps the reference's operation order
+constexpr bool kFast = ATI_KFAST != 0;
 
 __device__ __forceinline__ int64_t idx3(int lxi, int let, int i, int j, int k, int nn) {
   // src/Subroutineso.f90:364-375
@@ -250,6 +257,92 @@ __device__ __forceinline__ void solve_line(const Coef<TC> &C, const TC *fac, int
   first = b1;
 }
 
+// The FP64 fast path's line solve: the same elimination with the forward
+// values carried as u = c2 v (scaled-factor rows, FU_RT per row), 10 FP64
+// operations per point of a derivative instead of 11.  Pipelined like solve_line.
+template <bool FILT, class Src, class Fw, class Sink>
+__device__ __forceinline__ void solve_line_u(const Coef<double> &C, const double *fu, int L, int ns, int ne,
+                                             const double *rcv, int64_t nbs, int jk, const Src &ld, Fw &fw, Sink &put,
+                                             double &first, double &last) {
+  double sbs0, sbs1, sbs2, sbe0, sbe1, sbe2;
+  line_ends<FILT, double>(C, L, ns, ne, rcv, nbs, jk, ld, sbs0, sbs1, sbs2, sbe0, sbe1, sbe2);
+  double a0 = ld(0), a1 = ld(1), a2 = ld(2), a3 = ld(3), a4 = ld(4), a5 = ld(5);
+  auto F = [&](int i, int k) { return __ldg(fu + i * FU_RT + k); };
+  double u2 = F(0, 7) * sbs0;
+  double u1 = F(1, 7) * sbs1 - F(1, 1) * u2;
+  fw.st(0, u2);
+  fw.st(1, u1);
+  {
+    const double v = F(2, 7) * sbs2 - F(2, 0) * u2 - F(2, 1) * u1;
+    fw.st(2, v);
+    u2 = u1; u1 = v;
+  }
+  auto fstep = [&](int i, double a6) {
+    double r;
+    if (!FILT) {
+      r = F(i, 2) * (a4 - a2) + F(i, 3) * (a5 - a1) + F(i, 4) * (a6 - a0);
+    } else {
+      const double t = 2.0 * a3;
+      r = F(i, 2) * (a2 + a4 - t) + F(i, 3) * (a1 + a5 - t) + F(i, 4) * (a0 + a6 - t);
+    }
+    const double v = r - F(i, 0) * u2 - F(i, 1) * u1;
+    fw.st(i, v);
+    u2 = u1; u1 = v;
+    a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
+  };
+  const int iend = L - 4;
+  int i = 3;
+  if (i + 3 <= iend) {
+    double n0 = ld(i + 3), n1 = ld(i + 4), n2 = ld(i + 5), n3 = ld(i + 6);
+    for (; i + 3 <= iend; i += 4) {
+      const double c0 = n0, c1 = n1, c2 = n2, c3 = n3;
+      if (i + 7 <= iend) { n0 = ld(i + 7); n1 = ld(i + 8); n2 = ld(i + 9); n3 = ld(i + 10); }
+      fstep(i, c0);
+      fstep(i + 1, c1);
+      fstep(i + 2, c2);
+      fstep(i + 3, c3);
+    }
+  }
+  for (; i <= iend; i++) fstep(i, ld(i + 3));
+  {
+    int k = L - 3;
+    double v = F(k, 7) * sbe2 - F(k, 0) * u2 - F(k, 1) * u1;
+    fw.st(k, v);
+    u2 = u1; u1 = v;
+    k = L - 2;
+    v = F(k, 7) * sbe1 - F(k, 0) * u2 - F(k, 1) * u1;
+    fw.st(k, v);
+    u2 = u1; u1 = v;
+    k = L - 1;
+    v = F(k, 7) * sbe0 - F(k, 0) * u2 - F(k, 1) * u1;
+    u2 = u1; u1 = v;  // u1 = u(L-1), u2 = u(L-2)
+  }
+  double b0 = u1;
+  double b1 = u2 - F(L - 2, 5) * b0;
+  last = b0;
+  put(L - 1, b0);
+  put(L - 2, b1);
+  auto bstep = [&](int k, double w) {
+    const double v = w - F(k, 5) * b1 - F(k, 6) * b0;
+    put(k, v);
+    b0 = b1; b1 = v;
+  };
+  int k = L - 3;
+  if (k >= 3) {
+    double m0 = fw.ld(k), m1 = fw.ld(k - 1), m2 = fw.ld(k - 2), m3 = fw.ld(k - 3);
+    for (; k >= 3; k -= 4) {
+      const double c0 = m0, c1 = m1, c2 = m2, c3 = m3;
+      if (k >= 7) { m0 = fw.ld(k - 4); m1 = fw.ld(k - 5); m2 = fw.ld(k - 6); m3 = fw.ld(k - 7); }
+      bstep(k, c0);
+      bstep(k - 1, c1);
+      bstep(k - 2, c2);
+      bstep(k - 3, c3);
+    }
+  }
+  for (; k >= 0; k--) bstep(k, fw.ld(k));
+  first = b1;
+}
+
 // line geometry of direction NN: base point, stride, face index, length
 template <int NN>
 __device__ __forceinline__ bool line_geom(const BlockDev &B, int t, int64_t &base, int64_t &stride, int &jk, int &L) {
@@ -326,6 +419,7 @@ struct SweepArgs {
   const TC *recv;
   int64_t recv_fs;
   TC *drva;
+  const double *facu;  // FP64 fast path: scaled-factor rows (FU_RT per row)
 };
 
 // eta and zeta lines: one thread per line; consecutive threads own
@@ -349,6 +443,8 @@ __global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
   const int64_t nbs = B.nbsize[NN];
   const TC *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
   const TC *fac = a.fac + B.fac_off[NN] * 5;
+  constexpr bool UF = kFast && std::is_same<TC, double>::value;  // scaled-factor rows
+  const double *fu = UF ? a.facu + B.fac_off[NN] * FU_RT : nullptr;
   const TI *pin = a.io.in + f * a.io.in_fs + base;
   GlobalSrc<TI, TC> ld{pin, stride, a.io.ofs[f]};
   TO *o2 = a.io.out2 ? a.io.out2 + f * a.io.out_fs + base : nullptr;
@@ -372,10 +468,12 @@ __global__ void __launch_bounds__(SG_MAX) k_sweep_g(SweepArgs<TI, TO, TC> a) {
     SmemFw<TC> fw{col, P};
     const SmemFw<TC> lds{col, P};
     auto sld = [&](int i) { return lds.ld(i); };
-    solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, sld, fw, put, first, last);
+    if constexpr (UF) solve_line_u<FILT>(C, fu, L, ns, ne, rcv, nbs, jk, sld, fw, put, first, last);
+    else solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, sld, fw, put, first, last);
   } else {
     GlobalFw<TC> fw{a.fw + f * a.fw_fs + base, stride};
-    solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
+    if constexpr (UF) solve_line_u<FILT>(C, fu, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
+    else solve_line<FILT, TC>(C, fac, L, ns, ne, rcv, nbs, jk, ld, fw, put, first, last);
   }
   if (!FILT && a.io.drva) {
     TC *d = a.drva + B.face_off[NN] * 10;
@@ -420,8 +518,15 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
   TO *out2 = a.io.out2 ? a.io.out2 + f * a.io.out_fs + off : nullptr;
   const Coef<TC> &C = *a.cf;
   const TC *fac = a.fac + B.fac_off[1] * 5;
+  constexpr bool UF = kFast && std::is_same<TC, double>::value;  // scaled-factor rows (see solve_line_u)
+  const double *fu = UF ? a.facu + B.fac_off[1] * FU_RT : nullptr;
   const int jk = t0 + t;
   const int64_t nbs = B.nbsize[1];
+  // forward row i from a closure right-hand side sb (rows 0-2 and the last three)
+  auto end_row = [&](int i, TC sb, TC g2, TC g1) -> TC {
+    if constexpr (UF) return fu[i * FU_RT + 7] * sb - fu[i * FU_RT + 0] * g2 - fu[i * FU_RT + 1] * g1;
+    else return sb - fac[i * 5 + 0] * g2 - fac[i * 5 + 1] * g1;
+  };
 
   // boundary rows and the first window from the line itself
   TC sbs0 = 0, sbs1 = 0, sbs2 = 0, sbe0 = 0, sbe1 = 0, sbe2 = 0;
@@ -431,10 +536,15 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
     GlobalSrc<TI, TC> ld{in + (int64_t)t * L, 1, a.io.ofs[f]};
     line_ends<FILT, TC>(C, L, B.ndf[0][1], B.ndf[1][1], rcv, nbs, jk, ld, sbs0, sbs1, sbs2, sbe0, sbe1, sbe2);
     a0 = ld(0); a1 = ld(1); a2 = ld(2); a3 = ld(3); a4 = ld(4); a5 = ld(5);
-    f2 = sbs0;
-    f1 = sbs1 - fac[1 * 5 + 1] * f2;
+    if constexpr (UF) {
+      f2 = fu[7] * sbs0;
+      f1 = fu[FU_RT + 7] * sbs1 - fu[FU_RT + 1] * f2;
+    } else {
+      f2 = sbs0;
+      f1 = sbs1 - fac[1 * 5 + 1] * f2;
+    }
     w0 = f2; w1 = f1;
-    const TC v = sbs2 - fac[2 * 5 + 0] * f2 - fac[2 * 5 + 1] * f1;
+    const TC v = end_row(2, sbs2, f2, f1);
     w2 = v;
     f2 = f1; f1 = v;
   }
@@ -473,8 +583,21 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
       for (int s = s0; s < cl; s++) {
         const int i = c0 + s - 3;
         const TC a6 = tile[bf][s][t];
-        const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
-        const TC v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+        TC v;
+        if constexpr (UF) {
+          const double *r = fu + i * FU_RT;
+          TC sb;
+          if (!FILT) {
+            sb = r[2] * (a4 - a2) + r[3] * (a5 - a1) + r[4] * (a6 - a0);
+          } else {
+            const TC q = 2.0 * a3;
+            sb = r[2] * (a2 + a4 - q) + r[3] * (a1 + a5 - q) + r[4] * (a0 + a6 - q);
+          }
+          v = sb - r[0] * f2 - r[1] * f1;
+        } else {
+          const TC sb = interior_rhs<FILT, TC>(C, a0, a1, a2, a3, a4, a5, a6);
+          v = sb - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+        }
         tile[bf][s][t] = v;
         f2 = f1; f1 = v;
         a0 = a1; a1 = a2; a2 = a3; a3 = a4; a4 = a5; a5 = a6;
@@ -487,19 +610,23 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
   // the last three rows and the first three results, in registers
   TC b0 = 0, b1 = 0;
   if (act) {
-    int i = L - 3;
-    TC v = sbe2 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    TC v = end_row(L - 3, sbe2, f2, f1);
     const TC fwl3 = v;
     f2 = f1; f1 = v;
-    i = L - 2;
-    v = sbe1 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    v = end_row(L - 2, sbe1, f2, f1);
     f2 = f1; f1 = v;
-    i = L - 1;
-    v = sbe0 - fac[i * 5 + 0] * f2 - fac[i * 5 + 1] * f1;
+    v = end_row(L - 1, sbe0, f2, f1);
     f2 = f1; f1 = v;
-    b0 = fac[(L - 1) * 5 + 2] * f1;
-    b1 = fac[(L - 2) * 5 + 2] * f2 - fac[(L - 2) * 5 + 3] * b0;
-    const TC r3 = fac[(L - 3) * 5 + 2] * fwl3 - fac[(L - 3) * 5 + 3] * b1 - fac[(L - 3) * 5 + 4] * b0;
+    TC r3;
+    if constexpr (UF) {
+      b0 = f1;
+      b1 = f2 - fu[(L - 2) * FU_RT + 5] * b0;
+      r3 = fwl3 - fu[(L - 3) * FU_RT + 5] * b1 - fu[(L - 3) * FU_RT + 6] * b0;
+    } else {
+      b0 = fac[(L - 1) * 5 + 2] * f1;
+      b1 = fac[(L - 2) * 5 + 2] * f2 - fac[(L - 2) * 5 + 3] * b0;
+      r3 = fac[(L - 3) * 5 + 2] * fwl3 - fac[(L - 3) * 5 + 3] * b1 - fac[(L - 3) * 5 + 4] * b0;
+    }
     if (!FILT && a.io.drva) {
       TC *d = a.drva + B.face_off[1] * 10;
       d[jk + nbs * ((a.io.m0 + f - 1) + 5 * 1)] = b0;  // drva(jk,m,1) = sb(ie)
@@ -538,7 +665,9 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
       const int se = c0 == 0 ? 3 : 0;
       for (int s = cl - 1; s >= se; s--) {
         const int i = c0 + s - 3;
-        const TC v = fac[i * 5 + 2] * tile[bf][s][t] - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
+        TC v;
+        if constexpr (UF) v = tile[bf][s][t] - fu[i * FU_RT + 5] * b1 - fu[i * FU_RT + 6] * b0;
+        else v = fac[i * 5 + 2] * tile[bf][s][t] - fac[i * 5 + 3] * b1 - fac[i * 5 + 4] * b0;
         tile[bf][s][t] = v;
         b0 = b1; b1 = v;
       }
@@ -1139,6 +1268,44 @@ __global__ void k_flux(Eng<R> e) {
         const R q = cvt<R>(e.qa[g]);
         F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
       }
+      if constexpr (kFast && !Freestream<R>::on) {
+        // FP64 fast path, the same fluxes with fewer FP64 operations (about 70
+        // instead of 85 a point): pressure and stress combined per component,
+        // sigma = p I - tau, and the energy flux as (rhoE + p) U - grad(xi) . (p u_inf + h)
+        const R pu1 = pp * u1, pu2 = pp * u2, pu3 = pp * u3;
+        R w1 = pu1, w2 = pu2, w3 = pu3;
+        R sg[3][3];
+        if (visc) {
+          const R txx = t[g], tyy = t[g + N], tzz = t[g + 2 * N];
+          const R txy = t[g + 3 * N], tyz = t[g + 4 * N], tzx = t[g + 5 * N];
+          sg[0][0] = pp - txx; sg[1][1] = pp - tyy; sg[2][2] = pp - tzz;
+          sg[0][1] = sg[1][0] = -txy; sg[1][2] = sg[2][1] = -tyz; sg[0][2] = sg[2][0] = -tzx;
+          w1 = pu1 + t[g + 6 * N]; w2 = pu2 + t[g + 7 * N]; w3 = pu3 + t[g + 8 * N];
+        }
+  #pragma unroll
+        for (int m = 2; m <= 4; m++) {
+          const R q = cvt<R>(e.qa[g + (m - 1) * N]);
+          const int r = m - 2;
+          R a, b, c;
+          if (visc) {
+            a = q * s1 + x1 * sg[r][0] + x2 * sg[r][1] + x3 * sg[r][2];
+            b = q * s2 + e1 * sg[r][0] + e2 * sg[r][1] + e3 * sg[r][2];
+            c = q * s3 + z1 * sg[r][0] + z2 * sg[r][1] + z3 * sg[r][2];
+          } else {
+            const R xm = r == 0 ? x1 : (r == 1 ? x2 : x3), em = r == 0 ? e1 : (r == 1 ? e2 : e3);
+            const R zm = r == 0 ? z1 : (r == 1 ? z2 : z3);
+            a = q * s1 + xm * pp; b = q * s2 + em * pp; c = q * s3 + zm * pp;
+          }
+          F[g + ((m - 1) * 3 + 0) * N] = a;
+          F[g + ((m - 1) * 3 + 1) * N] = b;
+          F[g + ((m - 1) * 3 + 2) * N] = c;
+        }
+        const R d5 = cvt<R>(e.qa[g + 4 * N]) + pp;
+        F[g + 12 * N] = d5 * s1 - (x1 * w1 + x2 * w2 + x3 * w3);
+        F[g + 13 * N] = d5 * s2 - (e1 * w1 + e2 * w2 + e3 * w3);
+        F[g + 14 * N] = d5 * s3 - (z1 * w1 + z2 * w2 + z3 * w3);
+        continue;
+      }
       R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
       if (visc) {
         ta[0] = t[g]; tb[0] = t[g + 3 * N]; tc[0] = t[g + 5 * N];
@@ -1714,6 +1881,7 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   a.lt = e.lt[nn];
   a.cf = e.cf;
   a.fac = filt ? e.facf : e.facd;
+  a.facu = filt ? e.facuf : e.facud;
   a.io = io;
   a.fw = e.fw + (nn - 1) * e.fw_dir;  // sweeps of different directions may run at once
   a.fw_fs = e.N;

@@ -41,6 +41,7 @@ struct Eng {
   const LTile *lts[4];  // segmented sweeps (mixed path): SEG_LINES lines per tile, per direction
   int nlts[4];
   const float *segd, *segf;  // their row tables (SEG_RT floats per factor row; derivative, filter)
+  const double *facud, *facuf;  // FP64 fast path: scaled-factor row tables (FU_RT per row; derivative, filter)
   int sg_lines[4];      // lines per CTA of the eta (2) and zeta (3) sweeps: the tiles of lt[2], lt[3]
   int maxlen[4];        // longest line per direction
   int64_t N;            // points of all blocks
@@ -130,6 +131,16 @@ __host__ __device__ inline int seg_count(int L) {
 //   [8] G, [9] H     the row's back-substituted values from b(s1) = 1, b(s1+1) = 1
 //   [10] c4          (zero on the last two rows); [2], [3], [11] unused
 constexpr int SEG_RT = 12;
+// Scaled-factor row table of the FP64 fast path's line solves, FU_RT doubles
+// per LU-factor row.  The forward values are carried as u(i) = c2(i) v(i), so
+// the back substitution needs no multiply by c2:
+//   u(i) = c2(i) r(i) - l0'(i) u(i-2) - l1'(i) u(i-1),  l0' = c2(i) l0 / c2(i-2), l1' = c2(i) l1 / c2(i-1)
+//   b(i) = u(i) - c3(i) b(i+1) - c4(i) b(i+2)
+// with the interior right-hand side c2(i) r(i) formed from the row's own
+// weights A, B, C (c2 times the scheme's three stencil weights):
+//   [0] l0', [1] l1' (zero where the row has none), [2] A, [3] B, [4] C,
+//   [5] c3, [6] c4 (zero past the line end), [7] c2
+constexpr int FU_RT = 8;
 // first row of segment k of S on a line of L points (the first L % S segments hold one row more)
 __host__ __device__ inline int seg_start(int k, int L, int S) {
   const int q = L / S, r = L % S;
