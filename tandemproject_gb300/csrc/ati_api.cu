@@ -662,6 +662,7 @@ static void fu_tables(const ati_handle *h, const std::vector<double> &fac, doubl
         r[5] = i <= L - 2 ? fc[i * 5 + 3] : 0.0;
         r[6] = i <= L - 3 ? fc[i * 5 + 4] : 0.0;
         r[7] = c2;
+        r[8] = 2.0 * (r[2] + r[3] + r[4]);
       }
     }
   }

@@ -282,8 +282,7 @@ __device__ __forceinline__ void solve_line_u(const Coef<double> &C, const double
     if (!FILT) {
       r = F(i, 2) * (a4 - a2) + F(i, 3) * (a5 - a1) + F(i, 4) * (a6 - a0);
     } else {
-      const double t = 2.0 * a3;
-      r = F(i, 2) * (a2 + a4 - t) + F(i, 3) * (a1 + a5 - t) + F(i, 4) * (a0 + a6 - t);
+      r = F(i, 2) * (a2 + a4) + F(i, 3) * (a1 + a5) + F(i, 4) * (a0 + a6) - F(i, 8) * a3;
     }
     const double v = r - F(i, 0) * u2 - F(i, 1) * u1;
     fw.st(i, v);
@@ -590,8 +589,7 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
           if (!FILT) {
             sb = r[2] * (a4 - a2) + r[3] * (a5 - a1) + r[4] * (a6 - a0);
           } else {
-            const TC q = 2.0 * a3;
-            sb = r[2] * (a2 + a4 - q) + r[3] * (a1 + a5 - q) + r[4] * (a0 + a6 - q);
+            sb = r[2] * (a2 + a4) + r[3] * (a1 + a5) + r[4] * (a0 + a6) - r[8] * a3;
           }
           v = sb - r[0] * f2 - r[1] * f1;
         } else {

@@ -139,8 +139,10 @@ constexpr int SEG_RT = 12;
 // with the interior right-hand side c2(i) r(i) formed from the row's own
 // weights A, B, C (c2 times the scheme's three stencil weights):
 //   [0] l0', [1] l1' (zero where the row has none), [2] A, [3] B, [4] C,
-//   [5] c3, [6] c4 (zero past the line end), [7] c2
-constexpr int FU_RT = 8;
+//   [5] c3, [6] c4 (zero past the line end), [7] c2,
+//   [8] D = 2 (A + B + C) (the filter's centre weight: its right-hand side is
+//       A (a(i-1) + a(i+1)) + B (a(i-2) + a(i+2)) + C (a(i-3) + a(i+3)) - D a(i)), [9] unused
+constexpr int FU_RT = 10;
 // first row of segment k of S on a line of L points (the first L % S segments hold one row more)
 __host__ __device__ inline int seg_start(int k, int L, int S) {
   const int q = L / S, r = L % S;
