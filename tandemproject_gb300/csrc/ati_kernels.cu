@@ -1228,6 +1228,61 @@ __global__ void k_visc(Eng<R> e) {
   }
 }
 
+// The FP64 fast path's fluxes at one point: the same fifteen components with
+// fewer FP64 operations (about 70 instead of 85): pressure and stress
+// combined, sigma = p I - tau, and the energy flux as
+// (rhoE + p) U - grad(xi) . (p u_inf + h).  VISC is a template argument so
+// that only one variant's operations are issued (a branch inside the point
+// loop was predicated, both sides executed).
+template <bool VISC>
+__device__ __forceinline__ void flux_fast_point(const Eng<double> &e, int64_t N, int64_t g, double u1, double u2,
+                                                double u3) {
+  const double *t = e.tau;
+  double *F = e.flx;
+  const double x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
+  const double e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
+  const double z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+  const double pp = e.p[g];
+  const double r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
+  const double s1 = x1 * r1 + x2 * r2 + x3 * r3;
+  const double s2 = e1 * r1 + e2 * r2 + e3 * r3;
+  const double s3 = z1 * r1 + z2 * r2 + z3 * r3;
+  const double q = e.qa[g];
+  F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
+  double w1, w2, w3, sg[3][3];
+  if constexpr (VISC) {
+    const double txx = t[g], tyy = t[g + N], tzz = t[g + 2 * N];
+    const double txy = t[g + 3 * N], tyz = t[g + 4 * N], tzx = t[g + 5 * N];
+    sg[0][0] = pp - txx; sg[1][1] = pp - tyy; sg[2][2] = pp - tzz;
+    sg[0][1] = sg[1][0] = -txy; sg[1][2] = sg[2][1] = -tyz; sg[0][2] = sg[2][0] = -tzx;
+    w1 = fma(pp, u1, t[g + 6 * N]); w2 = fma(pp, u2, t[g + 7 * N]); w3 = fma(pp, u3, t[g + 8 * N]);
+  } else {
+    w1 = pp * u1; w2 = pp * u2; w3 = pp * u3;
+  }
+#pragma unroll
+  for (int m = 2; m <= 4; m++) {
+    const double qm = e.qa[g + (m - 1) * N];
+    const int r = m - 2;
+    double a, b, c;
+    if constexpr (VISC) {
+      a = qm * s1 + x1 * sg[r][0] + x2 * sg[r][1] + x3 * sg[r][2];
+      b = qm * s2 + e1 * sg[r][0] + e2 * sg[r][1] + e3 * sg[r][2];
+      c = qm * s3 + z1 * sg[r][0] + z2 * sg[r][1] + z3 * sg[r][2];
+    } else {
+      const double xm = r == 0 ? x1 : (r == 1 ? x2 : x3), em = r == 0 ? e1 : (r == 1 ? e2 : e3);
+      const double zm = r == 0 ? z1 : (r == 1 ? z2 : z3);
+      a = qm * s1 + xm * pp; b = qm * s2 + em * pp; c = qm * s3 + zm * pp;
+    }
+    F[g + ((m - 1) * 3 + 0) * N] = a;
+    F[g + ((m - 1) * 3 + 1) * N] = b;
+    F[g + ((m - 1) * 3 + 2) * N] = c;
+  }
+  const double d5 = e.qa[g + 4 * N] + pp;
+  F[g + 12 * N] = d5 * s1 - (x1 * w1 + x2 * w2 + x3 * w3);
+  F[g + 13 * N] = d5 * s2 - (e1 * w1 + e2 * w2 + e3 * w3);
+  F[g + 14 * N] = d5 * s3 - (z1 * w1 + z2 * w2 + z3 * w3);
+}
+
 // contravariant velocities and the fifteen flux components
 // (src/Main3D.f90:710-766): flx plane (m-1)*3 + (nn-1)
 template <typename R>
@@ -1238,6 +1293,11 @@ __global__ void k_flux(Eng<R> e) {
     Scalars &SC = e.scal[T.cs];
     const R u1 = (R)SC.umf[1], u2 = (R)SC.umf[2], u3 = (R)SC.umf[3];
     const bool visc = S.nviscous == 1;
+    if constexpr (kFast && !Freestream<R>::on) {
+      if (visc) { POINT_LOOP(T, g) flux_fast_point<true>(e, N, g, u1, u2, u3); }
+      else { POINT_LOOP(T, g) flux_fast_point<false>(e, N, g, u1, u2, u3); }
+      continue;
+    }
     const R *t = e.tau;
     R *F = e.flx;
     POINT_LOOP(T, g) {
@@ -1265,44 +1325,6 @@ __global__ void k_flux(Eng<R> e) {
         s3 = z1 * r1 + z2 * r2 + z3 * r3;
         const R q = cvt<R>(e.qa[g]);
         F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
-      }
-      if constexpr (kFast && !Freestream<R>::on) {
-        // FP64 fast path, the same fluxes with fewer FP64 operations (about 70
-        // instead of 85 a point): pressure and stress combined per component,
-        // sigma = p I - tau, and the energy flux as (rhoE + p) U - grad(xi) . (p u_inf + h)
-        const R pu1 = pp * u1, pu2 = pp * u2, pu3 = pp * u3;
-        R w1 = pu1, w2 = pu2, w3 = pu3;
-        R sg[3][3];
-        if (visc) {
-          const R txx = t[g], tyy = t[g + N], tzz = t[g + 2 * N];
-          const R txy = t[g + 3 * N], tyz = t[g + 4 * N], tzx = t[g + 5 * N];
-          sg[0][0] = pp - txx; sg[1][1] = pp - tyy; sg[2][2] = pp - tzz;
-          sg[0][1] = sg[1][0] = -txy; sg[1][2] = sg[2][1] = -tyz; sg[0][2] = sg[2][0] = -tzx;
-          w1 = pu1 + t[g + 6 * N]; w2 = pu2 + t[g + 7 * N]; w3 = pu3 + t[g + 8 * N];
-        }
-  #pragma unroll
-        for (int m = 2; m <= 4; m++) {
-          const R q = cvt<R>(e.qa[g + (m - 1) * N]);
-          const int r = m - 2;
-          R a, b, c;
-          if (visc) {
-            a = q * s1 + x1 * sg[r][0] + x2 * sg[r][1] + x3 * sg[r][2];
-            b = q * s2 + e1 * sg[r][0] + e2 * sg[r][1] + e3 * sg[r][2];
-            c = q * s3 + z1 * sg[r][0] + z2 * sg[r][1] + z3 * sg[r][2];
-          } else {
-            const R xm = r == 0 ? x1 : (r == 1 ? x2 : x3), em = r == 0 ? e1 : (r == 1 ? e2 : e3);
-            const R zm = r == 0 ? z1 : (r == 1 ? z2 : z3);
-            a = q * s1 + xm * pp; b = q * s2 + em * pp; c = q * s3 + zm * pp;
-          }
-          F[g + ((m - 1) * 3 + 0) * N] = a;
-          F[g + ((m - 1) * 3 + 1) * N] = b;
-          F[g + ((m - 1) * 3 + 2) * N] = c;
-        }
-        const R d5 = cvt<R>(e.qa[g + 4 * N]) + pp;
-        F[g + 12 * N] = d5 * s1 - (x1 * w1 + x2 * w2 + x3 * w3);
-        F[g + 13 * N] = d5 * s2 - (e1 * w1 + e2 * w2 + e3 * w3);
-        F[g + 14 * N] = d5 * s3 - (z1 * w1 + z2 * w2 + z3 * w3);
-        continue;
       }
       R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
       if (visc) {
