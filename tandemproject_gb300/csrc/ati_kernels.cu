@@ -1392,6 +1392,10 @@ __global__ void k_div(Eng<R> e) {
     POINT_LOOP(T, g) {
       const R as = e.asz[g], bs = e.bsz[g];
       const bool sponge = as != (R)0 || bs != (R)0;
+      // the mixed path: the sponge zone is a thin layer, and warps without a sponge point skip its FP64
+      // subtractions and conversions (a warp vote makes the branch a real one; a per-point test was
+      // predicated and issued that FP64 work everywhere).  The FP64 kernel streams and keeps one variant.
+      const bool any_sponge = Freestream<R>::on ? __any_sync(__activemask(), sponge) : true;
       R fs[5] = {0, 0, 0, 0, 0};
       if constexpr (Freestream<R>::on) {
         // divergence of the freestream fluxes: rho_inf, p_inf, rhoE_inf times the metric divergence
@@ -1401,23 +1405,28 @@ __global__ void k_div(Eng<R> e) {
         fs[1] = (R)S.poo * g1; fs[2] = (R)S.poo * g2; fs[3] = (R)S.poo * g3;
         fs[4] = (R)(S.hamm1 * S.poo) * ug;
       }
+      // two versions of the point's update, chosen per warp
+      auto update = [&](auto with_sponge) {
   #pragma unroll
-      for (int m = 1; m <= 5; m++) {
-        R d = F[g + ((m - 1) * 3 + 0) * N] + F[g + ((m - 1) * 3 + 1) * N] + F[g + ((m - 1) * 3 + 2) * N];
-        if constexpr (Freestream<R>::on) d = d + fs[m - 1];
-        if (sponge) {
-          if constexpr (Freestream<R>::on) {  // the pressure plane already holds p - p_inf, p_inf = 1/gamma
-            if (m == 1) d = d + as * cvt<R>(e.qa[g] - 1.0);
-            else if (m <= 4) d = d + as * cvt<R>(e.qa[g + (m - 1) * N]);
-            else d = d + bs * e.p[g];
-          } else {
-            if (m == 1) d = d + as * (cvt<R>(e.qa[g]) - (R)1);
-            else if (m <= 4) d = d + as * (cvt<R>(e.qa[g + (m - 1) * N]) - (R)0);
-            else d = d + bs * (e.p[g] - ham * (R)1);
+        for (int m = 1; m <= 5; m++) {
+          R d = F[g + ((m - 1) * 3 + 0) * N] + F[g + ((m - 1) * 3 + 1) * N] + F[g + ((m - 1) * 3 + 2) * N];
+          if constexpr (Freestream<R>::on) d = d + fs[m - 1];
+          if (decltype(with_sponge)::value && sponge) {
+            if constexpr (Freestream<R>::on) {  // the pressure plane already holds p - p_inf, p_inf = 1/gamma
+              if (m == 1) d = d + as * cvt<R>(e.qa[g] - 1.0);
+              else if (m <= 4) d = d + as * cvt<R>(e.qa[g + (m - 1) * N]);
+              else d = d + bs * e.p[g];
+            } else {
+              if (m == 1) d = d + as * (cvt<R>(e.qa[g]) - (R)1);
+              else if (m <= 4) d = d + as * (cvt<R>(e.qa[g + (m - 1) * N]) - (R)0);
+              else d = d + bs * (e.p[g] - ham * (R)1);
+            }
           }
+          e.de[g + (m - 1) * N] = d;
         }
-        e.de[g + (m - 1) * N] = d;
-      }
+      };
+      if (!Freestream<R>::on || any_sponge) update(std::true_type{});
+      else update(std::false_type{});
     }
   }
 }
