@@ -105,3 +105,11 @@ def test_integer_pipe_conversions_match_the_instructions(ati_lib):
     bad = ctypes.c_int64(-1)
     assert L.ati_check_conversions(1 << 24, ctypes.byref(bad)) == 0
     assert bad.value == 0
+
+
+def test_mixed_rejects_lines_beyond_the_segmented_tile(ati_lib):
+    """The mixed path's segmented solves hold a line of up to 1,600 points in shared memory."""
+    from tandemproject_gb300.config import MIXED, small_case
+    from tandemproject_gb300.solver import AtiError
+    with pytest.raises(AtiError):
+        make(small_case(lxibk=(1700, 64, 64), precision=MIXED))
