@@ -393,19 +393,16 @@ def main():
                  "tiles": list(mtiles),
                  "kernel_share": {k: round(v[0] / mtot, 4) for k, v in mprof.items() if v[1]}}
 
-    # end to end through the C ABI: pinned host state in, step, state out
-    host = [torch.empty(5 * case.npts(mb), dtype=torch.float64, pin_memory=True) for mb in range(cfg.nblocks)]
-    hnp = [h.numpy() for h in host]
-    for mb in range(cfg.nblocks):
-        case.get_state(mb, out=hnp[mb])
+    # end to end through the C ABI: pinned host state in (one copy of every block), step, state out
+    host = torch.empty(5 * case.points_total(), dtype=torch.float64, pin_memory=True)
+    hnp = host.numpy()
+    case.get_state_all(out=hnp)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        for mb in range(cfg.nblocks):
-            case.set_state(mb, hnp[mb])
+        case.set_state_all(hnp)
         case.step(1)
-        for mb in range(cfg.nblocks):
-            case.get_state(mb, out=hnp[mb])
+        case.get_state_all(out=hnp)
     barrier()
     t_e2e = time.perf_counter() - t0
     if dist is not None:

@@ -203,6 +203,15 @@ int ati_jacobian_sign(ati_handle_t *h, int32_t *flags);
 /* State and field copies (block blk, Fortran layout, all components). */
 int ati_set_state(ati_handle_t *h, int blk, const double *q);
 int ati_get_state(ati_handle_t *h, int blk, double *q);
+/* The whole state of a handle in one transfer per direction (no counterpart in
+ * the reference, where each MPI rank holds one block): q[c * n + g] for
+ * component c = 0..4 and point g of all blocks in handle order (block b's
+ * points at g = off_b .. off_b + npts_b - 1, off_b the sum of the earlier
+ * blocks' npts), n = ati_points_total.  With pinned host memory each call is
+ * one DMA copy; ati_get_state_all waits for it. */
+int ati_set_state_all(ati_handle_t *h, const double *q);
+int ati_get_state_all(ati_handle_t *h, double *q);
+int ati_points_total(ati_handle_t *h, int64_t *n);
 int ati_set_field(ati_handle_t *h, int blk, int field, const double *v);
 int ati_get_field(ati_handle_t *h, int blk, int field, double *v);
 int ati_get_face(ati_handle_t *h, int blk, int which, int nn, double *v);

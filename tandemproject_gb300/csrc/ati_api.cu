@@ -1034,6 +1034,24 @@ extern "C" int ati_set_state(ati_handle_t *h, int blk, const double *q) {
 }
 extern "C" int ati_get_state(ati_handle_t *h, int blk, double *q) { return copy_field(h, blk, ATI_F_QA, q, false); }
 
+// the state planes qa are one contiguous [5][N] array: the whole state is one copy
+extern "C" int ati_set_state_all(ati_handle_t *h, const double *q) {
+  if (!h || !q) return fail(h, ATI_EINVAL, "ati_set_state_all: bad argument");
+  CK(cudaMemcpyAsync(h->ed.qa, q, sizeof(double) * 5 * h->N, cudaMemcpyHostToDevice, h->st));
+  return ATI_OK;
+}
+extern "C" int ati_get_state_all(ati_handle_t *h, double *q) {
+  if (!h || !q) return fail(h, ATI_EINVAL, "ati_get_state_all: bad argument");
+  CK(cudaMemcpyAsync(q, h->ed.qa, sizeof(double) * 5 * h->N, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return ATI_OK;
+}
+extern "C" int ati_points_total(ati_handle_t *h, int64_t *n) {
+  if (!h || !n) return fail(h, ATI_EINVAL, "ati_points_total: bad argument");
+  *n = h->N;
+  return ATI_OK;
+}
+
 extern "C" int ati_get_face(ati_handle_t *h, int blk, int which, int nn, double *v) {
   if (!h || blk < 0 || blk >= h->nb || nn < 1 || nn > 3 || !v) return fail(h, ATI_EINVAL, "ati_get_face: bad argument");
   const BlockDev &B = h->blk[blk];

@@ -42,6 +42,9 @@ SIGNATURES = {
     "ati_init": ([_vp], ctypes.c_int),
     "ati_set_state": ([_vp, _i32, _dp], ctypes.c_int),
     "ati_get_state": ([_vp, _i32, _dp], ctypes.c_int),
+    "ati_set_state_all": ([_vp, _dp], ctypes.c_int),
+    "ati_get_state_all": ([_vp, _dp], ctypes.c_int),
+    "ati_points_total": ([_vp, _vp], ctypes.c_int),
     "ati_set_field": ([_vp, _i32, _i32, _dp], ctypes.c_int),
     "ati_get_field": ([_vp, _i32, _i32, _dp], ctypes.c_int),
     "ati_get_face": ([_vp, _i32, _i32, _i32, _dp], ctypes.c_int),
@@ -192,6 +195,24 @@ class Case:
     def set_state(self, mb, q):
         a = np.ascontiguousarray(q, dtype=np.float64)
         self._chk(self.L.ati_set_state(self.h, mb, _dp_of(a)))
+
+    def points_total(self):
+        n = ctypes.c_int64()
+        self._chk(self.L.ati_points_total(self.h, ctypes.byref(n)))
+        return n.value
+
+    def get_state_all(self, out=None):
+        """The state of every block, [5][points_total] with blocks in handle order, in one copy."""
+        if out is None:
+            out = np.empty(5 * self.points_total())
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == 5 * self.points_total()
+        self._chk(self.L.ati_get_state_all(self.h, _dp_of(out)))
+        return out.reshape(5, -1)
+
+    def set_state_all(self, q):
+        a = np.ascontiguousarray(q, dtype=np.float64)
+        assert a.size == 5 * self.points_total()
+        self._chk(self.L.ati_set_state_all(self.h, _dp_of(a)))
 
     def get_face(self, mb, which, nn):
         lxi, let, lze, _ = self.dims[mb]

@@ -114,3 +114,21 @@ def test_plot3d_grid_and_solution(case, tmp_path):
         for m in range(1, 4):
             np.testing.assert_array_equal(data[m], (q[m] / q[0] + umf[m - 1]).astype(np.float32))
         np.testing.assert_array_equal(data[4], case.get_field(mb, F_P)[0].astype(np.float32))
+
+
+def test_whole_state_copies_match_the_block_copies(case):
+    """ati_get/set_state_all: one [5][points_total] array, blocks in handle order."""
+    n = case.points_total()
+    assert n == sum(case.npts(mb) for mb in range(case.cfg.nblocks))
+    q = case.get_state_all()
+    assert q.shape == (5, n)
+    off = 0
+    for mb in range(case.cfg.nblocks):
+        np.testing.assert_array_equal(q[:, off:off + case.npts(mb)], case.get_state(mb))
+        off += case.npts(mb)
+    q2 = q.copy()
+    q2[0] *= 1.0 + 1e-9
+    case.set_state_all(q2)
+    np.testing.assert_array_equal(case.get_state(2), q2[:, sum(case.npts(mb) for mb in range(2)):][:, :case.npts(2)])
+    case.set_state_all(q)
+    np.testing.assert_array_equal(case.get_state_all(), q)
