@@ -776,7 +776,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     o_fsbcc = take(std::max<int64_t>(h->nsbcc, 1) * F4); o_frpex = take(std::max<int64_t>(h->nwall, 1) * F4);
     o_cff = take(sizeof(Coef<float>));
     for (int nn = 1; nn <= 3; nn++) o_lts[nn] = take(sizeof(LTile) * std::max<size_t>(h->hlts[nn].size(), 1));
-    o_segd = take((size_t)h->nfac * SEG_RT * F4); o_segf = take((size_t)h->nfac * SEG_RT * F4);
+    // (SEG_PAD rows of padding before and after: the kernel reads a few rows ahead of its segment)
+    o_segd = take((size_t)(h->nfac + 2 * SEG_PAD) * SEG_RT * F4);
+    o_segf = take((size_t)(h->nfac + 2 * SEG_PAD) * SEG_RT * F4);
   }
   cudaError_t e = cudaMalloc(&h->arena, bytes);
   if (e != cudaSuccess) {
@@ -835,7 +837,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
       m.lts[nn] = (const LTile *)(h->arena + o_lts[nn]);
       m.nlts[nn] = (int)h->hlts[nn].size();
     }
-    m.segd = Fp(o_segd); m.segf = Fp(o_segf);
+    m.segd = Fp(o_segd) + SEG_PAD * SEG_RT; m.segf = Fp(o_segf) + SEG_PAD * SEG_RT;
   }
   // junctions (src/SingleTurbulence3D.f90:386-398), bkx = 3, bky = 2, per case
   std::vector<JunctionDev> jn;

@@ -809,18 +809,20 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
       // the arithmetic itself (the loads of a pass come before its stores)
       float *pc = col + i * RS;
       const float *tr = row(i);
+      auto l2 = [](const float *t) { return __ldg(reinterpret_cast<const float2 *>(t)); };
+      // each pass loads the next pass's factors first (rows past the block read the table's padding)
+      float2 m0 = l2(tr), m1 = l2(tr + SEG_RT), m2 = l2(tr + 2 * SEG_RT), m3 = l2(tr + 3 * SEG_RT);
       for (; i + 3 < iown; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
         const float b0 = pc[3 * RS], b1 = pc[4 * RS], b2 = pc[5 * RS], b3 = pc[6 * RS];
-        const float2 m0 = __ldg(reinterpret_cast<const float2 *>(tr));
-        const float2 m1 = __ldg(reinterpret_cast<const float2 *>(tr + SEG_RT));
-        const float2 m2 = __ldg(reinterpret_cast<const float2 *>(tr + 2 * SEG_RT));
-        const float2 m3 = __ldg(reinterpret_cast<const float2 *>(tr + 3 * SEG_RT));
+        const float2 n0 = l2(tr + 4 * SEG_RT), n1 = l2(tr + 5 * SEG_RT), n2 = l2(tr + 6 * SEG_RT);
+        const float2 n3 = l2(tr + 7 * SEG_RT);
         float p;
         p = rhs(a0, a1, a2, a3, a4, a5, b0) - m0.x * pm2 - m0.y * pm1; pc[0] = p; pm2 = pm1; pm1 = p;
         p = rhs(a1, a2, a3, a4, a5, b0, b1) - m1.x * pm2 - m1.y * pm1; pc[RS] = p; pm2 = pm1; pm1 = p;
         p = rhs(a2, a3, a4, a5, b0, b1, b2) - m2.x * pm2 - m2.y * pm1; pc[2 * RS] = p; pm2 = pm1; pm1 = p;
         p = rhs(a3, a4, a5, b0, b1, b2, b3) - m3.x * pm2 - m3.y * pm1; pc[3 * RS] = p; pm2 = pm1; pm1 = p;
         a0 = a4; a1 = a5; a2 = b0; a3 = b1; a4 = b2; a5 = b3;
+        m0 = n0; m1 = n1; m2 = n2; m3 = n3;
       }
     }
     for (; i < iown; i++) {
@@ -875,10 +877,10 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
     const TI *pi = in + o;
     auto sweep = [&](auto direct) {
       constexpr bool D = decltype(direct)::value;
-      // one row: t = (g, h, c2, masked c3) and the masked c4 of the row
-      auto bwd = [&](float *c, const float *t) {
-        const float4 g = __ldg(reinterpret_cast<const float4 *>(t + 4));
-        const float c4 = __ldg(t + 10);
+      // one row: g = (g, h, c2, masked c3) and the masked c4 of the row, loaded a pass ahead
+      auto l4 = [](const float *t) { return __ldg(reinterpret_cast<const float4 *>(t + 4)); };
+      auto l1 = [](const float *t) { return __ldg(t + 10); };
+      auto bwd = [&](float *c, const float4 g, const float c4) {
         const float v = *c + g.x * x.x + g.y * x.y;
         const float q = g.z * v - g.w * q1 - c4 * q2;
         if constexpr (D) {
@@ -894,13 +896,22 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
         }
         q2 = q1; q1 = q;
       };
+      float4 g0 = l4(tr), g1 = l4(tr - SEG_RT), g2 = l4(tr - 2 * SEG_RT), g3 = l4(tr - 3 * SEG_RT);
+      float k0 = l1(tr), k1 = l1(tr - SEG_RT), k2 = l1(tr - 2 * SEG_RT), k3 = l1(tr - 3 * SEG_RT);
       for (; i - 3 >= s0; i -= 4, pc -= 4 * RS, tr -= 4 * SEG_RT) {
-        bwd(pc, tr);
-        bwd(pc - RS, tr - SEG_RT);
-        bwd(pc - 2 * RS, tr - 2 * SEG_RT);
-        bwd(pc - 3 * RS, tr - 3 * SEG_RT);
+        // the next pass's rows (rows before the block read the table's padding)
+        const float4 h0 = l4(tr - 4 * SEG_RT), h1 = l4(tr - 5 * SEG_RT), h2 = l4(tr - 6 * SEG_RT);
+        const float4 h3 = l4(tr - 7 * SEG_RT);
+        const float j0 = l1(tr - 4 * SEG_RT), j1 = l1(tr - 5 * SEG_RT), j2 = l1(tr - 6 * SEG_RT);
+        const float j3 = l1(tr - 7 * SEG_RT);
+        bwd(pc, g0, k0);
+        bwd(pc - RS, g1, k1);
+        bwd(pc - 2 * RS, g2, k2);
+        bwd(pc - 3 * RS, g3, k3);
+        g0 = h0; g1 = h1; g2 = h2; g3 = h3;
+        k0 = j0; k1 = j1; k2 = j2; k3 = j3;
       }
-      for (; i >= s0; i--, pc -= RS, tr -= SEG_RT) bwd(pc, tr);
+      for (; i >= s0; i--, pc -= RS, tr -= SEG_RT) bwd(pc, l4(tr), l1(tr));
     };
     if (!multi && NN != 1) {
       sweep(std::true_type{});
@@ -940,6 +951,8 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
         const float2 g = __ldg(reinterpret_cast<const float2 *>(t));
         return *c + g.x * y.x + g.y * y.y;
       };
+      auto fg = [&](const float *c, const float2 g) { return *c + g.x * y.x + g.y * y.y; };
+      auto l2 = [](const float *t) { return __ldg(reinterpret_cast<const float2 *>(t)); };
       if (drv) {
         if (w == 0) drv[jk + nbs * ((m - 1) + 5 * 0)] = fv(col, row(0) + 8);  // drva(jk,m,0) = sb(is)
         if (w == S - 1) drv[jk + nbs * ((m - 1) + 5 * 1)] = fv(col + (L - 1) * RS, row(L - 1) + 8);
@@ -947,11 +960,14 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
       int i = s0;
       float *pc = col + i * RS;
       const float *tr = row(i) + 8;
+      float2 e0 = l2(tr), e1 = l2(tr + SEG_RT), e2 = l2(tr + 2 * SEG_RT), e3 = l2(tr + 3 * SEG_RT);
       if constexpr (NN == 1) {
         for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
-          const float r0 = fv(pc, tr), r1 = fv(pc + RS, tr + SEG_RT);
-          const float r2 = fv(pc + 2 * RS, tr + 2 * SEG_RT), r3 = fv(pc + 3 * RS, tr + 3 * SEG_RT);
+          const float2 f0 = l2(tr + 4 * SEG_RT), f1 = l2(tr + 5 * SEG_RT), f2 = l2(tr + 6 * SEG_RT);
+          const float2 f3 = l2(tr + 7 * SEG_RT);
+          const float r0 = fg(pc, e0), r1 = fg(pc + RS, e1), r2 = fg(pc + 2 * RS, e2), r3 = fg(pc + 3 * RS, e3);
           pc[0] = r0; pc[RS] = r1; pc[2 * RS] = r2; pc[3 * RS] = r3;
+          e0 = f0; e1 = f1; e2 = f2; e3 = f3;
         }
         for (; i < s1; i++, pc += RS, tr += SEG_RT) *pc = fv(pc, tr);
       } else {
@@ -970,9 +986,11 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
           if (FILT) pi += stride;
         };
         for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
-          const float r0 = fv(pc, tr), r1 = fv(pc + RS, tr + SEG_RT);
-          const float r2 = fv(pc + 2 * RS, tr + 2 * SEG_RT), r3 = fv(pc + 3 * RS, tr + 3 * SEG_RT);
+          const float2 f0 = l2(tr + 4 * SEG_RT), f1 = l2(tr + 5 * SEG_RT), f2 = l2(tr + 6 * SEG_RT);
+          const float2 f3 = l2(tr + 7 * SEG_RT);
+          const float r0 = fg(pc, e0), r1 = fg(pc + RS, e1), r2 = fg(pc + 2 * RS, e2), r3 = fg(pc + 3 * RS, e3);
           put(r0); put(r1); put(r2); put(r3);
+          e0 = f0; e1 = f1; e2 = f2; e3 = f3;
         }
         for (; i < s1; i++, pc += RS, tr += SEG_RT) put(fv(pc, tr));
       }

@@ -131,6 +131,8 @@ __host__ __device__ inline int seg_count(int L) {
 //   [8] G, [9] H     the row's back-substituted values from b(s1) = 1, b(s1+1) = 1
 //   [10] c4          (zero on the last two rows); [2], [3], [11] unused
 constexpr int SEG_RT = 12;
+// rows of zero padding on each side of a row table (reads ahead of a segment stay in the allocation)
+constexpr int SEG_PAD = 8;
 // Scaled-factor row table of the FP64 fast path's line solves, FU_RT doubles
 // per LU-factor row.  The forward values are carried as u(i) = c2(i) v(i), so
 // the back substitution needs no multiply by c2:
