@@ -999,16 +999,27 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   if constexpr (NN == 1) {
     __syncthreads();
     const int64_t o0 = B.off + (int64_t)LT.t0 * L;
-    for (int ln = w; ln < nl; ln += nwarp)
-      for (int i = lane; i < L; i += 32) {
-        const int64_t p = o0 + (int64_t)ln * L + i;
-        const float v = tile[i * RS + ln];
-        TO r;
-        if (FILT) r = (TO)(in[p] + cvt<TI>(v));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
-        else r = (TO)v;
-        out[p] = r;
-        if (out2) out2[p] = r;
+    auto wr = [&](int64_t p, float v, TI qin) {
+      TO r;
+      if (FILT) r = (TO)(qin + cvt<TI>(v));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
+      else r = (TO)v;
+      out[p] = r;
+      if (out2) out2[p] = r;
+    };
+    for (int ln = w; ln < nl; ln += nwarp) {
+      const int64_t lb = o0 + (int64_t)ln * L;
+      int i = lane;
+      // four points a pass, their inputs read before any of them is stored (the filter runs in place)
+      for (; i + 96 < L; i += 128) {
+        TI q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+        if (FILT) { q0 = in[lb + i]; q1 = in[lb + i + 32]; q2 = in[lb + i + 64]; q3 = in[lb + i + 96]; }
+        wr(lb + i, tile[i * RS + ln], q0);
+        wr(lb + i + 32, tile[(i + 32) * RS + ln], q1);
+        wr(lb + i + 64, tile[(i + 64) * RS + ln], q2);
+        wr(lb + i + 96, tile[(i + 96) * RS + ln], q3);
       }
+      for (; i < L; i += 32) wr(lb + i, tile[i * RS + ln], FILT ? in[lb + i] : (TI)0);
+    }
   }
 }
 
