@@ -672,16 +672,28 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
     }
     __syncthreads();
     const int sw = c0 == 0 ? 3 : 0;
-    if (lane < cl && lane >= sw)
-      for (int ln = warp; ln < nl; ln += NW) {
+    if (lane < cl && lane >= sw) {
+      auto wr = [&](int ln, TI qin) {
         const int64_t p = (int64_t)ln * L + c0 + lane - 3;
         const TC v = tile[bf][lane][ln];
         TO r;
-        if (FILT) r = (TO)(in[p] + cvt<TI>(v));
+        if (FILT) r = (TO)(qin + cvt<TI>(v));
         else r = (TO)v;
         out[p] = r;
         if (out2) out2[p] = r;
+      };
+      auto qin = [&](int ln) -> TI { return FILT ? in[(int64_t)ln * L + c0 + lane - 3] : (TI)0; };
+      int ln = warp;
+      // four lines a pass, their inputs read before any of them is stored (the filter runs in place)
+      for (; ln + 3 * NW < nl; ln += 4 * NW) {
+        const TI q0 = qin(ln), q1 = qin(ln + NW), q2 = qin(ln + 2 * NW), q3 = qin(ln + 3 * NW);
+        wr(ln, q0);
+        wr(ln + NW, q1);
+        wr(ln + 2 * NW, q2);
+        wr(ln + 3 * NW, q3);
       }
+      for (; ln < nl; ln += NW) wr(ln, qin(ln));
+    }
   }
   if (act && !FILT && a.io.drva) {
     TC *d = a.drva + B.face_off[1] * 10;
