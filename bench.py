@@ -439,6 +439,8 @@ def main():
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
                          "peak_source": "measured FP64 FMA throughput of this GPU (ati_probe_fma_tflops)"},
+                "limit": "the FP64 pipe (ncu: 89-92 % busy in the line sweeps and k_flux at 12-34 % of HBM); "
+                         "frac is against HBM, fp64.frac against the FP64 FMA peak",
                 "stage_hbm_frac": STAGE_BYTES_FP64 * value / ws / 1e9 / hbm_peak,
                 "kernel_share": {k: round(v[0] / tot, 4) for k, v in prof.items() if v[1]}}
 
