@@ -1961,7 +1961,7 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   if constexpr (std::is_same<TC, float>::value) {
     // the mixed path: segmented solves over tiles of SEG_LINES lines
     const float *seg = filt ? e.segf : e.segd;
-    if (seg && e.nlts[nn] > 0) {
+    if (seg && e.nlts[nn] > 0 && (filt || !io.out2)) {  // (a derivative with a second output: sequential kernels)
       a.lt = e.lts[nn];
       const int nt = SEG_LINES * seg_count(e.maxlen[nn]);
       const size_t smem = seg_smem_bytes(e.maxlen[nn]);

@@ -7,7 +7,7 @@
 // when memory is fragmented).  ati_deriv_lines_noalloc serves them: the
 // caller passes its own input and output arrays, and the only extra memory
 // the kernel needs -- the LU factor table and the forward-elimination values
-// -- lives in the file-scope device array below, which the driver reserves
+// -- lives in the file-scope device array below, which the CUDA driver reserves
 // when the library is loaded (about 16 MB on every GPU that loads it, held
 // until the process exits).  No call allocates or frees anything.
 //
