@@ -1326,8 +1326,10 @@ __device__ __forceinline__ void flux_fast_point(const Eng<double> &e, int64_t N,
 
 // contravariant velocities and the fifteen flux components
 // (src/Main3D.f90:710-766): flx plane (m-1)*3 + (nn-1)
+// (the FP32 kernel streams: five CTAs of 256 threads an SM, at most 51 registers a thread, keep more loads
+// in flight than the 80 registers it would take unbounded; measured 380 -> 296 us a launch on 8.85 M points)
 template <typename R>
-__global__ void k_flux(Eng<R> e) {
+__global__ void __launch_bounds__(256, Freestream<R>::on ? 5 : 1) k_flux(Eng<R> e) {
   const int64_t N = e.N;
   TILE_LOOP(e, T) {
     const Scheme &S = e.sc[T.cs];
