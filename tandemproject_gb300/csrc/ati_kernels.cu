@@ -1421,8 +1421,8 @@ __global__ void __launch_bounds__(256, Freestream<R>::on ? 5 : 1) k_flux(Eng<R> 
 // divergence de(:,m) = rr1+rr2+rr3 (src/Main3D.f90:722...) plus the sponge of
 // spongego (src/SingleTurbulence3D.f90:368-372) on sponge points
 template <typename R>
-// (the FP32 kernel streams: eight CTAs of 256 threads an SM, at most 32 registers a thread)
-__global__ void __launch_bounds__(256, Freestream<R>::on ? 8 : 5) k_div(Eng<R> e) {
+// (the kernel streams: eight CTAs of 256 threads an SM, at most 32 registers a thread)
+__global__ void __launch_bounds__(256, 8) k_div(Eng<R> e) {
   const int64_t N = e.N;
   TILE_LOOP(e, T) {
     const Scheme &S = e.sc[T.cs];
