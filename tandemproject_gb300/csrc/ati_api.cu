@@ -583,8 +583,9 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
   make_tiles(h, SG_DEFAULT, SG_DEFAULT, PT_DEFAULT);
   for (int nn = 1; nn <= 3; nn++) {
     h->hlts[nn].clear();
+    const int step = SEG_LINES * seg_groups(h->maxlen[nn]);
     for (int gb = 0; gb < h->nb; gb++)
-      for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += SEG_LINES) h->hlts[nn].push_back(LTile{gb, t0});
+      for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += step) h->hlts[nn].push_back(LTile{gb, t0});
     if (h->mixed && h->maxlen[nn] > SEG_LMAX)
       return fail(h, ATI_EINVAL, "mixed precision: lines of up to " + std::to_string(SEG_LMAX) + " points");
   }
@@ -836,6 +837,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     for (int nn = 1; nn <= 3; nn++) {
       m.lts[nn] = (const LTile *)(h->arena + o_lts[nn]);
       m.nlts[nn] = (int)h->hlts[nn].size();
+      m.seg_groups[nn] = seg_groups(h->maxlen[nn]);
     }
     m.segd = Fp(o_segd) + SEG_PAD * SEG_RT; m.segf = Fp(o_segf) + SEG_PAD * SEG_RT;
   }

@@ -719,23 +719,28 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
 // sequential solve by rounding only, and depend on the line length alone.
 // ---------------------------------------------------------------------------
 template <int NN, bool FILT, typename TI, typename TO>
-__global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, TO, float> a, const float *rtab) {
+__global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, TO, float> a, const float *rtab,
+                                                                  int groups) {
   extern __shared__ __align__(16) unsigned char seg_smem[];
   constexpr int RS = SEG_LINES + 1;  // tile row stride in words: a warp's column reads and row reads are conflict-free
   constexpr bool ASYNC = std::is_same<TI, float>::value;
   const int nwarp = (int)(blockDim.x >> 5);
   float2 *cf = reinterpret_cast<float2 *>(seg_smem);  // [segment][line] values a segment passes on
   float2 *cx = cf + nwarp * SEG_LINES;                 // [segment][line] values a segment receives
-  float *tile = reinterpret_cast<float *>(cx + nwarp * SEG_LINES);
   const LTile LT = a.lt[blockIdx.x];
   const BlockDev &B = a.blk[LT.b];
   const int f = blockIdx.y;
   const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
-  const int nl = min(SEG_LINES, (int)B.nbsize[NN] - LT.t0);
   const int L = NN == 1 ? B.lxi + 1 : (NN == 2 ? B.let + 1 : B.lze + 1);
+  // groups > 1 (every line of the launch one segment long): warp w solves its own group of SEG_LINES lines with
+  // its own tile; otherwise the CTA is one group and warp w solves segment w of its lines
+  const int gsz = groups > 1 ? 1 : nwarp, grp = w / gsz, wl = w - grp * gsz;
+  const int t0 = LT.t0 + grp * SEG_LINES;
+  const int nl = min(SEG_LINES, (int)B.nbsize[NN] - t0);  // (no lines: the group idles)
+  float *tile = reinterpret_cast<float *>(cx + nwarp * SEG_LINES) + (int64_t)grp * L * (SEG_LINES + 1);
   int64_t base = 0, stride = 1;
   int jk = 0, Lg = 0;
-  line_geom<NN>(B, LT.t0 + lane, base, stride, jk, Lg);
+  line_geom<NN>(B, t0 + lane, base, stride, jk, Lg);
   const TI *in = a.io.in + f * a.io.in_fs;
   const TI ofs = a.io.ofs[f];
 
@@ -747,8 +752,8 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   };
   if constexpr (NN == 1) {
     // xi lines are contiguous: a warp copies one line at a time, lanes along the line
-    const TI *src0 = in + B.off + (int64_t)LT.t0 * L;
-    for (int ln = w; ln < nl; ln += nwarp) {
+    const TI *src0 = in + B.off + (int64_t)t0 * L;
+    for (int ln = wl; ln < nl; ln += gsz) {
       const TI *src = src0 + (int64_t)ln * L + lane;
       float *dst = tile + lane * RS + ln;
 #pragma unroll 4
@@ -757,11 +762,11 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   } else {
     // consecutive eta/zeta lines are consecutive points of a row: a warp copies one row at a time
     if (lane < nl) {
-      const TI *src = in + base + (int64_t)w * stride;
-      const int64_t step = (int64_t)nwarp * stride;
-      float *dst = tile + w * RS + lane;
+      const TI *src = in + base + (int64_t)wl * stride;
+      const int64_t step = (int64_t)gsz * stride;
+      float *dst = tile + wl * RS + lane;
 #pragma unroll 4
-      for (int i = w; i < L; i += nwarp, src += step, dst += nwarp * RS) stage(dst, src);
+      for (int i = wl; i < L; i += gsz, src += step, dst += gsz * RS) stage(dst, src);
     }
   }
   if constexpr (ASYNC) {
@@ -771,8 +776,8 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   __syncthreads();
 
   const int S = seg_count(L);
-  const bool act = w < S && lane < nl;
-  const int s0 = seg_start(w, L, S), s1 = seg_start(w + 1, L, S);
+  const bool act = wl < S && lane < nl;
+  const int s0 = seg_start(wl, L, S), s1 = seg_start(wl + 1, L, S);
   float *col = tile + lane;
   // the block's row table, SEG_RT floats per row (layout at SEG_RT)
   const float *rt = rtab + (int64_t)B.fac_off[NN] * SEG_RT;
@@ -792,7 +797,7 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   float a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, h0 = 0, h1 = 0, h2 = 0;
   if (act) {
     auto sld = [&](int i) { return col[i * RS]; };
-    if (w == 0 || w == S - 1) {
+    if (wl == 0 || wl == S - 1) {
       const float *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
       line_ends<FILT, float>(C, L, B.ndf[0][NN], B.ndf[1][NN], rcv, B.nbsize[NN], jk, sld, sbs0, sbs1, sbs2, sbe0,
                              sbe1, sbe2);
@@ -800,7 +805,7 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
     if (ilo < ihi) {
       a0 = sld(ilo - 3); a1 = sld(ilo - 2); a2 = sld(ilo - 1); a3 = sld(ilo); a4 = sld(ilo + 1); a5 = sld(ilo + 2);
     }
-    if (w < S - 1) { h0 = sld(s1); h1 = sld(s1 + 1); h2 = sld(s1 + 2); }
+    if (wl < S - 1) { h0 = sld(s1); h1 = sld(s1 + 1); h2 = sld(s1 + 2); }
   }
   __syncthreads();
 
@@ -966,8 +971,8 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
       auto fg = [&](const float *c, const float2 g) { return *c + g.x * y.x + g.y * y.y; };
       auto l2 = [](const float *t) { return __ldg(reinterpret_cast<const float2 *>(t)); };
       if (drv) {
-        if (w == 0) drv[jk + nbs * ((m - 1) + 5 * 0)] = fv(col, row(0) + 8);  // drva(jk,m,0) = sb(is)
-        if (w == S - 1) drv[jk + nbs * ((m - 1) + 5 * 1)] = fv(col + (L - 1) * RS, row(L - 1) + 8);
+        if (wl == 0) drv[jk + nbs * ((m - 1) + 5 * 0)] = fv(col, row(0) + 8);  // drva(jk,m,0) = sb(is)
+        if (wl == S - 1) drv[jk + nbs * ((m - 1) + 5 * 1)] = fv(col + (L - 1) * RS, row(L - 1) + 8);
       }
       int i = s0;
       float *pc = col + i * RS;
@@ -1010,7 +1015,7 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   }
   if constexpr (NN == 1) {
     __syncthreads();
-    const int64_t o0 = B.off + (int64_t)LT.t0 * L;
+    const int64_t o0 = B.off + (int64_t)t0 * L;
     auto wr = [&](int64_t p, float v, TI qin) {
       TO r;
       if (FILT) r = (TO)(qin + cvt<TI>(v));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
@@ -1018,7 +1023,7 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
       out[p] = r;
       if (out2) out2[p] = r;
     };
-    for (int ln = w; ln < nl; ln += nwarp) {
+    for (int ln = wl; ln < nl; ln += gsz) {
       const int64_t lb = o0 + (int64_t)ln * L;
       int i = lane;
       // four points a pass, their inputs read before any of them is stored (the filter runs in place)
@@ -1966,10 +1971,11 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
     const float *seg = filt ? e.segf : e.segd;
     if (seg && e.nlts[nn] > 0 && (filt || !io.out2)) {  // (a derivative with a second output: sequential kernels)
       a.lt = e.lts[nn];
-      const int nt = SEG_LINES * seg_count(e.maxlen[nn]);
-      const size_t smem = seg_smem_bytes(e.maxlen[nn]);
+      const int G = e.seg_groups[nn];
+      const int nt = SEG_LINES * (G > 1 ? G : seg_count(e.maxlen[nn]));
+      const size_t smem = seg_smem_bytes(e.maxlen[nn], G);
       const dim3 g(e.nlts[nn], io.nf);
-#define ATI_SEG(D, F) k_sweep_seg<D, F, TI, TO><<<g, nt, smem, st>>>(a, seg)
+#define ATI_SEG(D, F) k_sweep_seg<D, F, TI, TO><<<g, nt, smem, st>>>(a, seg, G)
       if (!filt) { if (nn == 1) ATI_SEG(1, false); else if (nn == 2) ATI_SEG(2, false); else ATI_SEG(3, false); }
       else { if (nn == 1) ATI_SEG(1, true); else if (nn == 2) ATI_SEG(2, true); else ATI_SEG(3, true); }
 #undef ATI_SEG

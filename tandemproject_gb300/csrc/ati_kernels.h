@@ -38,8 +38,9 @@ struct Eng {
   int npt;
   const LTile *lt[4];   // line-sweep work queue per direction nn = 1..3
   int nlt[4];
-  const LTile *lts[4];  // segmented sweeps (mixed path): SEG_LINES lines per tile, per direction
+  const LTile *lts[4];  // segmented sweeps (mixed path): SEG_LINES x seg_groups lines per tile, per direction
   int nlts[4];
+  int seg_groups[4];    // line groups per CTA of a segmented sweep (> 1 when every line is one segment)
   const float *segd, *segf;  // their row tables (SEG_RT floats per factor row; derivative, filter)
   const double *facud, *facuf;  // FP64 fast path: scaled-factor row tables (FU_RT per row; derivative, filter)
   int sg_lines[4];      // lines per CTA of the eta (2) and zeta (3) sweeps: the tiles of lt[2], lt[3]
@@ -150,9 +151,14 @@ __host__ __device__ inline int seg_start(int k, int L, int S) {
   const int q = L / S, r = L % S;
   return k * q + (k < r ? k : r);
 }
-// dynamic shared memory of a segmented sweep over lines of up to maxlen points
-inline size_t seg_smem_bytes(int maxlen) {
-  return (size_t)seg_count(maxlen) * SEG_LINES * 2 * 2 * sizeof(float) + (size_t)maxlen * (SEG_LINES + 1) * sizeof(float);
+// Lines of one segment leave a CTA of one warp; SEG_GROUPS groups of SEG_LINES lines then share a CTA (one
+// warp and one tile each), when every line of a direction is one segment long
+constexpr int SEG_GROUPS = 4;
+inline int seg_groups(int maxlen) { return seg_count(maxlen) == 1 ? SEG_GROUPS : 1; }
+// dynamic shared memory of a segmented sweep over lines of up to maxlen points, in groups line groups
+inline size_t seg_smem_bytes(int maxlen, int groups) {
+  const int nwarp = groups > 1 ? groups : seg_count(maxlen);
+  return (size_t)nwarp * SEG_LINES * 2 * 2 * sizeof(float) + (size_t)groups * maxlen * (SEG_LINES + 1) * sizeof(float);
 }
 
 // per-field offsets of a closure (mpigo) over a wider input type

@@ -184,3 +184,7 @@ def test_segment_rules(L):
     smem = S * SEG_LINES * 16 + L * (SEG_LINES + 1) * 4
     assert smem <= 227 * 1024
     assert S * SEG_LINES <= SEG_LINES * SEG_MAX
+    if S == 1:  # one-segment lines: SEG_GROUPS groups of lines share a CTA, each with its own tile
+        groups = int(re.search(r"constexpr int SEG_GROUPS = (\d+);", HDR.read_text()).group(1))
+        assert groups * SEG_LINES * 16 + groups * L * (SEG_LINES + 1) * 4 <= 227 * 1024
+        assert groups * SEG_LINES <= SEG_LINES * SEG_MAX
