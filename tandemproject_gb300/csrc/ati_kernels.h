@@ -153,7 +153,7 @@ __host__ __device__ inline int seg_start(int k, int L, int S) {
 }
 // Lines of one segment leave a CTA of one warp; SEG_GROUPS groups of SEG_LINES lines then share a CTA (one
 // warp and one tile each), when every line of a direction is one segment long
-constexpr int SEG_GROUPS = 4;
+constexpr int SEG_GROUPS = 2;
 inline int seg_groups(int maxlen) { return seg_count(maxlen) == 1 ? SEG_GROUPS : 1; }
 // dynamic shared memory of a segmented sweep over lines of up to maxlen points, in groups line groups
 inline size_t seg_smem_bytes(int maxlen, int groups) {
