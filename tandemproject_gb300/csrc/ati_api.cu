@@ -73,7 +73,7 @@ struct ati_handle {
   double *fw1 = nullptr;                // FP64 forward scratch of the granular calls
   FaceTask *dtasks = nullptr;
   std::vector<FaceTask> htasks;
-  TaskRange tl_mpigo, tl_gcbc, tl_gcbc_dir[4], tl_wall, tl_pack, tl_avg_dir[4], tl_force, tl_all;
+  TaskRange tl_mpigo, tl_mpigo_x, tl_gcbc, tl_gcbc_dir[4], tl_wall, tl_pack, tl_avg_dir[4], tl_force, tl_all;
   JunctionDev *djn = nullptr;
   int njct = 0, jnk = 0;
   double *area = nullptr, *wnor = nullptr, *dforce = nullptr, *dspg = nullptr;
@@ -536,6 +536,11 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
     r.n = (int)T.size() - r.off;
   };
   add(h->tl_mpigo, [](const BlockDev &B, int nn, int ip) { return B.ndf[ip][nn] == 1; });
+  // the mixed path's segmented derivative sweeps close faces periodic onto their own block themselves
+  add(h->tl_mpigo_x, [h](const BlockDev &B, int nn, int ip) {
+    const int gb = (int)(&B - h->blk.data());
+    return B.ndf[ip][nn] == 1 && !(B.nbc[ip][nn] == 45 && B.ncd[ip][nn] == gb);
+  });
   add(h->tl_gcbc, [](const BlockDev &B, int nn, int ip) { return is_gcbc(B.nbc[ip][nn]); });
   for (int d = 1; d <= 3; d++)
     add(h->tl_gcbc_dir[d], [d](const BlockDev &B, int nn, int ip) { return nn == d && is_gcbc(B.nbc[ip][nn]); });
@@ -1564,6 +1569,7 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
   cudaStream_t st = h->st;
   const int64_t N = h->N;
   const Eng<double> &ed = h->ed;
+  const TaskRange &mpt = Freestream<R>::on ? h->tl_mpigo_x : h->tl_mpigo;  // (segmented sweeps: see tl_mpigo_x)
   auto sc = [&](int op) {
     if (strict) strict::scalar(ed, st, op, nk);
     else fast::scalar(ed, st, op, nk);
@@ -1582,7 +1588,7 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
   }
   if (h->cfg.nviscous == 1) {
     // d(u,v,w,T)/d(zeta,eta,xi) (src/Main3D.f90:629-651): four fields per launch
-    PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, 0, e.prim,
+    PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, mpt), mpt.n, mpt.maxline, 0, e.prim,
                                   e.prim, e.prim, N, 4));
     three_directions(h, [&](int nn, cudaStream_t s) {
       SweepIO<R, R> io{e.prim, N, e.dv + (nn - 1) * N, 3 * N, nullptr, 4, 2, true};
@@ -1592,7 +1598,7 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
   }
   // fluxes and their derivatives (src/Main3D.f90:710-768): five fields per launch
   PROF(h, ATI_K_FLUX, C::pw(strict, e, st, PW_FLUX));
-  PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, h->tl_mpigo), h->tl_mpigo.n, h->tl_mpigo.maxline, 0, e.flx,
+  PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, mpt), mpt.n, mpt.maxline, 0, e.flx,
                                 e.flx + N, e.flx + 2 * N, 3 * N, 5));
   three_directions(h, [&](int nn, cudaStream_t s) {
     SweepIO<R, R> io{e.flx + (nn - 1) * N, 3 * N, e.flx + (nn - 1) * N, 3 * N, nullptr, 5, 1, true};

@@ -798,9 +798,31 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   if (act) {
     auto sld = [&](int i) { return col[i * RS]; };
     if (wl == 0 || wl == S - 1) {
+      // the closure values of the line ends (what mpigo leaves in recv).  In a derivative, a face periodic onto
+      // its own block (BC 45 with the block as neighbour) takes them from the other end of the same line, which
+      // is staged: the sums of k_mpigo (src/Subroutines3D.f90:16-80) in its operation order, skipping the shared
+      // point.  (The filter's closures come from the state before its first direction, src/Main3D.f90:555-561,
+      // so a filter sweep, which sees the state after the earlier directions, reads them from recv.)
       const float *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
-      line_ends<FILT, float>(C, L, B.ndf[0][NN], B.ndf[1][NN], rcv, B.nbsize[NN], jk, sld, sbs0, sbs1, sbs2, sbe0,
-                             sbe1, sbe2);
+      const int64_t nbs = B.nbsize[NN];
+      constexpr int nt = FILT ? 1 : 0, mp = FILT ? LMF : LMD;
+      auto closure = [&](int r0, int dir, float *o) {
+        float c0 = 0, c1 = 0, sap0 = 0;
+        for (int i = 0; i <= mp; i++) {
+          const float v = sld(r0 + i * dir);
+          if (i == 0) sap0 = v;
+          c0 += C.pbco[nt][0][i] * v;
+          c1 += C.pbco[nt][1][i] * v;
+        }
+        o[0] = c0; o[1] = c1; o[2] = sap0;
+      };
+      float rl[6];
+      for (int ip = 0; ip <= 1; ip++) {
+        if (B.ndf[ip][NN] != 1) continue;
+        if (!FILT && B.nbc[ip][NN] == 45 && B.ncd[ip][NN] == LT.b) closure(ip == 0 ? L - 2 : 1, ip == 0 ? -1 : 1, rl + 3 * ip);
+        else for (int q = 0; q < 3; q++) rl[3 * ip + q] = rcv[jk + nbs * (3 * ip + q)];
+      }
+      line_ends<FILT, float>(C, L, B.ndf[0][NN], B.ndf[1][NN], rl, 1, 0, sld, sbs0, sbs1, sbs2, sbe0, sbe1, sbe2);
     }
     if (ilo < ihi) {
       a0 = sld(ilo - 3); a1 = sld(ilo - 2); a2 = sld(ilo - 1); a3 = sld(ilo); a4 = sld(ilo + 1); a5 = sld(ilo + 2);
