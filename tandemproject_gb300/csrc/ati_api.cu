@@ -1690,10 +1690,25 @@ static int step_graph(ati_handle *h) {
     const int64_t l0 = h->launches;
     int rc = one_step(h);
     cudaError_t e = cudaStreamEndCapture(h->st, &g);
-    h->glaunches[v] = h->launches - l0;
     h->launches = l0;
     if (rc) return rc;
     if (e != cudaSuccess) return fail(h, ATI_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    // the kernels the graph holds (launch sites that had nothing to do launched nothing)
+    size_t nnode = 0;
+    e = cudaGraphGetNodes(g, nullptr, &nnode);
+    std::vector<cudaGraphNode_t> nodes(nnode);
+    if (e == cudaSuccess && nnode) e = cudaGraphGetNodes(g, nodes.data(), &nnode);
+    int64_t nk = 0;
+    for (size_t q = 0; q < nnode && e == cudaSuccess; q++) {
+      cudaGraphNodeType t;
+      e = cudaGraphNodeGetType(nodes[q], &t);
+      if (t == cudaGraphNodeTypeKernel) nk++;
+    }
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return fail(h, ATI_ECUDA, std::string("graph nodes: ") + cudaGetErrorString(e));
+    }
+    h->glaunches[v] = nk;
     e = cudaGraphInstantiate(&h->gexec[v], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, ATI_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
