@@ -1720,12 +1720,22 @@ __global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
     for (int q = 0; q < 5; q++) s += xt[r][q] * dif[q];
     dh[r] = s;
   }
+  // spread dq over the boundary point and the next MBCI points (the reads of all of them first: the stores
+  // of one point would otherwise hold back the reads of the next)
   const R *w = e.sbcc + T.sbcc_off + (int64_t)jk * (MBCI + 1);
+  int64_t g2[MBCI + 1];
+  R dv[MBCI + 1][5];
+#pragma unroll
   for (int ii = 0; ii <= MBCI; ii++) {
-    const int64_t g2 = B.off + idx3(B.lxi, B.let, i + iq * ii, j, k, nn);
+    g2[ii] = B.off + idx3(B.lxi, B.let, i + iq * ii, j, k, nn);
+#pragma unroll
+    for (int q = 0; q < 5; q++) dv[ii][q] = e.de[g2[ii] + q * N];
+  }
+#pragma unroll
+  for (int ii = 0; ii <= MBCI; ii++) {
     const R wv = w[ii];
 #pragma unroll
-    for (int q = 0; q < 5; q++) e.de[g2 + q * N] = e.de[g2 + q * N] + wv * dh[q];
+    for (int q = 0; q < 5; q++) e.de[g2[ii] + q * N] = dv[ii][q] + wv * dh[q];
   }
 }
 
