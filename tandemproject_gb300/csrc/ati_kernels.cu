@@ -1754,13 +1754,14 @@ __global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
   const double ra1 = (double)((T.bc - 20) / 5);
   const double rp = e.rpex[T.wall_off + jk];
   const double ra2 = 1.0 - rp, ra3 = 1.0 - ra1 * ra2;
-  const double fctr = (1.0 - ra3) * e.qa[g];
-  const double q2 = ra3 * e.qa[g + N] - fctr * SC.umf[1];
-  const double q3 = ra3 * e.qa[g + 2 * N] - fctr * SC.umf[2];
-  const double q4 = ra3 * e.qa[g + 3 * N] - fctr * SC.umf[3];
+  // the point's state read before any store (rho is not written here)
+  const double q1 = e.qa[g], m2 = e.qa[g + N], m3 = e.qa[g + 2 * N], m4 = e.qa[g + 3 * N], q5 = e.qa[g + 4 * N];
+  const double fctr = (1.0 - ra3) * q1;
+  const double q2 = ra3 * m2 - fctr * SC.umf[1];
+  const double q3 = ra3 * m3 - fctr * SC.umf[2];
+  const double q4 = ra3 * m4 - fctr * SC.umf[3];
   e.qa[g + N] = q2; e.qa[g + 2 * N] = q3; e.qa[g + 3 * N] = q4;
-  const double q1 = e.qa[g];
-  e.qa[g + 4 * N] = rp * e.qa[g + 4 * N] + ra2 * (ra0 * q1 + 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
+  e.qa[g + 4 * N] = rp * q5 + ra2 * (ra0 * q1 + 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
 }
 
 // junction averaging of the corner lines shared by four blocks
@@ -1799,8 +1800,11 @@ __global__ void k_pack(Eng<double> e, const FaceTask *tasks) {
   face_point(B, T.nn, T.ip, jk, i, j, k);
   const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = e.N, nbs = T.nline;
   double *drva = e.drva + B.face_off[T.nn] * 10;
+  double qv[5];
 #pragma unroll
-  for (int q = 0; q < 5; q++) drva[jk + nbs * (q + 5 * T.ip)] = e.qa[g + q * N];
+  for (int q = 0; q < 5; q++) qv[q] = e.qa[g + q * N];  // (the reads first, then the stores)
+#pragma unroll
+  for (int q = 0; q < 5; q++) drva[jk + nbs * (q + 5 * T.ip)] = qv[q];
   e.cnt[g] = 1.0;
 }
 
@@ -1816,15 +1820,21 @@ __global__ void k_avg(Eng<double> e, const FaceTask *tasks) {
   const int64_t g = B.off + idx3(B.lxi, B.let, i, j, k, T.nn), N = e.N, nbs = T.nline;
   const double *nbr = e.drva + Bn.face_off[T.nn] * 10;
   double *drvb = e.drvb + B.face_off[T.nn] * 10;
+  // every read first (the neighbour's packed face, the point's state and count), then the stores
+  double dv[5], qv[5];
+#pragma unroll
+  for (int q = 0; q < 5; q++) {
+    dv[q] = nbr[jk + nbs * (q + 5 * (1 - T.ip))];
+    qv[q] = e.qa[g + q * N];
+  }
   const double cnt = e.cnt[g] + 1.0;
   e.cnt[g] = cnt;
   const double w = 1.0 / cnt;
   e.cnt[g + N] = w;
 #pragma unroll
   for (int q = 0; q < 5; q++) {
-    const double dv = nbr[jk + nbs * (q + 5 * (1 - T.ip))];
-    drvb[jk + nbs * (q + 5 * T.ip)] = dv;
-    e.qa[g + q * N] = w * ((cnt - 1.0) * e.qa[g + q * N] + dv);
+    drvb[jk + nbs * (q + 5 * T.ip)] = dv[q];
+    e.qa[g + q * N] = w * ((cnt - 1.0) * qv[q] + dv[q]);
   }
 }
 
