@@ -1512,8 +1512,12 @@ __global__ void k_rk(Eng<R> e) {
     const double dtk = SC.dtk;
     POINT_LOOP(T, g) {
       const double r1 = dtk * e.yacod[g];
+      double qo[5];
+      R de[5];
 #pragma unroll
-      for (int q = 0; q < 5; q++) e.qa[g + q * N] = e.qo[g + q * N] - r1 * cvt<double>(e.de[g + q * N]);
+      for (int q = 0; q < 5; q++) { qo[q] = e.qo[g + q * N]; de[q] = e.de[g + q * N]; }  // reads before the stores
+#pragma unroll
+      for (int q = 0; q < 5; q++) e.qa[g + q * N] = qo[q] - r1 * cvt<double>(de[q]);
     }
   }
 }
