@@ -1,6 +1,7 @@
-// ati_convert.cu — device check of the integer-pipe FP32 -> FP64 conversion
-// against the conversion instruction, over bit patterns that cover every
-// exponent (normal, subnormal, zero, infinity, NaN).
+// ati_convert.cu — device check of the integer-pipe conversions (FP32 -> FP64
+// widening, FP64 -> FP32 rounding) against the conversion instruction, over bit
+// patterns that cover every exponent (normal, subnormal, zero, infinity, NaN) and
+// the rounding ties.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -30,6 +31,23 @@ __global__ void k_check_conv(int64_t n, unsigned long long *bad) {
     const float f = __uint_as_float(fb);
     const double wa = ati::widen(f), wb = (double)f;
     if (!((wa != wa && wb != wb) || __double_as_longlong(wa) == __double_as_longlong(wb))) nb++;
+    // narrowing: random doubles over the whole exponent range, exact ties and near-ties of the dropped 29 bits,
+    // the edges of the normal float range, zeros, infinities and NaNs
+    const uint64_t r2 = mix64(r ^ 0xD1B54A32D192ED03ull);
+    uint64_t db = r2;
+    switch (i & 7) {
+      case 1: db = (db & ~0x1fffffffull) | 0x10000000ull; break;                  // exact tie
+      case 2: db = (db & ~0x1fffffffull) | (0x10000000ull + ((r >> 3) & 1 ? 1 : -1)); break;  // near tie
+      case 3: db = (db & 0x800fffffffffffffull) | ((uint64_t)(896 + (r & 3)) << 52); break;    // below / at min normal
+      case 4: db = (db & 0x800fffffffffffffull) | ((uint64_t)(1149 + (r & 3)) << 52); break;   // near max / overflow
+      case 5: db = (db & 0x800fffffffffffffull) | ((uint64_t)(1023 + (int)(r % 41) - 20) << 52); break;  // O(1)
+      case 6: db = (r & 1) ? (db & 0x8000000000000000ull) : ((db & 0x800fffffffffffffull) | 0x7ff0000000000000ull);
+              break;                                                                  // zeros, inf, NaN
+      default: break;
+    }
+    const double d = __longlong_as_double((long long)db);
+    const float na = ati::narrow(d), nb2 = (float)d;
+    if (!((na != na && nb2 != nb2) || __float_as_uint(na) == __float_as_uint(nb2))) nb++;
   }
   if (nb) atomicAdd(bad, nb);
 }

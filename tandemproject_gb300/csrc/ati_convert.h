@@ -24,10 +24,29 @@ __device__ __forceinline__ double widen(float f) {
   return (double)f;  // subnormal, infinity, NaN
 }
 
+// double -> float, rounded to nearest even, for results in the normal float range:
+// the significand's top 23 bits plus a rounding increment decided by the 29 bits
+// dropped (above half, or exactly half with an odd result); a carry out of the
+// significand moves into the exponent, as the rounding requires (up to infinity).
+// Zero, results below the normal range, overflow, infinities and NaNs fall back
+// to the instruction.  Bit for bit the instruction's result (checked on the device
+// by ati_check_conversions).
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u < 254u) {  // float exponent e - 896 in 1..254
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29), r = lo & 0x1fffffffu;
+    const unsigned f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+    return __uint_as_float(f + (unsigned)((r > 0x10000000u) | ((r == 0x10000000u) & (m & 1u))));
+  }
+  return (float)d;
+}
+
 // conversion between the engine types: FP32 -> FP64 on the integer pipes.  The
-// other direction stays with the conversion instruction: rounding takes some
+// other direction stays with the conversion instruction here: rounding takes some
 // 15 integer operations and branches, slower in the line sweeps' load loops than
-// the FP64 pipe it would spare (measured on the mixed filter sweeps)
+// the FP64 pipe it would spare (measured on the mixed filter sweeps); kernels
+// bound by the FP64 pipe call narrow() themselves
 template <typename TO, typename TI>
 __device__ __forceinline__ TO cvt(TI v) {
   if constexpr (std::is_same<TO, TI>::value) return v;

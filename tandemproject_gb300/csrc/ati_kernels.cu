@@ -1142,13 +1142,19 @@ __global__ void k_prim(Eng<R> e) {
     const R gamm1 = (R)S.gamm1, gam = (R)S.gam, srefp1dre = (R)S.srefp1dre, srefoo = (R)S.srefoo;
     int bad = 0;
     const double rhoE_inf = S.hamm1 * S.poo;
+    // (the mixed kernel is bound by the FP64 pipe, which also runs the conversion instruction: the state is
+    // rounded to FP32 on the integer pipes instead, bit for bit the same)
+    auto rnd = [](double v) -> R {
+      if constexpr (Freestream<R>::on) return narrow(v);
+      else return (R)v;
+    };
     POINT_LOOP(T, g) {
-      const R q1 = cvt<R>(e.qa[g]), q2 = cvt<R>(e.qa[g + N]), q3 = cvt<R>(e.qa[g + 2 * N]), q4 = cvt<R>(e.qa[g + 3 * N]);
+      const R q1 = rnd(e.qa[g]), q2 = rnd(e.qa[g + N]), q3 = rnd(e.qa[g + 2 * N]), q4 = rnd(e.qa[g + 3 * N]);
       const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
       R pp, d5;
       if constexpr (Freestream<R>::on) {
         // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
-        const R re = cvt<R>(e.qa[g + 4 * N] - rhoE_inf);
+        const R re = rnd(e.qa[g + 4 * N] - rhoE_inf);
         pp = gamm1 * (re - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
         d5 = gam * ((R)S.poo + pp) * d1;
       } else {
