@@ -45,8 +45,9 @@ __device__ __forceinline__ float narrow(double d) {
 // conversion between the engine types: FP32 -> FP64 on the integer pipes.  The
 // other direction stays with the conversion instruction here: rounding takes some
 // 15 integer operations and branches, slower in the line sweeps' load loops than
-// the FP64 pipe it would spare (measured on the mixed filter sweeps); kernels
-// bound by the FP64 pipe call narrow() themselves
+// the FP64 pipe it would spare (measured on the mixed filter sweeps), and in the
+// register-bounded flux kernel (297 -> 346 us); the primitives kernel, bound by
+// the FP64 pipe, calls narrow() itself (142 -> 133 us)
 template <typename TO, typename TI>
 __device__ __forceinline__ TO cvt(TI v) {
   if constexpr (std::is_same<TO, TI>::value) return v;
