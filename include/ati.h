@@ -277,14 +277,16 @@ int ati_profile_enable(ati_handle_t *h, int enable);
 int ati_profile_read(ati_handle_t *h, int nslots, double *ms, int64_t *launches);
 int ati_launch_count(ati_handle_t *h, int64_t *count);
 /* Work-queue tile shapes in use: out[0] xi lines per CTA, out[1] eta and
- * out[2] zeta lines per CTA, out[3] points per pointwise tile.  ati_init picks
- * out[1..3] by timing candidates on the handle's own grid (results do not
- * depend on them: every line and point is computed the same way). */
+ * out[2] zeta lines per CTA, out[3] points per tile of the flux kernel.
+ * ati_init picks out[1..2] and, per pointwise kernel, the points per tile by
+ * timing candidates on the handle's own grid (results do not depend on them:
+ * every line and point is computed the same way). */
 int ati_tiles(ati_handle_t *h, int32_t out[4]);
-/* Pins the tile shapes (same meaning as ati_tiles; 0 keeps the current value):
- * in[0] must be 0 or the fixed xi tile, in[1] and in[2] multiples of 32 in
- * [32, 256], in[3] a multiple of 256 in [256, 4096].  Waits for the steps in
- * flight and re-captures the step graphs at the next step. */
+/* Pins the tile shapes (same meaning as ati_tiles; 0 keeps the current value;
+ * in[3] then applies to every pointwise kernel): in[0] must be 0 or the fixed
+ * xi tile, in[1] and in[2] multiples of 32 in [32, 256], in[3] a multiple of
+ * 256 in [256, 4096].  Waits for the steps in flight and re-captures the step
+ * graphs at the next step. */
 int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events against the solver's. */

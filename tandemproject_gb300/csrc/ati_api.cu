@@ -57,6 +57,11 @@ struct ati_handle {
   std::vector<LTile> hlt[4];
   std::vector<LTile> hlts[4];  // tiles of the segmented sweeps (mixed path), SEG_LINES lines each
   size_t max_pt = 0, max_lt[4] = {0, 0, 0, 0};
+  // point tiles of the candidate sizes (PT_CAND), uploaded once; pw_pt[kind] is a pointwise kernel's own timed
+  // size (0: the shared queue of pt_points)
+  std::vector<PTile> hptc[3];
+  const PTile *dptc[3] = {nullptr, nullptr, nullptr};
+  int pw_pt[PW_KINDS] = {};
   int sg_lines[4] = {XC_NL, XC_NL, SG_DEFAULT, SG_DEFAULT}, pt_points = PT_DEFAULT;  // tile shapes (timed at ati_init)
   int64_t N = 0, F = 0, nfac = 0, nsbcc = 0, nwall = 0;
   int maxlen[4] = {0, 0, 0, 0};
@@ -417,17 +422,37 @@ extern "C" int ati_abi_version(void) { return ATI_ABI_VERSION; }
 
 extern "C" const char *ati_last_error(const ati_handle_t *h) { return h ? h->err.c_str() : g_create_err.c_str(); }
 
-// work queues: point tiles of pt points of one case, line tiles of one block
-// (XC_NL xi lines, sg2 eta lines, sg3 zeta lines)
-static void make_tiles(ati_handle *h, int sg2, int sg3, int pt) {
+// the candidate point-tile sizes of the pointwise kernels
+static const int PT_CAND[3] = {PT_MIN, 4 * PT_MIN, PT_MAX};
+
+// point tiles of pt points, each within one case
+static void point_tiles(const ati_handle *h, int pt, std::vector<PTile> &out) {
   const int nbc = h->nb / h->ncase;
-  h->hpt.clear();
+  out.clear();
   for (int cs = 0; cs < h->ncase; cs++) {
     const int64_t g0 = h->blk[h->case_b0[cs]].off;
     const BlockDev &Bl = h->blk[h->case_b0[cs] + nbc - 1];
     const int64_t g1 = Bl.off + Bl.npts;
-    for (int64_t g = g0; g < g1; g += pt) h->hpt.push_back(PTile{cs, 0, g, std::min(g + pt, g1)});
+    for (int64_t g = g0; g < g1; g += pt) out.push_back(PTile{cs, 0, g, std::min(g + pt, g1)});
   }
+}
+
+// point every engine's pointwise kinds at their own tiles (pw_pt), or at the shared queue
+static void apply_pw_tiles(ati_handle *h) {
+  for (int w = 0; w < PW_KINDS; w++) {
+    const PTile *q = nullptr;
+    int n = 0;
+    for (int c = 0; c < 3; c++)
+      if (h->pw_pt[w] == PT_CAND[c]) { q = h->dptc[c]; n = (int)h->hptc[c].size(); }
+    h->ed.ptk[w] = h->ef.ptk[w] = q;
+    h->ed.nptk[w] = h->ef.nptk[w] = n;
+  }
+}
+
+// work queues: point tiles of pt points of one case, line tiles of one block
+// (XC_NL xi lines, sg2 eta lines, sg3 zeta lines)
+static void make_tiles(ati_handle *h, int sg2, int sg3, int pt) {
+  point_tiles(h, pt, h->hpt);
   for (int nn = 1; nn <= 3; nn++) {
     h->hlt[nn].clear();
     const int step = nn == 1 ? XC_NL : (nn == 2 ? sg2 : sg3);
@@ -584,6 +609,7 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
   // work queues, at their finest tiles (the device arrays are sized for these)
   make_tiles(h, SG_MIN, SG_MIN, PT_MIN);
   h->max_pt = h->hpt.size();
+  for (int c = 0; c < 3; c++) point_tiles(h, PT_CAND[c], h->hptc[c]);
   for (int nn = 1; nn <= 3; nn++) h->max_lt[nn] = h->hlt[nn].size();
   make_tiles(h, SG_DEFAULT, SG_DEFAULT, PT_DEFAULT);
   for (int nn = 1; nn <= 3; nn++) {
@@ -767,7 +793,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_sc = take(sizeof(Scheme) * ncase), o_cfd = take(sizeof(Coef<double>)),
                o_scal = take(sizeof(Scalars) * ncase), o_task = take(sizeof(FaceTask) * h->htasks.size()),
                o_jn = take(sizeof(JunctionDev) * 2 * ncase), o_woff = take(nforce * sizeof(int64_t)),
-               o_pt = take(sizeof(PTile) * h->max_pt), o_lt1 = take(sizeof(LTile) * h->max_lt[1]),
+               o_pt = take(sizeof(PTile) * h->max_pt), o_ptc0 = take(sizeof(PTile) * h->hptc[0].size()),
+               o_ptc1 = take(sizeof(PTile) * h->hptc[1].size()), o_ptc2 = take(sizeof(PTile) * h->hptc[2].size()),
+               o_lt1 = take(sizeof(LTile) * h->max_lt[1]),
                o_lt2 = take(sizeof(LTile) * h->max_lt[2]), o_lt3 = take(sizeof(LTile) * h->max_lt[3]),
                o_facud = take((size_t)h->nfac * FU_RT * D8), o_facuf = take((size_t)h->nfac * FU_RT * D8);
   // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(3 x 5) xim etm zem(3) yaco asz bsz(1) gm(3)
@@ -799,6 +827,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   Scheme *dsc = (Scheme *)(h->arena + o_sc);
   Scalars *dscal = (Scalars *)(h->arena + o_scal);
   const PTile *dpt = (const PTile *)(h->arena + o_pt);
+  h->dptc[0] = (const PTile *)(h->arena + o_ptc0);
+  h->dptc[1] = (const PTile *)(h->arena + o_ptc1);
+  h->dptc[2] = (const PTile *)(h->arena + o_ptc2);
   const LTile *dlt[4] = {nullptr, (const LTile *)(h->arena + o_lt1), (const LTile *)(h->arena + o_lt2),
                          (const LTile *)(h->arena + o_lt3)};
   Eng<double> &d = h->ed;
@@ -904,6 +935,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   up(h->djn, jn.data(), sizeof(JunctionDev) * jn.size());
   up(h->dwoff, woff.data(), sizeof(int64_t) * woff.size());
   up(dpt, h->hpt.data(), sizeof(PTile) * h->hpt.size());
+  for (int c = 0; c < 3; c++) up(h->dptc[c], h->hptc[c].data(), sizeof(PTile) * h->hptc[c].size());
   for (int nn = 1; nn <= 3; nn++) up(dlt[nn], h->hlt[nn].data(), sizeof(LTile) * h->hlt[nn].size());
   if (h->mixed) {
     up(h->ef.cf, &cff, sizeof(cff));
@@ -1006,6 +1038,13 @@ static double *field_base(ati_handle *h, int field, int &ncomp, const float **f3
   }
 }
 
+// The mixed path's step takes the viscous stresses inside its flux kernel and keeps no stress planes: the
+// forces and the stress output rebuild the last stage's planes (k_visc) from the derivative planes, viscosity
+// and primitives that stage left, which nothing changes until the next stage.
+static void stress_planes(ati_handle *h) {
+  if (h->mixed && h->cfg.nviscous == 1) fast::pointwise_f(h->ef, h->st, PW_VISC);
+}
+
 static int copy_field(ati_handle *h, int blk, int field, double *host, bool to_dev) {
   if (!h || blk < 0 || blk >= h->nb || !host) return fail(h, ATI_EINVAL, "field copy: bad argument");
   int nc = 0;
@@ -1023,6 +1062,7 @@ static int copy_field(ati_handle *h, int blk, int field, double *host, bool to_d
   if (to_dev) {
     CK(cudaMemcpy2DAsync(base + B.off, dp, host, w, w, nc, cudaMemcpyHostToDevice, h->st));
   } else {
+    if (field == ATI_F_STRESS) stress_planes(h);
     if (f32) {  // widen the FP32 stage field into the FP64 array first (the mixed pressure plane holds p - p_inf)
       const double add = field == ATI_F_P ? h->sh.s.poo : 0.0;
       k_to_double<<<256, 256, 0, h->st>>>(f32, base, (int64_t)nc * h->N, add);
@@ -1182,6 +1222,8 @@ extern "C" int ati_set_tiles(ati_handle_t *h, const int32_t in[4]) {
   CK(cudaStreamSynchronize(h->st));  // steps in flight read the queues
   make_tiles(h, sg2, sg3, pt);
   if (int rc = upload_tiles(h)) return rc;
+  std::fill(h->pw_pt, h->pw_pt + PW_KINDS, 0);  // every pointwise kernel on the pinned tiles
+  apply_pw_tiles(h);
   drop_graphs(h);  // the step graphs hold the old grid shapes
   return ATI_OK;
 }
@@ -1507,9 +1549,27 @@ static int autotune_t(ati_handle *h, Eng<R> &e) {
     sg2 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(v, SG_DEFAULT, PT_DEFAULT); }, sweep_of(2));
     sg3 = pick(sgc, SG_DEFAULT, [&](int v) { set_tiles(sg2, v, PT_DEFAULT); }, sweep_of(3));
   }
-  const int pt = pick({PT_MIN, 4 * PT_MIN, PT_MAX}, PT_DEFAULT, [&](int v) { set_tiles(sg2, sg3, v); },
-                      [&] { C::pw(strict, e, h->st, PW_FLUX); });
-  set_tiles(sg2, sg3, pt);
+  set_tiles(sg2, sg3, PT_DEFAULT);
+  // point tiles, per pointwise kernel: their best sizes differ (the tile's set-up is a chain of dependent loads
+  // that small tiles repeat for every point; large tiles leave a partial last wave of CTAs)
+  const int flux_kind = h->mixed && h->cfg.nviscous == 1 ? PW_FLUX_STRESS : PW_FLUX;
+  std::vector<int> kinds{PW_PRIM, flux_kind, PW_DIV, PW_RK};
+  if (!h->mixed && h->cfg.nviscous == 1) kinds.push_back(PW_VISC);
+  // the RK update rewrites qa from qo and de: qa is kept aside and put back (de and the stage planes written
+  // here are recomputed before they are read)
+  double *keep = h->ed.fw;
+  CK(cudaMemcpyAsync(keep, h->ed.qa, sizeof(double) * 5 * N, cudaMemcpyDeviceToDevice, h->st));
+  std::vector<int> cand(PT_CAND, PT_CAND + 3);
+  for (int w : kinds) {
+    const int v = pick(cand, PT_DEFAULT, [&](int c) { h->pw_pt[w] = c; apply_pw_tiles(h); },
+                       [&] { C::pw(strict, e, h->st, w); });
+    h->pw_pt[w] = v == PT_DEFAULT ? 0 : v;
+    apply_pw_tiles(h);
+  }
+  h->pw_pt[PW_CFL] = h->pw_pt[PW_PRIM];  // (once every ten steps: it takes the tiles of the same loads)
+  apply_pw_tiles(h);
+  if (h->pw_pt[flux_kind]) h->pt_points = h->pw_pt[flux_kind];  // the size ati_tiles reports
+  CK(cudaMemcpyAsync(h->ed.qa, keep, sizeof(double) * 5 * N, cudaMemcpyDeviceToDevice, h->st));
   if (flush) cudaFree(flush);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
@@ -1594,10 +1654,12 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
       SweepIO<R, R> io{e.prim, N, e.dv + (nn - 1) * N, 3 * N, nullptr, 4, 2, true};
       PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, s, nn, false, io));
     });
-    PROF(h, ATI_K_VISC, C::pw(strict, e, st, PW_VISC));
+    if (!Freestream<R>::on) PROF(h, ATI_K_VISC, C::pw(strict, e, st, PW_VISC));
   }
-  // fluxes and their derivatives (src/Main3D.f90:710-768): five fields per launch
-  PROF(h, ATI_K_FLUX, C::pw(strict, e, st, PW_FLUX));
+  // fluxes and their derivatives (src/Main3D.f90:710-768): five fields per launch; the mixed path takes the
+  // stresses inside the flux kernel and leaves the stress planes to stress_planes()
+  const bool fused = Freestream<R>::on && h->cfg.nviscous == 1;
+  PROF(h, ATI_K_FLUX, C::pw(strict, e, st, fused ? PW_FLUX_STRESS : PW_FLUX));
   PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, mpt), mpt.n, mpt.maxline, 0, e.flx,
                                 e.flx + N, e.flx + 2 * N, 3 * N, 5));
   three_directions(h, [&](int nn, cudaStream_t s) {
@@ -1762,8 +1824,10 @@ extern "C" int ati_case_forces(ati_handle_t *h, int cs, double out[2]) {
   if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
   const TaskRange &r = h->tl_force_c[cs];
   const int q0 = r.off - h->tl_force.off;  // position in the wall-face list
-  if (h->mixed)
+  if (h->mixed) {
+    stress_planes(h);
     strict::forces_f(h->ef, h->st, tp(h, r), r.n, h->area, h->wnor, h->dwoff + q0, h->dforce + 2 * q0);
+  }
   else strict::forces_d(h->ed, h->st, tp(h, r), r.n, h->area, h->wnor, h->dwoff + q0, h->dforce + 2 * q0);
   CKL();
   std::vector<double> part((size_t)2 * r.n);

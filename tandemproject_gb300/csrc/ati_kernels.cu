@@ -1241,63 +1241,81 @@ __global__ void k_cfl(Eng<R> e) {
   if (cur >= 0) flush(cur, m1, m2);
 }
 
-// physical gradients of u, v, w, T and the viscous stresses and heat fluxes
-// (src/Main3D.f90:631-692), from the twelve derivative planes dv
+// the scheme constants of the viscous stresses, taken once per tile
+template <typename R>
+struct ViscConst {
+  R gp, tgp, tt, sm1, sm2;
+  int les;
+  __device__ explicit ViscConst(const Scheme &S)
+      : gp((R)S.gamm1prndtli), tgp((R)S.tgamm1prndtli), tt((R)S.two_three), sm1((R)S.smago1), sm2((R)S.smago2),
+        les(S.les) {}
+};
+
+// physical gradients of u, v, w, T and the viscous stresses and heat fluxes at one point
+// (src/Main3D.f90:631-692), from the twelve derivative planes dv and the point's metrics:
+// t = txx, tyy, tzz, txy, tyz, tzx and the energy terms hxx, hyy, hzz
+template <typename R>
+__device__ __forceinline__ void stress_point(const Eng<R> &e, const ViscConst<R> &V, int64_t N, int64_t g, R x1,
+                                             R x2, R x3, R e1, R e2, R e3, R z1, R z2, R z3, R t[9]) {
+  const R *dv = e.dv;
+  R c[4][3];
+#pragma unroll
+  for (int f = 0; f < 4; f++) {
+    const R r1 = dv[g + (f * 3 + 0) * N], r2 = dv[g + (f * 3 + 1) * N], r3 = dv[g + (f * 3 + 2) * N];
+    c[f][0] = x1 * r1 + e1 * r2 + z1 * r3;
+    c[f][1] = x2 * r1 + e2 * r2 + z2 * r3;
+    c[f][2] = x3 * r1 + e3 * r2 + z3 * r3;
+  }
+  // txx,hzz,tzx from u; txy,tyy,hxx from v; hyy,tyz,tzz from w; ss(:,1:3) from T
+  R txx = c[0][0], hzz = c[0][1], tzx = c[0][2];
+  R txy = c[1][0], tyy = c[1][1], hxx = c[1][2];
+  R hyy = c[2][0], tyz = c[2][1], tzz = c[2][2];
+  const R yac = e.yaco[g];
+  R r1 = e.mu[g] * yac;
+  R r2 = V.gp * r1, r3 = 0, d5;
+  if (V.les == 1) {
+    const R d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
+                 (hxx + tyz) * (hxx + tyz);
+    const R varr = (R)pow(-1.0 / (double)yac, 1.5);
+    const R q1 = cvt<R>(e.qa[g]);
+    r3 = q1 * (V.sm1 * V.sm1) * varr * sqrt((R)2 * d1);
+    r1 = r1 + r3 * yac;
+    r2 = r2 + V.tgp * r3 * yac;
+    r3 = V.tt * (q1 * V.sm2 * varr * d1);
+    d5 = V.tt * (txx + tyy + tzz);
+    txx = r1 * ((R)2 * txx - d5) - r3;
+    tyy = r1 * ((R)2 * tyy - d5) - r3;
+    tzz = r1 * ((R)2 * tzz - d5) - r3;
+  } else {
+    d5 = V.tt * (txx + tyy + tzz);
+    txx = r1 * ((R)2 * txx - d5);
+    tyy = r1 * ((R)2 * tyy - d5);
+    tzz = r1 * ((R)2 * tzz - d5);
+  }
+  const R ntxy = r1 * (txy + hzz), ntyz = r1 * (tyz + hxx), ntzx = r1 * (tzx + hyy);
+  const R d2 = e.prim[g], d3 = e.prim[g + N], d4 = e.prim[g + 2 * N];
+  t[0] = txx; t[1] = tyy; t[2] = tzz;
+  t[3] = ntxy; t[4] = ntyz; t[5] = ntzx;
+  t[6] = r2 * c[3][0] + d2 * txx + d3 * ntxy + d4 * ntzx;
+  t[7] = r2 * c[3][1] + d2 * ntxy + d3 * tyy + d4 * ntyz;
+  t[8] = r2 * c[3][2] + d2 * ntzx + d3 * ntyz + d4 * tzz;
+}
+
+// the stress planes tau (plane k holds t[k] of stress_point)
 template <typename R>
 __global__ void k_visc(Eng<R> e) {
   const int64_t N = e.N;
   TILE_LOOP(e, T) {
-    const Scheme &S = e.sc[T.cs];
-    Scalars &SC = e.scal[T.cs];
-    const R gp = (R)S.gamm1prndtli, tgp = (R)S.tgamm1prndtli, tt = (R)S.two_three;
-    const R sm1 = (R)S.smago1, sm2 = (R)S.smago2;
-    const R *dv = e.dv;
-    R *t = e.tau;
+    const ViscConst<R> V(e.sc[T.cs]);
+    R *tau = e.tau;
     POINT_LOOP(T, g) {
       const R x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
       const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
       const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
-      R c[4][3];
-  #pragma unroll
-      for (int f = 0; f < 4; f++) {
-        const R r1 = dv[g + (f * 3 + 0) * N], r2 = dv[g + (f * 3 + 1) * N], r3 = dv[g + (f * 3 + 2) * N];
-        c[f][0] = x1 * r1 + e1 * r2 + z1 * r3;
-        c[f][1] = x2 * r1 + e2 * r2 + z2 * r3;
-        c[f][2] = x3 * r1 + e3 * r2 + z3 * r3;
-      }
-      // txx,hzz,tzx from u; txy,tyy,hxx from v; hyy,tyz,tzz from w; ss(:,1:3) from T
-      R txx = c[0][0], hzz = c[0][1], tzx = c[0][2];
-      R txy = c[1][0], tyy = c[1][1], hxx = c[1][2];
-      R hyy = c[2][0], tyz = c[2][1], tzz = c[2][2];
-      const R yac = e.yaco[g];
-      R r1 = e.mu[g] * yac;
-      R r2 = gp * r1, r3 = 0, d5;
-      if (S.les == 1) {
-        const R d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
-                     (hxx + tyz) * (hxx + tyz);
-        const R varr = (R)pow(-1.0 / (double)yac, 1.5);
-        const R q1 = cvt<R>(e.qa[g]);
-        r3 = q1 * (sm1 * sm1) * varr * sqrt((R)2 * d1);
-        r1 = r1 + r3 * yac;
-        r2 = r2 + tgp * r3 * yac;
-        r3 = tt * (q1 * sm2 * varr * d1);
-        d5 = tt * (txx + tyy + tzz);
-        txx = r1 * ((R)2 * txx - d5) - r3;
-        tyy = r1 * ((R)2 * tyy - d5) - r3;
-        tzz = r1 * ((R)2 * tzz - d5) - r3;
-      } else {
-        d5 = tt * (txx + tyy + tzz);
-        txx = r1 * ((R)2 * txx - d5);
-        tyy = r1 * ((R)2 * tyy - d5);
-        tzz = r1 * ((R)2 * tzz - d5);
-      }
-      const R ntxy = r1 * (txy + hzz), ntyz = r1 * (tyz + hxx), ntzx = r1 * (tzx + hyy);
-      const R d2 = e.prim[g], d3 = e.prim[g + N], d4 = e.prim[g + 2 * N];
-      t[g] = txx; t[g + N] = tyy; t[g + 2 * N] = tzz;
-      t[g + 3 * N] = ntxy; t[g + 4 * N] = ntyz; t[g + 5 * N] = ntzx;
-      t[g + 6 * N] = r2 * c[3][0] + d2 * txx + d3 * ntxy + d4 * ntzx;
-      t[g + 7 * N] = r2 * c[3][1] + d2 * ntxy + d3 * tyy + d4 * ntyz;
-      t[g + 8 * N] = r2 * c[3][2] + d2 * ntzx + d3 * ntyz + d4 * tzz;
+      R t[9];
+      stress_point<R>(e, V, N, g, x1, x2, x3, e1, e2, e3, z1, z2, z3, t);
+#pragma unroll
+      for (int k = 0; k < 9; k++) tau[g + k * N] = t[k];
     }
   }
 }
@@ -1361,14 +1379,18 @@ __device__ __forceinline__ void flux_fast_point(const Eng<double> &e, int64_t N,
 // (src/Main3D.f90:710-766): flx plane (m-1)*3 + (nn-1)
 // (the FP32 kernel streams: five CTAs of 256 threads an SM, at most 51 registers a thread, keep more loads
 // in flight than the 80 registers it would take unbounded; measured 380 -> 296 us a launch on 8.85 M points)
-template <typename R>
-__global__ void __launch_bounds__(256, Freestream<R>::on ? 5 : 1) k_flux(Eng<R> e) {
+// With STRESS the kernel takes the viscous stresses at the point itself (stress_point, the work of k_visc)
+// instead of reading the stress planes: the mixed path's viscous step then never writes or reads those nine
+// planes (72 B a point).  Only launched when the case is viscous.
+template <typename R, bool STRESS = false>
+__global__ void __launch_bounds__(256, Freestream<R>::on ? (STRESS ? 4 : 5) : 1) k_flux(Eng<R> e) {
   const int64_t N = e.N;
   TILE_LOOP(e, T) {
     const Scheme &S = e.sc[T.cs];
     Scalars &SC = e.scal[T.cs];
     const R u1 = (R)SC.umf[1], u2 = (R)SC.umf[2], u3 = (R)SC.umf[3];
-    const bool visc = S.nviscous == 1;
+    const bool visc = STRESS || S.nviscous == 1;
+    const ViscConst<R> V(S);
     if constexpr (kFast && !Freestream<R>::on) {
       if (visc) { POINT_LOOP(T, g) flux_fast_point<true>(e, N, g, u1, u2, u3); }
       else { POINT_LOOP(T, g) flux_fast_point<false>(e, N, g, u1, u2, u3); }
@@ -1402,8 +1424,13 @@ __global__ void __launch_bounds__(256, Freestream<R>::on ? 5 : 1) k_flux(Eng<R> 
         const R q = cvt<R>(e.qa[g]);
         F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
       }
-      R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
-      if (visc) {
+      R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, tv[9];
+      if constexpr (STRESS) {
+        stress_point<R>(e, V, N, g, x1, x2, x3, e1, e2, e3, z1, z2, z3, tv);
+        ta[0] = tv[0]; tb[0] = tv[3]; tc[0] = tv[5];
+        ta[1] = tv[3]; tb[1] = tv[1]; tc[1] = tv[4];
+        ta[2] = tv[5]; tb[2] = tv[4]; tc[2] = tv[2];
+      } else if (visc) {
         ta[0] = t[g]; tb[0] = t[g + 3 * N]; tc[0] = t[g + 5 * N];
         ta[1] = t[g + 3 * N]; tb[1] = t[g + N]; tc[1] = t[g + 4 * N];
         ta[2] = t[g + 5 * N]; tb[2] = t[g + 4 * N]; tc[2] = t[g + 2 * N];
@@ -1440,7 +1467,9 @@ __global__ void __launch_bounds__(256, Freestream<R>::on ? 5 : 1) k_flux(Eng<R> 
           c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
         }
         if (visc) {
-          const R ha = t[g + 6 * N], hb = t[g + 7 * N], hc = t[g + 8 * N];
+          R ha, hb, hc;
+          if constexpr (STRESS) { ha = tv[6]; hb = tv[7]; hc = tv[8]; }
+          else { ha = t[g + 6 * N]; hb = t[g + 7 * N]; hc = t[g + 8 * N]; }
           a = a - x1 * ha - x2 * hb - x3 * hc;
           b = b - e1 * ha - e2 * hb - e3 * hc;
           c = c - z1 * ha - z2 * hb - z3 * hc;
@@ -2114,7 +2143,12 @@ static int pw_grid(int64_t N) {
 }
 
 template <typename R>
-static void pointwise_t(const Eng<R> &e, cudaStream_t st, int which) {
+static void pointwise_t(const Eng<R> &eng, cudaStream_t st, int which) {
+  Eng<R> e = eng;
+  if (eng.ptk[which]) {  // the kernel's own tile size
+    e.pt = eng.ptk[which];
+    e.npt = eng.nptk[which];
+  }
   if (e.npt == 0) return;
   const int g = e.npt < 152 * 16 ? e.npt : 152 * 16, t = 256;  // CTAs walk the point tiles, stride gridDim.x
   switch (which) {
@@ -2122,6 +2156,9 @@ static void pointwise_t(const Eng<R> &e, cudaStream_t st, int which) {
     case PW_CFL: k_cfl<R><<<g, t, 0, st>>>(e); break;
     case PW_VISC: k_visc<R><<<g, t, 0, st>>>(e); break;
     case PW_FLUX: k_flux<R><<<g, t, 0, st>>>(e); break;
+    case PW_FLUX_STRESS:  // the mixed path's viscous fluxes (the FP64 path writes the stress planes)
+      if constexpr (Freestream<R>::on) k_flux<R, true><<<g, t, 0, st>>>(e);
+      break;
     case PW_DIV: k_div<R><<<g, t, 0, st>>>(e); break;
     case PW_RK: k_rk<R><<<g, t, 0, st>>>(e); break;
   }

@@ -27,6 +27,9 @@ struct Coef {
 // Device pointers of a handle (one case or a batch) for intermediates of
 // type R, passed by value.  Per-case data (sc, scal) is indexed by the case
 // of a block (BlockDev::cs) or of a point tile (PTile::cs).
+// kinds of pointwise kernel (the PW_ enumeration)
+constexpr int PW_KINDS = 7;
+
 template <typename R>
 struct Eng {
   const BlockDev *blk;
@@ -46,6 +49,9 @@ struct Eng {
   int sg_lines[4];      // lines per CTA of the eta (2) and zeta (3) sweeps: the tiles of lt[2], lt[3]
   int maxlen[4];        // longest line per direction
   int64_t N;            // points of all blocks
+  // a pointwise kernel's own point tiles, when its timed best differs from pt (index: the PW_ kind; null: pt)
+  const PTile *ptk[PW_KINDS];
+  int nptk[PW_KINDS];
   double *qa, *qo;      // state (5 planes each), FP64
   const double *yacod;  // Jacobian, FP64 (RK update)
   double *cnt;          // visit counts of the interface averaging (2 planes), FP64
@@ -81,7 +87,8 @@ struct Freestream<float> {
   static constexpr bool on = true;
 };
 
-enum { PW_PRIM, PW_CFL, PW_VISC, PW_FLUX, PW_DIV, PW_RK };
+enum { PW_PRIM, PW_CFL, PW_VISC, PW_FLUX, PW_DIV, PW_RK, PW_FLUX_STRESS };
+static_assert(PW_FLUX_STRESS + 1 == PW_KINDS, "PW_KINDS counts the pointwise kernels");
 enum { FK_GCBC_PREP, FK_GCBC_APPLY, FK_WALL, FK_PACK, FK_AVG };
 enum { SC_MOVEF_A, SC_CFL_RESET, SC_DT_NEW, SC_DT, SC_MOVEF_B, SC_ADVANCE, SC_INIT };
 
@@ -105,7 +112,7 @@ struct SweepIO {
 
 // lines per work-queue tile of the xi sweeps (shared-memory chunks); the
 // eta/zeta sweeps take SG_MIN..SG_MAX lines per CTA and the pointwise kernels
-// PT_MIN..PT_MAX points per tile, chosen per handle by timing (ati_init)
+// PT_MIN..PT_MAX points per tile, chosen per handle and pointwise kernel by timing (ati_init)
 constexpr int XC_NL = 64;
 constexpr int SG_MIN = 32, SG_MAX = 256, SG_DEFAULT = 128;
 // (a tile of 256 points is one point per thread: consecutive CTAs then sweep

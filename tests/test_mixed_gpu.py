@@ -59,6 +59,16 @@ def test_mixed_impulsive_start_tracks_fp64(ati_lib):
     print("impulsive start, mixed vs fp64 after 100 steps", e, whole)
     assert e[0] < 2e-6 and e[4] < 2e-6 and whole < 2e-6
     assert np.all(e[1:4] < 1e-4)
+    # the mixed step takes the stresses inside its flux kernel: the stress output is rebuilt from the last
+    # stage's derivative planes, and must be the last stage's stresses as the FP64 path keeps them
+    from tandemproject_gb300.solver import F_STRESS
+    num = den = 0.0
+    for mb in range(6):
+        sd, sm = d.get_field(mb, F_STRESS), m.get_field(mb, F_STRESS)
+        num += np.sum((sm - sd) ** 2)
+        den += np.sum(sd ** 2)
+    print("stress planes, mixed vs fp64", np.sqrt(num / den))
+    assert den > 0 and np.sqrt(num / den) < 1e-3
 
 
 def test_mixed_filter_step_matches_fp64_closely(ati_lib):
