@@ -1132,48 +1132,122 @@ __global__ void k_mpigo(const BlockDev *blk, const Coef<TC> *cf, const FaceTask 
     if (const PTile T = (e).pt[t_]; true)
 #define POINT_LOOP(T, g) for (int64_t g = (T).g0 + threadIdx.x; g < (T).g1; g += blockDim.x)
 
-// primitives, pressure, temperature, Sutherland viscosity (src/Main3D.f90:576-583)
+// ---------------------------------------------------------------------------
+// Shared-memory staging of the mixed path's streaming kernels.  Each thread
+// copies (cp.async) the input planes of the points it will take STG - 1 points
+// ahead into its own column of a ring of STG slots, and waits only for its own
+// oldest copies: the loads of the next points are in flight while it computes,
+// without holding registers, and no thread waits on another (no barrier).
+// A slot is refilled one iteration after it was read, once the values read from
+// it have been used.
+// ---------------------------------------------------------------------------
+template <typename T, int NPL, int STG>
+struct Ring {
+  T *col;  // this thread's column: slot s, plane p at col[(s * NPL + p) * nt]
+  int nt;
+  __device__ Ring(T *smem, int nthreads) : col(smem + threadIdx.x), nt(nthreads) {}
+  __device__ T *at(int s, int p) const { return col + (s * NPL + p) * nt; }
+  __device__ T get(int s, int p) const { return *at(s, p); }
+  static constexpr size_t bytes(int nthreads) { return sizeof(T) * NPL * STG * (size_t)nthreads; }
+};
+
+// the stage loop of one tile: fetch(slot, g) issues the copies of point g, take(slot, g) consumes them
+template <int STG, class Fetch, class Take>
+__device__ __forceinline__ void staged_points(const PTile &T, Fetch &&fetch, Take &&take) {
+  const int nt = blockDim.x;
+  int64_t g = T.g0 + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < STG - 1; k++) {
+    if (g + (int64_t)k * nt < T.g1) fetch(k, g + (int64_t)k * nt);
+    cp_async_commit();
+  }
+  for (int s = 0; g < T.g1; g += nt, s = s + 1 == STG ? 0 : s + 1) {
+    const int64_t gn = g + (int64_t)(STG - 1) * nt;
+    if (gn < T.g1) fetch(s == 0 ? STG - 1 : s - 1, gn);
+    cp_async_commit();
+    cp_async_wait<STG - 1>();
+    take(s, g);
+  }
+}
+
+// primitives, pressure, temperature, Sutherland viscosity (src/Main3D.f90:576-583) of point g from its state
+// q[0..4] (as read from qa); false for a non-physical state
+template <typename R>
+struct PrimConst {  // the scheme constants of prim_point, taken once per tile
+  R gamm1, gam, srefp1dre, srefoo, poo;
+  double rhoE_inf;
+  __device__ explicit PrimConst(const Scheme &S)
+      : gamm1((R)S.gamm1), gam((R)S.gam), srefp1dre((R)S.srefp1dre), srefoo((R)S.srefoo), poo((R)S.poo),
+        rhoE_inf(S.hamm1 * S.poo) {}
+};
+template <typename R>
+__device__ __forceinline__ bool prim_point(const Eng<R> &e, const PrimConst<R> &C, int64_t N, int64_t g,
+                                           const double q[5]) {
+  const R gamm1 = C.gamm1, gam = C.gam, srefp1dre = C.srefp1dre, srefoo = C.srefoo;
+  const double rhoE_inf = C.rhoE_inf;
+  // (the mixed kernel is bound by the FP64 pipe, which also runs the conversion instruction: the state is
+  // rounded to FP32 on the integer pipes instead, bit for bit the same)
+  auto rnd = [](double v) -> R {
+    if constexpr (Freestream<R>::on) return narrow(v);
+    else return (R)v;
+  };
+  const R q1 = rnd(q[0]), q2 = rnd(q[1]), q3 = rnd(q[2]), q4 = rnd(q[3]);
+  const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
+  R pp, d5;
+  if constexpr (Freestream<R>::on) {
+    // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
+    const R re = rnd(q[4] - rhoE_inf);
+    pp = gamm1 * (re - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
+    d5 = gam * (C.poo + pp) * d1;
+  } else {
+    const R q5 = cvt<R>(q[4]);
+    pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
+    d5 = gam * pp * d1;
+  }
+  // T^1.5 as T*sqrt(T): the value of pow(T,1.5) to ~1 ulp with far fewer instructions
+  const R mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
+  e.prim[g] = d2; e.prim[g + N] = d3; e.prim[g + 2 * N] = d4; e.prim[g + 3 * N] = d5;
+  e.p[g] = pp;
+  e.mu[g] = mu;
+  const R pabs = Freestream<R>::on ? C.poo + pp : pp;
+  bool finite;
+  if constexpr (Freestream<R>::on) finite = ((__double2hiint(q[4]) >> 20) & 0x7ff) != 0x7ff;
+  else finite = fabs(q[4]) < 1e300;
+  return q1 > (R)0 && pabs > (R)0 && finite;
+}
+
 template <typename R>
 __global__ void k_prim(Eng<R> e) {
   const int64_t N = e.N;
   TILE_LOOP(e, T) {
-    const Scheme &S = e.sc[T.cs];
-    Scalars &SC = e.scal[T.cs];
-    const R gamm1 = (R)S.gamm1, gam = (R)S.gam, srefp1dre = (R)S.srefp1dre, srefoo = (R)S.srefoo;
+    const PrimConst<R> C(e.sc[T.cs]);
     int bad = 0;
-    const double rhoE_inf = S.hamm1 * S.poo;
-    // (the mixed kernel is bound by the FP64 pipe, which also runs the conversion instruction: the state is
-    // rounded to FP32 on the integer pipes instead, bit for bit the same)
-    auto rnd = [](double v) -> R {
-      if constexpr (Freestream<R>::on) return narrow(v);
-      else return (R)v;
-    };
     POINT_LOOP(T, g) {
-      const R q1 = rnd(e.qa[g]), q2 = rnd(e.qa[g + N]), q3 = rnd(e.qa[g + 2 * N]), q4 = rnd(e.qa[g + 3 * N]);
-      const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
-      R pp, d5;
-      if constexpr (Freestream<R>::on) {
-        // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
-        const R re = rnd(e.qa[g + 4 * N] - rhoE_inf);
-        pp = gamm1 * (re - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
-        d5 = gam * ((R)S.poo + pp) * d1;
-      } else {
-        const R q5 = cvt<R>(e.qa[g + 4 * N]);
-        pp = gamm1 * (q5 - (R)0.5 * (q2 * d2 + q3 * d3 + q4 * d4));
-        d5 = gam * pp * d1;
-      }
-      // T^1.5 as T*sqrt(T): the value of pow(T,1.5) to ~1 ulp with far fewer instructions
-      const R mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
-      e.prim[g] = d2; e.prim[g + N] = d3; e.prim[g + 2 * N] = d4; e.prim[g + 3 * N] = d5;
-      e.p[g] = pp;
-      e.mu[g] = mu;
-      const R pabs = Freestream<R>::on ? (R)S.poo + pp : pp;
-      bool finite;
-      if constexpr (Freestream<R>::on) finite = ((__double2hiint(e.qa[g + 4 * N]) >> 20) & 0x7ff) != 0x7ff;
-      else finite = fabs((double)e.qa[g + 4 * N]) < 1e300;
-      if (!(q1 > (R)0) || !(pabs > (R)0) || !finite) bad = 1;
+      const double q[5] = {e.qa[g], e.qa[g + N], e.qa[g + 2 * N], e.qa[g + 3 * N], e.qa[g + 4 * N]};
+      if (!prim_point<R>(e, C, N, g, q)) bad = 1;
     }
-    if (bad) atomicOr(&SC.flag, 1);
+    if (bad) atomicOr(&e.scal[T.cs].flag, 1);
+  }
+}
+
+// the mixed path's primitives with the state staged through shared memory (Ring), PRS_STG points ahead
+constexpr int PRS_STG = 4;
+__global__ void __launch_bounds__(256) k_prim_staged(Eng<float> e) {
+  __shared__ double prs_smem[5 * PRS_STG * 256];
+  const int64_t N = e.N;
+  Ring<double, 5, PRS_STG> rd(prs_smem, blockDim.x);
+  auto fetch = [&](int s, int64_t g) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) cp_async<8>(rd.at(s, p), e.qa + g + p * N);
+  };
+  TILE_LOOP(e, T) {
+    const PrimConst<float> C(e.sc[T.cs]);
+    int bad = 0;
+    staged_points<PRS_STG>(T, fetch, [&](int s, int64_t g) {
+      const double q[5] = {rd.get(s, 0), rd.get(s, 1), rd.get(s, 2), rd.get(s, 3), rd.get(s, 4)};
+      if (!prim_point<float>(e, C, N, g, q)) bad = 1;
+    });
+    if (bad) atomicOr(&e.scal[T.cs].flag, 1);
   }
 }
 
@@ -1251,17 +1325,29 @@ struct ViscConst {
         les(S.les) {}
 };
 
+// a point's inputs of the stresses, read from the engine's planes
+template <typename R>
+struct PlaneIn {
+  const Eng<R> &e;
+  int64_t N, g;
+  __device__ R dv(int k) const { return e.dv[g + k * N]; }
+  __device__ R yac() const { return e.yaco[g]; }
+  __device__ R mu() const { return e.mu[g]; }
+  __device__ R rho() const { return cvt<R>(e.qa[g]); }
+  __device__ R vel(int k) const { return e.prim[g + k * N]; }
+};
+
 // physical gradients of u, v, w, T and the viscous stresses and heat fluxes at one point
 // (src/Main3D.f90:631-692), from the twelve derivative planes dv and the point's metrics:
-// t = txx, tyy, tzz, txy, tyz, tzx and the energy terms hxx, hyy, hzz
-template <typename R>
-__device__ __forceinline__ void stress_point(const Eng<R> &e, const ViscConst<R> &V, int64_t N, int64_t g, R x1,
-                                             R x2, R x3, R e1, R e2, R e3, R z1, R z2, R z3, R t[9]) {
-  const R *dv = e.dv;
+// t = txx, tyy, tzz, txy, tyz, tzx and the energy terms hxx, hyy, hzz.  In gives the point's
+// inputs (PlaneIn: from the planes; the staged flux kernel: from shared memory).
+template <typename R, class In>
+__device__ __forceinline__ void stress_point(const In &in, const ViscConst<R> &V, R x1, R x2, R x3, R e1, R e2,
+                                             R e3, R z1, R z2, R z3, R t[9]) {
   R c[4][3];
 #pragma unroll
   for (int f = 0; f < 4; f++) {
-    const R r1 = dv[g + (f * 3 + 0) * N], r2 = dv[g + (f * 3 + 1) * N], r3 = dv[g + (f * 3 + 2) * N];
+    const R r1 = in.dv(f * 3 + 0), r2 = in.dv(f * 3 + 1), r3 = in.dv(f * 3 + 2);
     c[f][0] = x1 * r1 + e1 * r2 + z1 * r3;
     c[f][1] = x2 * r1 + e2 * r2 + z2 * r3;
     c[f][2] = x3 * r1 + e3 * r2 + z3 * r3;
@@ -1270,14 +1356,14 @@ __device__ __forceinline__ void stress_point(const Eng<R> &e, const ViscConst<R>
   R txx = c[0][0], hzz = c[0][1], tzx = c[0][2];
   R txy = c[1][0], tyy = c[1][1], hxx = c[1][2];
   R hyy = c[2][0], tyz = c[2][1], tzz = c[2][2];
-  const R yac = e.yaco[g];
-  R r1 = e.mu[g] * yac;
+  const R yac = in.yac();
+  R r1 = in.mu() * yac;
   R r2 = V.gp * r1, r3 = 0, d5;
   if (V.les == 1) {
     const R d1 = txx * txx + tyy * tyy + tzz * tzz + (hzz + txy) * (hzz + txy) + (hyy + tzx) * (hyy + tzx) +
                  (hxx + tyz) * (hxx + tyz);
     const R varr = (R)pow(-1.0 / (double)yac, 1.5);
-    const R q1 = cvt<R>(e.qa[g]);
+    const R q1 = in.rho();
     r3 = q1 * (V.sm1 * V.sm1) * varr * sqrt((R)2 * d1);
     r1 = r1 + r3 * yac;
     r2 = r2 + V.tgp * r3 * yac;
@@ -1293,7 +1379,7 @@ __device__ __forceinline__ void stress_point(const Eng<R> &e, const ViscConst<R>
     tzz = r1 * ((R)2 * tzz - d5);
   }
   const R ntxy = r1 * (txy + hzz), ntyz = r1 * (tyz + hxx), ntzx = r1 * (tzx + hyy);
-  const R d2 = e.prim[g], d3 = e.prim[g + N], d4 = e.prim[g + 2 * N];
+  const R d2 = in.vel(0), d3 = in.vel(1), d4 = in.vel(2);
   t[0] = txx; t[1] = tyy; t[2] = tzz;
   t[3] = ntxy; t[4] = ntyz; t[5] = ntzx;
   t[6] = r2 * c[3][0] + d2 * txx + d3 * ntxy + d4 * ntzx;
@@ -1313,7 +1399,7 @@ __global__ void k_visc(Eng<R> e) {
       const R e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
       const R z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
       R t[9];
-      stress_point<R>(e, V, N, g, x1, x2, x3, e1, e2, e3, z1, z2, z3, t);
+      stress_point<R>(PlaneIn<R>{e, N, g}, V, x1, x2, x3, e1, e2, e3, z1, z2, z3, t);
 #pragma unroll
       for (int k = 0; k < 9; k++) tau[g + k * N] = t[k];
     }
@@ -1379,18 +1465,15 @@ __device__ __forceinline__ void flux_fast_point(const Eng<double> &e, int64_t N,
 // (src/Main3D.f90:710-766): flx plane (m-1)*3 + (nn-1)
 // (the FP32 kernel streams: five CTAs of 256 threads an SM, at most 51 registers a thread, keep more loads
 // in flight than the 80 registers it would take unbounded; measured 380 -> 296 us a launch on 8.85 M points)
-// With STRESS the kernel takes the viscous stresses at the point itself (stress_point, the work of k_visc)
-// instead of reading the stress planes: the mixed path's viscous step then never writes or reads those nine
-// planes (72 B a point).  Only launched when the case is viscous.
-template <typename R, bool STRESS = false>
-__global__ void __launch_bounds__(256, Freestream<R>::on ? (STRESS ? 4 : 5) : 1) k_flux(Eng<R> e) {
+// (the mixed path's viscous fluxes take the stresses at the point instead: k_flux_staged)
+template <typename R>
+__global__ void __launch_bounds__(256, Freestream<R>::on ? 5 : 1) k_flux(Eng<R> e) {
   const int64_t N = e.N;
   TILE_LOOP(e, T) {
     const Scheme &S = e.sc[T.cs];
     Scalars &SC = e.scal[T.cs];
     const R u1 = (R)SC.umf[1], u2 = (R)SC.umf[2], u3 = (R)SC.umf[3];
-    const bool visc = STRESS || S.nviscous == 1;
-    const ViscConst<R> V(S);
+    const bool visc = S.nviscous == 1;
     if constexpr (kFast && !Freestream<R>::on) {
       if (visc) { POINT_LOOP(T, g) flux_fast_point<true>(e, N, g, u1, u2, u3); }
       else { POINT_LOOP(T, g) flux_fast_point<false>(e, N, g, u1, u2, u3); }
@@ -1424,13 +1507,8 @@ __global__ void __launch_bounds__(256, Freestream<R>::on ? (STRESS ? 4 : 5) : 1)
         const R q = cvt<R>(e.qa[g]);
         F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
       }
-      R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0}, tv[9];
-      if constexpr (STRESS) {
-        stress_point<R>(e, V, N, g, x1, x2, x3, e1, e2, e3, z1, z2, z3, tv);
-        ta[0] = tv[0]; tb[0] = tv[3]; tc[0] = tv[5];
-        ta[1] = tv[3]; tb[1] = tv[1]; tc[1] = tv[4];
-        ta[2] = tv[5]; tb[2] = tv[4]; tc[2] = tv[2];
-      } else if (visc) {
+      R ta[3] = {0, 0, 0}, tb[3] = {0, 0, 0}, tc[3] = {0, 0, 0};
+      if (visc) {
         ta[0] = t[g]; tb[0] = t[g + 3 * N]; tc[0] = t[g + 5 * N];
         ta[1] = t[g + 3 * N]; tb[1] = t[g + N]; tc[1] = t[g + 4 * N];
         ta[2] = t[g + 5 * N]; tb[2] = t[g + 4 * N]; tc[2] = t[g + 2 * N];
@@ -1467,9 +1545,7 @@ __global__ void __launch_bounds__(256, Freestream<R>::on ? (STRESS ? 4 : 5) : 1)
           c = d5 * s3 - pp * (u1 * z1 + u2 * z2 + u3 * z3);
         }
         if (visc) {
-          R ha, hb, hc;
-          if constexpr (STRESS) { ha = tv[6]; hb = tv[7]; hc = tv[8]; }
-          else { ha = t[g + 6 * N]; hb = t[g + 7 * N]; hc = t[g + 8 * N]; }
+          const R ha = t[g + 6 * N], hb = t[g + 7 * N], hc = t[g + 8 * N];
           a = a - x1 * ha - x2 * hb - x3 * hc;
           b = b - e1 * ha - e2 * hb - e3 * hc;
           c = c - z1 * ha - z2 * hb - z3 * hc;
@@ -1477,6 +1553,95 @@ __global__ void __launch_bounds__(256, Freestream<R>::on ? (STRESS ? 4 : 5) : 1)
         F[g + 12 * N] = a; F[g + 13 * N] = b; F[g + 14 * N] = c;
       }
     }
+  }
+}
+
+// the mixed path's viscous fluxes (k_flux with the stresses of k_visc taken at the point), inputs staged:
+// 5 FP64 state planes and 27 FP32 planes a point (metrics 9, derivative planes 12, Jacobian, viscosity,
+// velocity 3, pressure); no stress plane is written or read
+constexpr int FXS_STG = 2, FXS_ND = 5, FXS_NF = 27;
+struct FluxStageIn {
+  const float *f;  // the point's FP32 planes in shared memory, plane stride nt
+  const double *d;
+  int nt;
+  __device__ float at(int p) const { return f[p * nt]; }
+  __device__ float dv(int k) const { return at(9 + k); }
+  __device__ float yac() const { return at(21); }
+  __device__ float mu() const { return at(22); }
+  __device__ float rho() const { return cvt<float>(d[0]); }
+  __device__ float vel(int k) const { return at(23 + k); }
+};
+size_t flux_staged_smem(int nt) {
+  return Ring<double, FXS_ND, FXS_STG>::bytes(nt) + Ring<float, FXS_NF, FXS_STG>::bytes(nt);
+}
+
+__global__ void __launch_bounds__(256, 3) k_flux_staged(Eng<float> e) {
+  extern __shared__ __align__(16) unsigned char fxs_smem[];
+  const int nt = blockDim.x;
+  const int64_t N = e.N;
+  Ring<double, FXS_ND, FXS_STG> rd((double *)fxs_smem, nt);
+  Ring<float, FXS_NF, FXS_STG> rf((float *)(fxs_smem + Ring<double, FXS_ND, FXS_STG>::bytes(nt)), nt);
+  float *F = e.flx;
+  auto fetch = [&](int s, int64_t g) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) cp_async<8>(rd.at(s, p), e.qa + g + p * N);
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+      cp_async<4>(rf.at(s, p), e.xim + g + p * N);
+      cp_async<4>(rf.at(s, 3 + p), e.etm + g + p * N);
+      cp_async<4>(rf.at(s, 6 + p), e.zem + g + p * N);
+      cp_async<4>(rf.at(s, 23 + p), e.prim + g + p * N);
+    }
+#pragma unroll
+    for (int p = 0; p < 12; p++) cp_async<4>(rf.at(s, 9 + p), e.dv + g + p * N);
+    cp_async<4>(rf.at(s, 21), e.yaco + g);
+    cp_async<4>(rf.at(s, 22), e.mu + g);
+    cp_async<4>(rf.at(s, 26), e.p + g);
+  };
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    const Scalars &SC = e.scal[T.cs];
+    const float u1 = (float)SC.umf[1], u2 = (float)SC.umf[2], u3 = (float)SC.umf[3];
+    const ViscConst<float> V(S);
+    const double rhooo = S.rhooo, rhoE_inf = S.hamm1 * S.poo;
+    const float poo = (float)S.poo;
+    staged_points<FXS_STG>(T, fetch, [&](int s, int64_t g) {
+      const FluxStageIn in{rf.at(s, 0), rd.at(s, 0), nt};
+      const float x1 = in.at(0), x2 = in.at(1), x3 = in.at(2);
+      const float e1 = in.at(3), e2 = in.at(4), e3 = in.at(5);
+      const float z1 = in.at(6), z2 = in.at(7), z3 = in.at(8);
+      float tv[9];
+      stress_point<float>(in, V, x1, x2, x3, e1, e2, e3, z1, z2, z3, tv);
+      const float pp = in.at(26);
+      // contravariant velocities of u and of umf apart (the freestream split of k_flux)
+      const float r1 = in.vel(0), r2 = in.vel(1), r3 = in.vel(2);
+      const float su1 = x1 * r1 + x2 * r2 + x3 * r3, sm1 = x1 * u1 + x2 * u2 + x3 * u3;
+      const float su2 = e1 * r1 + e2 * r2 + e3 * r3, sm2 = e1 * u1 + e2 * u2 + e3 * u3;
+      const float su3 = z1 * r1 + z2 * r2 + z3 * r3, sm3 = z1 * u1 + z2 * u2 + z3 * u3;
+      const float s1 = su1 + sm1, s2 = su2 + sm2, s3 = su3 + sm3;
+      const double q1 = rd.get(s, 0);
+      const float q = cvt<float>(q1), qp = cvt<float>(q1 - rhooo);
+      F[g] = q * su1 + qp * sm1; F[g + N] = q * su2 + qp * sm2; F[g + 2 * N] = q * su3 + qp * sm3;
+      const float ta[3] = {tv[0], tv[3], tv[5]}, tb[3] = {tv[3], tv[1], tv[4]}, tc[3] = {tv[5], tv[4], tv[2]};
+      const float xm[3] = {x1, x2, x3}, em[3] = {e1, e2, e3}, zm[3] = {z1, z2, z3};
+#pragma unroll
+      for (int m = 2; m <= 4; m++) {
+        const float qm = cvt<float>(rd.get(s, m - 1));
+        const float a = qm * s1 + xm[m - 2] * pp - x1 * ta[m - 2] - x2 * tb[m - 2] - x3 * tc[m - 2];
+        const float b = qm * s2 + em[m - 2] * pp - e1 * ta[m - 2] - e2 * tb[m - 2] - e3 * tc[m - 2];
+        const float c = qm * s3 + zm[m - 2] * pp - z1 * ta[m - 2] - z2 * tb[m - 2] - z3 * tc[m - 2];
+        F[g + ((m - 1) * 3 + 0) * N] = a;
+        F[g + ((m - 1) * 3 + 1) * N] = b;
+        F[g + ((m - 1) * 3 + 2) * N] = c;
+      }
+      // (rhoE + p) U - p (umf . grad xi) - rhoE_inf (umf . grad xi), less the heat-flux terms
+      const double q5 = rd.get(s, 4);
+      const float d5 = cvt<float>(q5) + poo + pp, re = cvt<float>(q5 - rhoE_inf);
+      const float ha = tv[6], hb = tv[7], hc = tv[8];
+      F[g + 12 * N] = d5 * su1 + re * sm1 - x1 * ha - x2 * hb - x3 * hc;
+      F[g + 13 * N] = d5 * su2 + re * sm2 - e1 * ha - e2 * hb - e3 * hc;
+      F[g + 14 * N] = d5 * su3 + re * sm3 - z1 * ha - z2 * hb - z3 * hc;
+    });
   }
 }
 
@@ -2100,9 +2265,14 @@ static cudaError_t seg_attr() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<3, true, TI, TO>, A, v);
   return e;
 }
+// the mixed path's kernels with more than 48 KB of dynamic shared memory: the segmented sweeps and the staged
+// flux kernel
 cudaError_t seg_init() {
   cudaError_t e = seg_attr<float, float>();
-  return e == cudaSuccess ? seg_attr<double, double>() : e;
+  if (e == cudaSuccess) e = seg_attr<double, double>();
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_flux_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)flux_staged_smem(256));
+  return e;
 }
 
 void sweep_ddd(const Eng<double> &e, cudaStream_t st, int nn, bool filt, const SweepIO<double, double> &io) {
@@ -2152,12 +2322,15 @@ static void pointwise_t(const Eng<R> &eng, cudaStream_t st, int which) {
   if (e.npt == 0) return;
   const int g = e.npt < 152 * 16 ? e.npt : 152 * 16, t = 256;  // CTAs walk the point tiles, stride gridDim.x
   switch (which) {
-    case PW_PRIM: k_prim<R><<<g, t, 0, st>>>(e); break;
+    case PW_PRIM:
+      if constexpr (Freestream<R>::on) k_prim_staged<<<g, t, 0, st>>>(e);
+      else k_prim<R><<<g, t, 0, st>>>(e);
+      break;
     case PW_CFL: k_cfl<R><<<g, t, 0, st>>>(e); break;
     case PW_VISC: k_visc<R><<<g, t, 0, st>>>(e); break;
     case PW_FLUX: k_flux<R><<<g, t, 0, st>>>(e); break;
     case PW_FLUX_STRESS:  // the mixed path's viscous fluxes (the FP64 path writes the stress planes)
-      if constexpr (Freestream<R>::on) k_flux<R, true><<<g, t, 0, st>>>(e);
+      if constexpr (Freestream<R>::on) k_flux_staged<<<g, t, flux_staged_smem(t), st>>>(e);
       break;
     case PW_DIV: k_div<R><<<g, t, 0, st>>>(e); break;
     case PW_RK: k_rk<R><<<g, t, 0, st>>>(e); break;
