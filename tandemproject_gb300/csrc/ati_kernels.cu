@@ -1622,14 +1622,15 @@ __global__ void __launch_bounds__(256, 3) k_flux_staged(Eng<float> e) {
       const double q1 = rd.get(s, 0);
       const float q = cvt<float>(q1), qp = cvt<float>(q1 - rhooo);
       F[g] = q * su1 + qp * sm1; F[g + N] = q * su2 + qp * sm2; F[g + 2 * N] = q * su3 + qp * sm3;
+      // the viscous terms are summed before they meet the inviscid flux (small terms first)
       const float ta[3] = {tv[0], tv[3], tv[5]}, tb[3] = {tv[3], tv[1], tv[4]}, tc[3] = {tv[5], tv[4], tv[2]};
       const float xm[3] = {x1, x2, x3}, em[3] = {e1, e2, e3}, zm[3] = {z1, z2, z3};
 #pragma unroll
       for (int m = 2; m <= 4; m++) {
         const float qm = cvt<float>(rd.get(s, m - 1));
-        const float a = qm * s1 + xm[m - 2] * pp - x1 * ta[m - 2] - x2 * tb[m - 2] - x3 * tc[m - 2];
-        const float b = qm * s2 + em[m - 2] * pp - e1 * ta[m - 2] - e2 * tb[m - 2] - e3 * tc[m - 2];
-        const float c = qm * s3 + zm[m - 2] * pp - z1 * ta[m - 2] - z2 * tb[m - 2] - z3 * tc[m - 2];
+        const float a = qm * s1 + xm[m - 2] * pp - (x1 * ta[m - 2] + x2 * tb[m - 2] + x3 * tc[m - 2]);
+        const float b = qm * s2 + em[m - 2] * pp - (e1 * ta[m - 2] + e2 * tb[m - 2] + e3 * tc[m - 2]);
+        const float c = qm * s3 + zm[m - 2] * pp - (z1 * ta[m - 2] + z2 * tb[m - 2] + z3 * tc[m - 2]);
         F[g + ((m - 1) * 3 + 0) * N] = a;
         F[g + ((m - 1) * 3 + 1) * N] = b;
         F[g + ((m - 1) * 3 + 2) * N] = c;
@@ -1638,9 +1639,9 @@ __global__ void __launch_bounds__(256, 3) k_flux_staged(Eng<float> e) {
       const double q5 = rd.get(s, 4);
       const float d5 = cvt<float>(q5) + poo + pp, re = cvt<float>(q5 - rhoE_inf);
       const float ha = tv[6], hb = tv[7], hc = tv[8];
-      F[g + 12 * N] = d5 * su1 + re * sm1 - x1 * ha - x2 * hb - x3 * hc;
-      F[g + 13 * N] = d5 * su2 + re * sm2 - e1 * ha - e2 * hb - e3 * hc;
-      F[g + 14 * N] = d5 * su3 + re * sm3 - z1 * ha - z2 * hb - z3 * hc;
+      F[g + 12 * N] = d5 * su1 + re * sm1 - (x1 * ha + x2 * hb + x3 * hc);
+      F[g + 13 * N] = d5 * su2 + re * sm2 - (e1 * ha + e2 * hb + e3 * hc);
+      F[g + 14 * N] = d5 * su3 + re * sm3 - (z1 * ha + z2 * hb + z3 * hc);
     });
   }
 }
