@@ -301,6 +301,12 @@ int ati_probe_fma_tflops(int fp64, double *tflops);
  * zeros, subnormals, infinities and NaNs, and returns how many results differ
  * (0 expected). */
 int ati_check_conversions(int64_t n, int64_t *mismatches);
+/* The FP64 fast build's primitives take 1/a and 1/sqrt(a) from hardware
+ * approximations refined by two Newton-Raphson steps; this evaluates both on
+ * n device-generated positive normal arguments (2^-200..2^200) and returns in
+ * worst[0] and worst[1] their largest relative differences from the IEEE
+ * division and square root (a few 2^-53 expected). */
+int ati_check_recip(int64_t n, double worst[2]);
 
 /* ---- allocation-free derivative (no counterpart in the reference) -------
  * For callers that must not allocate GPU memory when they call in: codes

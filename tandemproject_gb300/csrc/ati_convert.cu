@@ -1,10 +1,12 @@
 // ati_convert.cu — device check of the integer-pipe conversions (FP32 -> FP64
 // widening, FP64 -> FP32 rounding) against the conversion instruction, over bit
 // patterns that cover every exponent (normal, subnormal, zero, infinity, NaN) and
-// the rounding ties.
+// the rounding ties; and of the Newton-refined reciprocal and inverse square root
+// of the FP64 fast build against the IEEE division and square root.
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <string>
 
 #include "../../include/ati.h"
@@ -52,7 +54,51 @@ __global__ void k_check_conv(int64_t n, unsigned long long *bad) {
   if (nb) atomicAdd(bad, nb);
 }
 
+// recip_nr / rsqrt_nr against the IEEE division and square root, positive normal arguments over 2^-200..2^200:
+// the largest relative differences, as bit patterns of non-negative doubles (ordered like the values)
+__global__ void k_check_recip(int64_t n, unsigned long long *worst) {
+  double w0 = 0, w1 = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = mix64((uint64_t)i * 0x9E3779B97F4A7C15ull + 7);
+    const uint64_t ex = 1023 - 200 + (r >> 52) % 401;
+    const double a = __longlong_as_double((long long)((ex << 52) | (r & 0xfffffffffffffull)));
+    const double x = ati::recip_nr(a), xr = 1.0 / a;
+    const double y = ati::rsqrt_nr(a), yr = 1.0 / sqrt(a);
+    w0 = fmax(w0, fabs(x - xr) / xr);
+    w1 = fmax(w1, fabs(y - yr) / yr);
+  }
+  atomicMax(&worst[0], (unsigned long long)__double_as_longlong(w0));
+  atomicMax(&worst[1], (unsigned long long)__double_as_longlong(w1));
+}
+
 }  // namespace
+
+extern "C" int ati_check_recip(int64_t n, double worst[2]) {
+  if (n < 0 || !worst) {
+    ati_set_thread_error("ati_check_recip: bad argument");
+    return ATI_EINVAL;
+  }
+  unsigned long long *d = nullptr, h[2] = {0, 0};
+  cudaError_t e = cudaMalloc(&d, sizeof(h));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(h));
+  if (e == cudaSuccess && n > 0) {
+    k_check_recip<<<1024, 256>>>(n, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  if (e != cudaSuccess) {
+    ati_set_thread_error((std::string("ati_check_recip: ") + cudaGetErrorString(e)).c_str());
+    return ATI_ECUDA;
+  }
+  for (int k = 0; k < 2; k++) {
+    const long long b = (long long)h[k];
+    double v;
+    memcpy(&v, &b, sizeof v);
+    worst[k] = v;
+  }
+  return ATI_OK;
+}
 
 extern "C" int ati_check_conversions(int64_t n, int64_t *mismatches) {
   if (n < 0 || !mismatches) {

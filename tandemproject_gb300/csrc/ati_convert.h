@@ -42,6 +42,33 @@ __device__ __forceinline__ float narrow(double d) {
   return (float)d;
 }
 
+// 1/a and 1/sqrt(a) for the FP64 fast build, for positive normal a: the
+// hardware approximations (PTX rcp.approx.ftz.f64, rsqrt.approx.ftz.f64) refined
+// by two Newton-Raphson steps each, x' = x + x (1 - a x) and
+// y' = y + y (1 - a y^2) / 2, each of which squares the relative error.  The
+// results are within a few ulp of the correctly rounded ones (the bound is
+// checked against the division and the square root on the device by
+// ati_check_recip); they take about half the FP64 operations of the IEEE
+// division and square root.
+__device__ __forceinline__ double recip_nr(double a) {
+  double x;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(x) : "d"(a));
+  double e = fma(-a, x, 1.0);
+  x = fma(x, e, x);
+  e = fma(-a, x, 1.0);
+  return fma(x, e, x);
+}
+__device__ __forceinline__ double rsqrt_nr(double a) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    const double e = fma(-(a * y), y, 1.0);
+    y = fma(y, 0.5 * e, y);
+  }
+  return y;
+}
+
 // conversion between the engine types: FP32 -> FP64 on the integer pipes.  The
 // other direction stays with the conversion instruction here: rounding takes some
 // 15 integer operations and branches, slower in the line sweeps' load loops than

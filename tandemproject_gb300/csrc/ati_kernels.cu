@@ -1191,8 +1191,14 @@ __device__ __forceinline__ bool prim_point(const Eng<R> &e, const PrimConst<R> &
     if constexpr (Freestream<R>::on) return narrow(v);
     else return (R)v;
   };
+  // (the FP64 fast build takes its reciprocals and square root from recip_nr / rsqrt_nr: the kernel is bound
+  // by the FP64 pipe, and the IEEE division and square root are its largest users)
+  constexpr bool NR = kFast && !Freestream<R>::on;
   const R q1 = rnd(q[0]), q2 = rnd(q[1]), q3 = rnd(q[2]), q4 = rnd(q[3]);
-  const R d1 = (R)1 / q1, d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
+  R d1;
+  if constexpr (NR) d1 = recip_nr(q1);
+  else d1 = (R)1 / q1;
+  const R d2 = q2 * d1, d3 = q3 * d1, d4 = q4 * d1;
   R pp, d5;
   if constexpr (Freestream<R>::on) {
     // p - p_inf from rhoE - rhoE_inf (taken in FP64 before rounding); (gamma-1) rhoE_inf = p_inf
@@ -1205,7 +1211,9 @@ __device__ __forceinline__ bool prim_point(const Eng<R> &e, const PrimConst<R> &
     d5 = gam * pp * d1;
   }
   // T^1.5 as T*sqrt(T): the value of pow(T,1.5) to ~1 ulp with far fewer instructions
-  const R mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
+  R mu;
+  if constexpr (NR) mu = srefp1dre * (d5 * (d5 * rsqrt_nr(d5))) * recip_nr(d5 + srefoo);
+  else mu = srefp1dre * (d5 * sqrt(d5)) / (d5 + srefoo);
   e.prim[g] = d2; e.prim[g + N] = d3; e.prim[g + 2 * N] = d4; e.prim[g + 3 * N] = d5;
   e.p[g] = pp;
   e.mu[g] = mu;

@@ -78,6 +78,7 @@ SIGNATURES = {
     "ati_tiles": ([_vp, _vp], ctypes.c_int),
     "ati_set_tiles": ([_vp, _vp], ctypes.c_int),
     "ati_check_conversions": ([ctypes.c_int64, _vp], ctypes.c_int),
+    "ati_check_recip": ([ctypes.c_int64, _dp], ctypes.c_int),
     "ati_turbulence_modes": ([_vp, _i32, _vp, _vp], ctypes.c_int),
     "ati_turbulence_sample": ([_vp, _i32, ctypes.c_double, ctypes.c_int64, _dp, _dp], ctypes.c_int),
     "ati_query": ([_vp, _vp], ctypes.c_int),

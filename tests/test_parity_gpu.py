@@ -213,3 +213,17 @@ def test_naca0012_0p6m_hundred_steps(ati_lib, oracle_lib):
     e = state_errors(gpu, orc)
     print("naca0012_0p6m 100 steps rel L2", e)
     assert np.all(e < TOL_STEP), e
+
+
+def test_newton_reciprocal_and_rsqrt_bounds(ati_lib):
+    """The FP64 fast build's primitives take 1/rho, 1/(T + S) and 1/sqrt(T) from
+    hardware approximations refined by two Newton-Raphson steps; over 2^24
+    arguments they stay within 4 x 2^-53 of the IEEE division and square root."""
+    import ctypes
+    from tandemproject_gb300.solver import load_library
+    L = load_library(ati_lib)
+    worst = (ctypes.c_double * 2)(-1.0, -1.0)
+    assert L.ati_check_recip(1 << 24, worst) == 0
+    print("Newton reciprocal / rsqrt, worst relative difference", worst[0], worst[1])
+    assert 0.0 <= worst[0] <= 4 * 2.0 ** -53
+    assert 0.0 <= worst[1] <= 4 * 2.0 ** -53
