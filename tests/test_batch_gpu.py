@@ -84,14 +84,16 @@ def test_pinned_tiles_give_identical_states(ati_lib, precision):
     from tandemproject_gb300.config import small_case
     from tandemproject_gb300.solver import AtiError, setup_case
     cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), precision=precision)
-    a, b = setup_case(cfg), setup_case(cfg)
+    a, b, c = setup_case(cfg), setup_case(cfg), setup_case(cfg)  # c: the timed tiles, one size per pointwise kernel
     a.set_tiles(eta=32, zeta=256, points=256)
     b.set_tiles(eta=256, zeta=32, points=4096)
     assert a.tiles() == (64, 32, 256, 256) and b.tiles() == (64, 256, 32, 4096)
-    a.step(6)
-    b.step(6)
+    for h in (a, b, c):
+        h.step(6)
     for mb in range(6):
         np.testing.assert_array_equal(a.get_state(mb), b.get_state(mb))
+        np.testing.assert_array_equal(a.get_state(mb), c.get_state(mb))
+    c.close()
     with pytest.raises(AtiError):
         a.set_tiles(eta=48)
     with pytest.raises(AtiError):
