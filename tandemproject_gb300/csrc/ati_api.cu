@@ -55,7 +55,9 @@ struct ati_handle {
   bool any_cfl = false;  // some case takes its dt from the CFL condition (dto < 0)
   std::vector<PTile> hpt;
   std::vector<LTile> hlt[4];
-  std::vector<LTile> hlts[4];  // tiles of the segmented sweeps (mixed path), SEG_LINES lines each
+  std::vector<LTile> hlts[4];  // tiles of the segmented sweeps (mixed path), by class (segc)
+  SegClass segc[4][SEG_NCLASS] = {};
+  int nsegc[4] = {0, 0, 0, 0};
   size_t max_pt = 0, max_lt[4] = {0, 0, 0, 0};
   // point tiles of the candidate sizes (PT_CAND), uploaded once; pw_pt[kind] is a pointwise kernel's own timed
   // size (0: the shared queue of pt_points)
@@ -613,12 +615,33 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
   for (int nn = 1; nn <= 3; nn++) h->max_lt[nn] = h->hlt[nn].size();
   make_tiles(h, SG_DEFAULT, SG_DEFAULT, PT_DEFAULT);
   for (int nn = 1; nn <= 3; nn++) {
-    h->hlts[nn].clear();
-    const int step = SEG_LINES * seg_groups(h->maxlen[nn]);
-    for (int gb = 0; gb < h->nb; gb++)
-      for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += step) h->hlts[nn].push_back(LTile{gb, t0});
     if (h->mixed && h->maxlen[nn] > SEG_LMAX)
       return fail(h, ATI_EINVAL, "mixed precision: lines of up to " + std::to_string(SEG_LMAX) + " points");
+    // classes of the segmented sweeps: the distinct segment counts of the blocks' lines, ascending (beyond
+    // SEG_NCLASS the largest counts share the last class, whose CTAs then idle a warp for the shorter lines)
+    auto len = [&](const BlockDev &B) { return nn == 1 ? B.lxi + 1 : (nn == 2 ? B.let + 1 : B.lze + 1); };
+    std::vector<int> counts;
+    for (int gb = 0; gb < h->nb; gb++) counts.push_back(seg_count(len(h->blk[gb])));
+    std::sort(counts.begin(), counts.end());
+    counts.erase(std::unique(counts.begin(), counts.end()), counts.end());
+    auto cls = [&](int L) {
+      const int r = (int)(std::lower_bound(counts.begin(), counts.end(), seg_count(L)) - counts.begin());
+      return std::min(r, SEG_NCLASS - 1);
+    };
+    h->nsegc[nn] = std::min((int)counts.size(), SEG_NCLASS);
+    h->hlts[nn].clear();
+    for (int c = 0; c < h->nsegc[nn]; c++) {
+      SegClass C{(int)h->hlts[nn].size(), 0, 0, 1};
+      for (int gb = 0; gb < h->nb; gb++)
+        if (cls(len(h->blk[gb])) == c) C.maxlen = std::max(C.maxlen, len(h->blk[gb]));
+      C.groups = seg_groups(C.maxlen);
+      for (int gb = 0; gb < h->nb; gb++) {
+        if (cls(len(h->blk[gb])) != c) continue;
+        for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += SEG_LINES * C.groups) h->hlts[nn].push_back(LTile{gb, t0});
+      }
+      C.n = (int)h->hlts[nn].size() - C.off;
+      h->segc[nn][c] = C;
+    }
   }
   return ATI_OK;
 }
@@ -872,8 +895,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     m.facd = Fp(o_ffacd); m.facf = Fp(o_ffacf); m.sbcc = Fp(o_fsbcc); m.rpex = Fp(o_frpex);
     for (int nn = 1; nn <= 3; nn++) {
       m.lts[nn] = (const LTile *)(h->arena + o_lts[nn]);
-      m.nlts[nn] = (int)h->hlts[nn].size();
-      m.seg_groups[nn] = seg_groups(h->maxlen[nn]);
+      m.nsegc[nn] = h->nsegc[nn];
+      for (int c = 0; c < SEG_NCLASS; c++) m.segc[nn][c] = h->segc[nn][c];
     }
     m.segd = Fp(o_segd) + SEG_PAD * SEG_RT; m.segf = Fp(o_segf) + SEG_PAD * SEG_RT;
   }

@@ -2224,16 +2224,20 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   if constexpr (std::is_same<TC, float>::value) {
     // the mixed path: segmented solves over tiles of SEG_LINES lines
     const float *seg = filt ? e.segf : e.segd;
-    if (seg && e.nlts[nn] > 0 && (filt || !io.out2)) {  // (a derivative with a second output: sequential kernels)
-      a.lt = e.lts[nn];
-      const int G = e.seg_groups[nn];
-      const int nt = SEG_LINES * (G > 1 ? G : seg_count(e.maxlen[nn]));
-      const size_t smem = seg_smem_bytes(e.maxlen[nn], G);
-      const dim3 g(e.nlts[nn], io.nf);
+    if (seg && e.nsegc[nn] > 0 && (filt || !io.out2)) {  // (a derivative with a second output: sequential kernels)
+      for (int c = 0; c < e.nsegc[nn]; c++) {  // one launch per class of equal segment counts
+        const SegClass &C = e.segc[nn][c];
+        if (C.n == 0) continue;
+        a.lt = e.lts[nn] + C.off;
+        const int G = C.groups;
+        const int nt = SEG_LINES * (G > 1 ? G : seg_count(C.maxlen));
+        const size_t smem = seg_smem_bytes(C.maxlen, G);
+        const dim3 g(C.n, io.nf);
 #define ATI_SEG(D, F) k_sweep_seg<D, F, TI, TO><<<g, nt, smem, st>>>(a, seg, G)
-      if (!filt) { if (nn == 1) ATI_SEG(1, false); else if (nn == 2) ATI_SEG(2, false); else ATI_SEG(3, false); }
-      else { if (nn == 1) ATI_SEG(1, true); else if (nn == 2) ATI_SEG(2, true); else ATI_SEG(3, true); }
+        if (!filt) { if (nn == 1) ATI_SEG(1, false); else if (nn == 2) ATI_SEG(2, false); else ATI_SEG(3, false); }
+        else { if (nn == 1) ATI_SEG(1, true); else if (nn == 2) ATI_SEG(2, true); else ATI_SEG(3, true); }
 #undef ATI_SEG
+      }
       return;
     }
   }

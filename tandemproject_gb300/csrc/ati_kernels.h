@@ -30,6 +30,14 @@ struct Coef {
 // kinds of pointwise kernel (the PW_ enumeration)
 constexpr int PW_KINDS = 7;
 
+// The segmented sweeps' tiles of one direction fall into classes of blocks whose lines have the same segment
+// count (a batch mixes line lengths): one launch per class, with the warps and shared memory of the class's
+// longest line.  A class is tiles [off, off + n) of lts, lines of up to maxlen points, groups line groups a CTA.
+struct SegClass {
+  int off, n, maxlen, groups;
+};
+constexpr int SEG_NCLASS = 8;  // classes per direction (more distinct segment counts share the last class)
+
 template <typename R>
 struct Eng {
   const BlockDev *blk;
@@ -41,9 +49,9 @@ struct Eng {
   int npt;
   const LTile *lt[4];   // line-sweep work queue per direction nn = 1..3
   int nlt[4];
-  const LTile *lts[4];  // segmented sweeps (mixed path): SEG_LINES x seg_groups lines per tile, per direction
-  int nlts[4];
-  int seg_groups[4];    // line groups per CTA of a segmented sweep (> 1 when every line is one segment)
+  const LTile *lts[4];  // segmented sweeps (mixed path): SEG_LINES x groups lines per tile, per direction, by class
+  SegClass segc[4][SEG_NCLASS];
+  int nsegc[4];
   const float *segd, *segf;  // their row tables (SEG_RT floats per factor row; derivative, filter)
   const double *facud, *facuf;  // FP64 fast path: scaled-factor row tables (FU_RT per row; derivative, filter)
   int sg_lines[4];      // lines per CTA of the eta (2) and zeta (3) sweeps: the tiles of lt[2], lt[3]
