@@ -51,7 +51,7 @@ SWEEP_FLOPS = {"deriv": 17, "filter": 22}
 # and writes the FP64 state
 SWEEP_BYTES_MIXED = {"deriv": 8, "filter": 16}
 # algorithmic bytes per point of the mixed path's pointwise kernels: the viscous
-# flux kernel k_flux<float, stress> reads the FP64 state (40 B), the FP32
+# flux kernel k_flux_staged reads the FP64 state (40 B), the FP32
 # metrics (36 B), the twelve derivative planes of u, v, w, T (48 B), Jacobian,
 # viscosity, velocity and pressure (24 B) and writes 15 FP32 fluxes (60 B); it
 # takes the stresses at the point, so no stress plane is written or read
@@ -377,7 +377,7 @@ def main():
         elif mdom in POINTWISE_BYTES_MIXED:
             mt = mprof[mdom][0] / max(mprof[mdom][1], 1) / 1e3
             mach = POINTWISE_BYTES_MIXED[mdom] * npts / mt / 1e9
-            mroof = {"bound": "hbm", "kernel": f"k_{mdom}<float, stress>, {POINTWISE_BYTES_MIXED[mdom]} B per point",
+            mroof = {"bound": "hbm", "kernel": f"k_flux_staged (viscous fluxes, stresses at the point), {POINTWISE_BYTES_MIXED[mdom]} B per point",
                      "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
                      "frac": mach / measured_peaks()[0]}
         else:
