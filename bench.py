@@ -374,10 +374,11 @@ def main():
             mroof = {"bound": "hbm", "kernel": f"k_sweep<{mdom}> in FP32, {SWEEP_BYTES_MIXED[mkind]} B per point-field",
                      "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
                      "frac": mach / measured_peaks()[0]}
-        elif mdom in POINTWISE_BYTES_MIXED:
+        elif mdom in POINTWISE_BYTES_MIXED and cfg.nviscous == 1:
             mt = mprof[mdom][0] / max(mprof[mdom][1], 1) / 1e3
             mach = POINTWISE_BYTES_MIXED[mdom] * npts / mt / 1e9
-            mroof = {"bound": "hbm", "kernel": f"k_flux_staged (viscous fluxes, stresses at the point), {POINTWISE_BYTES_MIXED[mdom]} B per point",
+            mroof = {"bound": "hbm", "kernel": "k_flux_staged (viscous fluxes, stresses at the point), "
+                                               f"{POINTWISE_BYTES_MIXED[mdom]} B per point",
                      "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
                      "frac": mach / measured_peaks()[0]}
         else:
