@@ -247,6 +247,21 @@ int ati_step(ati_handle_t *h, int nsteps);
 int ati_step_async(ati_handle_t *h, int nsteps);
 int ati_query(ati_handle_t *h, int *idle);
 int ati_check(ati_handle_t *h);
+/* Failure detection (the reference's only check is the dt = 0 "Overflow."
+ * stop, src/Main3D.f90:1086-1090).  Every case of a handle has its own device
+ * flag, set by the primitives kernel for a NaN/Inf or non-positive density or
+ * pressure, by the CFL maxima or by a non-finite dt; it stays set until
+ * ati_init.  Cases of a batch share no data on the device, so a case that
+ * fails keeps stepping (its state stays non-finite) while the others go on
+ * unchanged: ati_step and ati_check name the first failed case, and
+ * ati_case_check returns ATI_ENONFINITE for case cs alone if it failed. */
+int ati_case_check(ati_handle_t *h, int cs);
+/* Bounded host waits (no counterpart in the reference): with seconds > 0,
+ * ati_synchronize, ati_step, ati_check and ati_case_check poll the handle's
+ * stream and give up after that long with ATI_ETIMEDOUT, the work still in
+ * flight (a later wait picks it up); 0 (the default) waits without limit.
+ * The ati_get_* copies always wait without limit. */
+int ati_set_wait_timeout(ati_handle_t *h, double seconds);
 
 /* ---- instrumentation (no counterpart in the reference) ------------------
  * With profiling enabled every kernel launch of the handle is bracketed by
@@ -315,22 +330,34 @@ int ati_check_recip(int64_t n, double worst[2]);
  * device or fail late).  Computes the compact first derivative of nlines
  * contiguous lines of len points each, in -> out (both caller-owned device
  * arrays, line t at offset t*len), with the one-sided boundary rows at both
- * ends -- the result ati_deriv gives along xi on blocks whose xi faces are
- * boundaries or interfaces, bit for bit -- asynchronously on `stream`
- * (a cudaStream_t; NULL = the legacy default stream).
+ * ends -- the result ati_deriv gives along xi on blocks whose two xi faces
+ * have ndf = 0 (boundary codes 10, 20, 25 and 30), bit for bit; faces with
+ * codes 35, 40 or 45 (ndf = 1) take closure rows instead and differ --
+ * asynchronously on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream).
  *  - Allocates and frees nothing.  Its scratch (LU factors and the
  *    forward-elimination values) is one static device array of
- *    5*ATI_NOALLOC_MAX_LEN + ATI_NOALLOC_MAX_POINTS doubles (about 16 MB),
- *    reserved on every GPU that loads this library until the process exits.
+ *    5*ATI_NOALLOC_MAX_LEN + ATI_NOALLOC_MAX_POINTS doubles (about 16 MB)
+ *    per GPU, held until the process exits.
+ *  - The first call on each device (and again after a device reset, which
+ *    gives the context a new array) looks up the array's device address with
+ *    cudaGetSymbolAddress, that device current.  Under CUDA's default lazy
+ *    module loading that look-up is also when the driver loads the module and
+ *    reserves the 16 MB, so the first call can fail with ATI_ECUDA on a device
+ *    with no room left: make one call (nlines may be 1) before a memory pool
+ *    takes the device's memory and before any stream capture, or set
+ *    CUDA_MODULE_LOADING=EAGER so that the array is reserved when the context
+ *    is created.
  *  - Rejects len outside 7..ATI_NOALLOC_MAX_LEN and nlines*len above
- *    ATI_NOALLOC_MAX_POINTS with ATI_EINVAL (text in ati_last_error(NULL)).
- *  - The first call on each device looks up the scratch array's device
- *    address (cudaGetSymbolAddress) with that device current; make that
- *    first call before any stream capture.
+ *    ATI_NOALLOC_MAX_POINTS with ATI_EINVAL (text in ati_last_error(NULL)),
+ *    and, without launching anything, a CUDA error already pending from
+ *    earlier work with ATI_ECUDA (that error is left pending).
  *  - All calls share the one scratch array and it keeps the previous call's
- *    contents; every value a call reads was written by the same call, so
- *    nothing needs clearing, but calls that overlap on the GPU (different
- *    streams, no ordering between them) race on it and must not be issued. */
+ *    contents: the LU factors depend only on len and are refactored when len
+ *    differs from the previous call's, and every other value a call reads it
+ *    wrote itself, so nothing needs clearing.  Calls must therefore be
+ *    ordered on the GPU: calls that overlap (different streams, no ordering
+ *    between them) race on the array and must not be issued. */
 #define ATI_NOALLOC_MAX_POINTS 2000000
 #define ATI_NOALLOC_MAX_LEN 4096
 int ati_deriv_lines_noalloc(const double *in, double *out, int64_t nlines, int32_t len, void *stream);

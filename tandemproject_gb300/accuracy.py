@@ -25,14 +25,20 @@ def rel_l2(a, b):
 
 
 def wall_psd(t, p):
-    """Mean PSD over wall points of p(t) resampled onto a uniform time grid
-    (the CFL time step varies), mean removed, Hann window."""
+    """One-sided power spectral density of the wall pressure, averaged over the
+    wall points: p[r, i] at times t[r] (the CFL time step varies, so each
+    point's series is first resampled linearly onto a uniform grid of the same
+    length), mean removed, Hann window.  Normalised so that the sum of psd * df
+    over the returned frequencies equals the variance of the windowed series
+    (a sinusoid of amplitude A gives A^2 / 2).  Returns (freq, psd)."""
     n = len(t)
     tu = np.linspace(t[0], t[-1], n)
     pu = np.stack([np.interp(tu, t, p[:, i]) for i in range(p.shape[1])], axis=1)
     pu = pu - pu.mean(axis=0)
     w = np.hanning(n)[:, None]
     spec = np.abs(np.fft.rfft(pu * w, axis=0)) ** 2
+    # one-sided: every bin but zero frequency (and Nyquist, for even n) stands for its negative twin too
+    spec[1:n - n // 2] *= 2.0
     dtu = (tu[-1] - tu[0]) / max(n - 1, 1)
     freq = np.fft.rfftfreq(n, dtu)
     return freq, spec.mean(axis=1) * dtu / (w ** 2).sum()

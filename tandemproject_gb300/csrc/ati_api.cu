@@ -13,10 +13,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -97,6 +99,7 @@ struct ati_handle {
   // instrumentation
   int64_t launches = 0;
   bool profiling = false;
+  double wait_timeout = 0.0;  // seconds a host wait may take (0: unbounded)
   struct Ev {
     cudaEvent_t a, b;
     int cls;
@@ -1024,9 +1027,34 @@ extern "C" int ati_destroy(ati_handle_t *h) {
   return ATI_OK;
 }
 
+// Waits for the handle's stream: unbounded by default, or polling until the handle's wait limit, after which it
+// returns ATI_ETIMEDOUT with the work still in flight (a later wait picks it up; nothing is cancelled).
+static int wait_stream(ati_handle *h) {
+  if (h->wait_timeout <= 0.0) {
+    CK(cudaStreamSynchronize(h->st));
+    return ATI_OK;
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    const cudaError_t e = cudaStreamQuery(h->st);
+    if (e == cudaSuccess) return ATI_OK;
+    if (e != cudaErrorNotReady) return fail(h, ATI_ECUDA, std::string("cudaStreamQuery: ") + cudaGetErrorString(e));
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (dt >= h->wait_timeout)
+      return fail(h, ATI_ETIMEDOUT, "the handle's work did not finish within the wait limit of " +
+                                        std::to_string(h->wait_timeout) + " s (still in flight)");
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+}
+
 extern "C" int ati_synchronize(ati_handle_t *h) {
   if (!h) return ATI_EINVAL;
-  CK(cudaStreamSynchronize(h->st));
+  return wait_stream(h);
+}
+
+extern "C" int ati_set_wait_timeout(ati_handle_t *h, double seconds) {
+  if (!h || !(seconds >= 0.0)) return fail(h, ATI_EINVAL, "ati_set_wait_timeout: bad argument");
+  h->wait_timeout = seconds;
   return ATI_OK;
 }
 
@@ -1740,14 +1768,34 @@ static int one_step(ati_handle *h) {
   return ATI_OK;
 }
 
-static int check_flag(ati_handle *h) {
-  std::vector<Scalars> sc(h->ncase);
+// The failure flags of every case, after the handle's work in flight (a bounded wait when the handle has a wait
+// limit: the copy is issued only once the stream is idle, so a timed-out wait leaves no copy behind).
+static int read_flags(ati_handle *h, std::vector<Scalars> &sc) {
+  if (int rc = wait_stream(h)) return rc;
+  sc.resize(h->ncase);
   CK(cudaMemcpyAsync(sc.data(), h->ed.scal, sizeof(Scalars) * h->ncase, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
+  return ATI_OK;
+}
+
+static int check_flag(ati_handle *h) {
+  std::vector<Scalars> sc;
+  if (int rc = read_flags(h, sc)) return rc;
   for (int c = 0; c < h->ncase; c++)
     if (sc[c].flag)
       return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state of case " +
                                          std::to_string(c) + " (flag " + std::to_string(sc[c].flag) + ")");
+  return ATI_OK;
+}
+
+extern "C" int ati_case_check(ati_handle_t *h, int cs) {
+  if (!h || cs < 0 || cs >= h->ncase) return fail(h, ATI_EINVAL, "ati_case_check: bad argument");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
+  std::vector<Scalars> sc;
+  if (int rc = read_flags(h, sc)) return rc;
+  if (sc[cs].flag)
+    return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state of case " +
+                                       std::to_string(cs) + " (flag " + std::to_string(sc[cs].flag) + ")");
   return ATI_OK;
 }
 

@@ -7,9 +7,17 @@
 // when memory is fragmented).  ati_deriv_lines_noalloc serves them: the
 // caller passes its own input and output arrays, and the only extra memory
 // the kernel needs -- the LU factor table and the forward-elimination values
-// -- lives in the file-scope device array below, which the CUDA driver reserves
-// when the library is loaded (about 16 MB on every GPU that loads it, held
-// until the process exits).  No call allocates or frees anything.
+// -- lives in the file-scope device array below (about 16 MB on every GPU that
+// uses it, held until the process exits).  No call allocates or frees anything.
+//
+// When the array is reserved: with CUDA's default lazy module loading this file's
+// module, and the array with it, is loaded into a context the first time the
+// module is used there, which is the first call's address look-up.  That first
+// call on a device therefore reserves the 16 MB, and it fails with ATI_ECUDA if
+// the device has no 16 MB left.  A caller whose own pool takes the device memory
+// makes one call (nlines may be 1) before the pool does, and before any stream
+// capture; with CUDA_MODULE_LOADING=EAGER in the environment the driver reserves
+// the array when the context is created instead.
 //
 // Arithmetic: the same one-sided compact scheme as deriv on a line whose two
 // ends are physical or interface boundaries (src/Subroutines3D.f90:84-141
@@ -20,6 +28,7 @@
 
 #include <cstdint>
 #include <mutex>
+#include <string>
 
 #include "../../include/ati.h"
 
@@ -151,7 +160,34 @@ __global__ void k_noalloc_deriv(const double *in, double *out, int64_t nlines, i
 }
 
 std::mutex g_mu;
-void *g_ptr[64] = {nullptr};  // device address of the scratch array, per device
+// per device: the scratch array's device address, the context it was looked up in, and the line length whose
+// LU factors the array holds (-1: none)
+void *g_ptr[64] = {nullptr};
+void *g_ctx[64] = {nullptr};
+int g_len[64];
+bool g_len_init = false;
+
+// cuCtxGetCurrent from the driver, fetched through the runtime (no link-time dependency on libcuda): a device
+// reset or a new primary context reloads the module, and the array may then sit at another address
+using CtxGetCurrent = int (*)(void **);
+CtxGetCurrent ctx_get_current() {
+  static CtxGetCurrent fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (CtxGetCurrent) nullptr;
+    return (CtxGetCurrent)p;
+  }();
+  return fn;
+}
+void *current_ctx() {
+  void *c = nullptr;
+  if (CtxGetCurrent f = ctx_get_current()) {
+    if (f(&c) != 0) c = nullptr;
+  }
+  return c;
+}
 
 Rows make_rows() {
   // interior and one-sided boundary coefficients (src/MainVar3D.f90:34-68,
@@ -195,31 +231,52 @@ extern "C" int ati_deriv_lines_noalloc(const double *in, double *out, int64_t nl
     ati_set_thread_error("ati_deriv_lines_noalloc: no current CUDA device");
     return ATI_ECUDA;
   }
+  // an error left pending by earlier, unrelated work is reported as such and left in place
+  if (cudaError_t pe = cudaPeekAtLastError(); pe != cudaSuccess) {
+    ati_set_thread_error((std::string("ati_deriv_lines_noalloc: a CUDA error from earlier work is pending "
+                                      "(not cleared, nothing launched): ") + cudaGetErrorString(pe)).c_str());
+    return ATI_ECUDA;
+  }
   void *base = nullptr;
+  bool refactor = false;
   {
-    // first call on this device: look up the device address of the scratch
-    // array (host code must not use the symbol itself as a device pointer)
+    // set-up, once per device and context: look up the device address of the scratch array with that device
+    // current (in host code the symbol itself is only a host-side stand-in, not a device address)
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_ptr[dev]) {
+    if (!g_len_init) {
+      for (int q = 0; q < 64; q++) g_len[q] = -1;
+      g_len_init = true;
+    }
+    void *ctx = current_ctx();
+    if (!g_ptr[dev] || !ctx || ctx != g_ctx[dev]) {
       void *p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p) {
-        ati_set_thread_error("ati_deriv_lines_noalloc: cudaGetSymbolAddress of the scratch array failed");
+        ati_set_thread_error((std::string("ati_deriv_lines_noalloc: cudaGetSymbolAddress of the scratch array "
+                                          "failed: ") + cudaGetErrorString(e)).c_str());
         return ATI_ECUDA;
       }
+      if (p != g_ptr[dev]) g_len[dev] = -1;  // a new array: no factors yet
       g_ptr[dev] = p;
+      g_ctx[dev] = current_ctx();
     }
     base = g_ptr[dev];
+    refactor = g_len[dev] != len;
+    g_len[dev] = len;
   }
   double *fac = (double *)base;
   double *fw = fac + 5 * (int64_t)kMaxLen;
   cudaStream_t st = (cudaStream_t)stream;
   const Rows R = make_rows();
-  k_noalloc_factors<<<1, 1, 0, st>>>(fac, len, R);
+  // the LU factors depend on the line length only: refactored when it changes (calls are ordered on the GPU, so
+  // a call finds the factors of the previous call in the array)
+  if (refactor) k_noalloc_factors<<<1, 1, 0, st>>>(fac, len, R);
   const int tpb = 128;
   k_noalloc_deriv<<<(unsigned)((nlines + tpb - 1) / tpb), tpb, 0, st>>>(in, out, nlines, len, fac, fw, R);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_len[dev] = -1;
     ati_set_thread_error(cudaGetErrorString(e));
     return ATI_ECUDA;
   }

@@ -83,6 +83,8 @@ SIGNATURES = {
     "ati_turbulence_sample": ([_vp, _i32, ctypes.c_double, ctypes.c_int64, _dp, _dp], ctypes.c_int),
     "ati_query": ([_vp, _vp], ctypes.c_int),
     "ati_check": ([_vp], ctypes.c_int),
+    "ati_case_check": ([_vp, _i32], ctypes.c_int),
+    "ati_set_wait_timeout": ([_vp, ctypes.c_double], ctypes.c_int),
     "ati_case_count": ([_vp, _vp], ctypes.c_int),
     "ati_case_blocks": ([_vp, _i32, _vp, _vp], ctypes.c_int),
     "ati_case_time": ([_vp, _i32, _vp], ctypes.c_int),
@@ -303,6 +305,10 @@ class Case:
     def synchronize(self):
         self._chk(self.L.ati_synchronize(self.h))
 
+    def set_wait_timeout(self, seconds):
+        """Bound the host waits of synchronize / step / check (0: no limit)."""
+        self._chk(self.L.ati_set_wait_timeout(self.h, float(seconds)))
+
     def profile(self, enable=True):
         """Bracket every launch with CUDA events on the case's stream."""
         self._chk(self.L.ati_profile_enable(self.h, 1 if enable else 0))
@@ -403,6 +409,10 @@ class Batch(Case):
         t = AtiTime()
         self._chk(self.L.ati_case_time(self.h, cs, ctypes.byref(t)))
         return t.as_tuple()
+
+    def case_check(self, cs):
+        """Raise AtiError (ATI_ENONFINITE) if case cs of the batch has failed."""
+        self._chk(self.L.ati_case_check(self.h, cs))
 
     def case_forces(self, cs):
         out = np.zeros(2)

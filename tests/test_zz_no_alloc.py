@@ -1,13 +1,18 @@
 """The allocation-free derivative entry point (ati_deriv_lines_noalloc).
 
-It exists for callers that cannot allocate GPU memory when they call in (a
-host code that owns all device memory through its own pool, or a running
-time loop that must not allocate).  Its scratch is a fixed static device
-array; the caller passes its own input and output arrays.  This test calls it
-through the C ABI twice in a row, on lines of two different lengths, and
-checks each result against the handle-based ati_deriv along xi, which runs
-the same arithmetic: the tolerance is the per-call parity bound 1e-12 (the
-two agree bit for bit).  This file is collected last on purpose.
+Some callers of this library cannot allocate GPU memory when they call in: a
+host code that hands all device memory to its own pool at start-up, or a time
+loop that must not allocate once it runs (an allocation can stall the device
+or fail late).  This entry point serves them: its scratch is one fixed static
+device array and the caller passes its own input and output arrays.
+
+The test calls it through the C ABI four times in a row, on lines of two
+lengths (the last call repeats the previous length, so it reuses the LU
+factors that call left in the scratch array), and checks every result against
+the handle-based ati_deriv along xi, which runs the same arithmetic: the
+tolerance is the per-call parity bound 1e-12 (the two agree bit for bit).  It
+also checks that calls after the first leave the device's free memory
+unchanged.  This file is collected last on purpose.
 """
 import ctypes
 
@@ -21,7 +26,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-12
 
 
-def test_noalloc_matches_deriv_two_calls(ati_lib):
+def test_noalloc_matches_deriv_consecutive_calls(ati_lib):
     import torch
 
     from tandemproject_gb300.config import small_case
@@ -44,12 +49,19 @@ def test_noalloc_matches_deriv_two_calls(ati_lib):
     case.deriv(1, 1, 1)  # the handle-based entry point: d/dxi of rr(:,1) into rr(:,1)
     expected = [case.get_field(mb, 3)[0] for mb in range(cfg.nblocks)]
     stream = torch.cuda.current_stream()
-    # two calls in a row on blocks with different xi lengths (25 and 65 points)
-    for mb in (0, 1, 0):
+    # every device array of the test is made before the first call, so free memory can only change through the calls
+    order = (0, 1, 0, 0)  # xi lengths 25, 65, 25, 25
+    bufs = {}
+    for mb in set(order):
+        din = torch.from_numpy(inputs[mb]).cuda()
+        bufs[mb] = (din, torch.empty_like(din))
+    torch.cuda.synchronize()
+    free_after_first = None
+    for n, mb in enumerate(order):
         lxi, let, lze, npts = case.dims[mb]
         nlines, ln = (let + 1) * (lze + 1), lxi + 1
-        din = torch.from_numpy(inputs[mb]).cuda()
-        dout = torch.full_like(din, float("nan"))
+        din, dout = bufs[mb]
+        dout.fill_(float("nan"))
         torch.cuda.synchronize()
         rc = L.ati_deriv_lines_noalloc(ctypes.c_void_p(din.data_ptr()), ctypes.c_void_p(dout.data_ptr()),
                                        nlines, ln, ctypes.c_void_p(stream.cuda_stream))
@@ -57,7 +69,12 @@ def test_noalloc_matches_deriv_two_calls(ati_lib):
         torch.cuda.synchronize()
         got = dout.cpu().numpy()
         e = rel_err(got, expected[mb])
-        assert e <= TOL, (mb, e)
+        assert e <= TOL, (n, mb, e)
+        free = torch.cuda.mem_get_info()[0]
+        if n == 0:
+            free_after_first = free
+        else:
+            assert free == free_after_first, (n, free, free_after_first)
     case.close()
 
 
