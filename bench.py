@@ -14,10 +14,11 @@ buffers (pinned host -> device copy of the state and device -> host copy of
 the result inside every step), the roofline of the dominant kernel measured
 live from profiled launches, a CPU baseline (the CPU restatement of the
 reference, all host cores, bounded sample), clocks sampled during the timed
-region and the number of kernel launches.  Sub-objects report the same case
-in mixed precision ("mixed"), 16 independent cases in one batched handle
-("batch") and a serving run with Poisson arrivals and p50/p95/p99 latency
-("serving").  Under torchrun every rank runs an
+region and the number of kernel launches.  Sub-objects report the mixed-
+precision path on its own configuration, the 24.6 M-point case, beside an
+FP64 run of the same case ("mixed"); 16 independent cases in one batched
+handle for 500 steps ("batch"); and serving runs of the FP64 and the mixed
+path with Poisson arrivals and p50/p95/p99 latency ("serving").  Under torchrun every rank runs an
 independent replica of the case (the path has no exchange between GPUs);
 value is the sum over ranks divided by the slowest rank's time.
 
@@ -135,6 +136,21 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+def _oracle_turbulence(o, cfg):
+    """The case's inflow turbulence on the oracle (the same mode table, summed in FP64); a note for the sample."""
+    from oracle import oracle as orc
+    modes = orc.build_modes(cfg)
+    if not modes.size:
+        return ""
+    o.set_turbulence(modes)
+    return f"; with the same inflow turbulence ({modes.shape[0]} modes, summed in FP64)"
+
+
+def _oracle_flags():
+    from oracle import build as ob
+    return ob.CFLAGS
+
+
 def cpu_baseline(cfg, grid, sample_steps=2, warm_steps=1):
     """The CPU restatement of the reference, all host threads, on the same case."""
     from oracle import oracle as orc
@@ -142,6 +158,7 @@ def cpu_baseline(cfg, grid, sample_steps=2, warm_steps=1):
     for mb in range(cfg.nblocks):
         o.set_grid(mb, grid[mb])
     o.init()
+    turb = _oracle_turbulence(o, cfg)
     o.step(warm_steps)
     t0 = time.perf_counter()
     o.step(sample_steps)
@@ -151,8 +168,7 @@ def cpu_baseline(cfg, grid, sample_steps=2, warm_steps=1):
     return {"value": cfg.npoints * cfg.nkrk * sample_steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{sample_steps} time steps ({sample_steps * cfg.nkrk} RK stages) of the full "
                       f"{cfg.npoints}-point case after {warm_steps} warm-up step, CPU restatement (oracle/), "
-                      f"OpenMP over lines, {cores} threads; the restatement has no inflow turbulence (new code "
-                      f"without a reference counterpart), so its inflow sponge targets rest"}
+                      f"OpenMP over lines, {cores} threads, gcc {' '.join(_oracle_flags())}{turb}"}
 
 
 def run_reference(args, cfg, grid):
@@ -162,6 +178,7 @@ def run_reference(args, cfg, grid):
     for mb in range(cfg.nblocks):
         o.set_grid(mb, grid[mb])
     o.init()
+    turb = _oracle_turbulence(o, cfg)
     t0 = time.perf_counter()
     o.step(args.warmup)
     t_warm = (time.perf_counter() - t0) / max(args.warmup, 1)
@@ -182,8 +199,8 @@ def run_reference(args, cfg, grid):
             "config": {"workload": args.preset, "points": cfg.npoints},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{k} time steps of the full case after {args.warmup} warm-up steps "
-                                       f"(CPU restatement of the reference; the Fortran reference has no compiler "
-                                       f"here)"},
+                                       f"(CPU restatement of the reference, gcc {' '.join(_oracle_flags())}; the "
+                                       f"Fortran reference has no compiler here){turb}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     o.close()
     return line
@@ -191,8 +208,9 @@ def run_reference(args, cfg, grid):
 
 def batch_leg(args, barrier):
     """The batched form: 16 independent cases (seed 7; NACA 00tt, t in 8-18 %, AoA 0-8 deg, M 0.2-0.4, inflow
-    turbulence 0-5 %, 1-6 M points each, spanwise 16-48) in one handle, mixed precision; against the same cases run
-    one handle at a time."""
+    turbulence 0-5 %, 1-6 M points each, spanwise 16-48) in one handle, mixed precision, args.batch_steps steps
+    (500, the batched configuration's step count); against the same cases run one handle at a time for
+    args.batch_seq_steps steps each (the per-step time is steady, so fewer steps measure it)."""
     import torch
     from tandemproject_gb300.solver import Case, setup_batch
     from tandemproject_gb300.workloads import batch_cases, fold_free_case
@@ -211,14 +229,16 @@ def batch_leg(args, barrier):
     l0 = b.launch_count()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
-    b.step(args.steps)
+    b.step(args.batch_steps)
     e1.record(st)
     barrier()
     t_b = e0.elapsed_time(e1) / 1e3
     launches = b.launch_count() - l0
+    for cs in range(len(cfgs)):
+        b.case_check(cs)
     b.close()
-    # the same cases, one handle at a time, same steps
-    t_seq = 0.0
+    # the same cases, one handle at a time
+    t_seq, ks = 0.0, args.batch_seq_steps
     for cfg, (_, g) in zip(cfgs, cg):
         c = Case(cfg)
         for mb in range(cfg.nblocks):
@@ -229,31 +249,44 @@ def batch_leg(args, barrier):
         barrier()
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a0.record(s1)
-        c.step(args.steps)
+        c.step(ks)
         a1.record(s1)
         barrier()
         t_seq += a0.elapsed_time(a1) / 1e3
         c.close()
-    return {"workload": "16 cases, seed 7: NACA 00tt t 8-18 %, AoA 0-8 deg, M 0.2-0.4, 1-6 M points (uneven), "
-                        "spanwise 16-48, mixed precision, one handle (ati_create_batch)",
-            "points": npts, "value": npts * 4 * args.steps / t_b, "unit": UNIT, "ms_per_step": t_b / args.steps * 1e3,
-            "gpu_launches_per_step": launches / args.steps,
-            "one_case_at_a_time": {"value": npts * 4 * args.steps / t_seq, "ms_per_step": t_seq / args.steps * 1e3},
-            "batching_speedup": t_seq / t_b,
+    v_b = npts * 4 * args.batch_steps / t_b
+    v_s = npts * 4 * ks / t_seq
+    return {"workload": f"16 cases, seed 7: NACA 00tt t 8-18 %, AoA 0-8 deg, M 0.2-0.4, 1-6 M points (uneven), "
+                        f"spanwise 16-48, mixed precision, one handle (ati_create_batch), {args.batch_steps} steps "
+                        f"after {args.warmup} warm-up steps",
+            "points": npts, "steps": args.batch_steps, "value": v_b, "unit": UNIT,
+            "ms_per_step": t_b / args.batch_steps * 1e3,
+            "gpu_launches_per_step": launches / args.batch_steps,
+            "one_case_at_a_time": {"value": v_s, "ms_per_step": t_seq / ks * 1e3, "steps_each": ks},
+            "batching_speedup": v_b / v_s,
             "note": "each case has von Karman inflow turbulence of its drawn intensity (2048 modes, L = 0.1 c)"}
 
 
 def serve_leg(args):
     """The serving form: Poisson arrivals (4/s, seed 99), sizes log-uniform 0.5-20 M points, admitted by device
-    footprint under a 150 GB budget, mixed precision; step counts U[200,2000] scaled to keep the run short."""
+    footprint, for the FP64 and the mixed path on the same request list.  Step counts U[200,2000] are scaled by
+    args.serve_step_scale and the budget is args.serve_budget_gb, both named in the workload: at full step counts
+    the run takes many minutes (a separate record), and at a tenth of them a 150 GB budget never binds, so the
+    bench's budget is the one under which admission holds requests back."""
+    from tandemproject_gb300.config import FP64, MIXED
     from tandemproject_gb300.serve import Server
     from tandemproject_gb300.workloads import serving_requests
-    reqs = serving_requests(args.serve_requests, seed=99, rate=4.0, step_scale=args.serve_step_scale)
-    done, summary = Server(budget_bytes=150 << 30).run(reqs)
-    summary["workload"] = (f"{args.serve_requests} requests, seed 99, Poisson 4/s, 0.5-20 M points log-uniform, "
-                           f"steps U[200,2000] x {args.serve_step_scale}, 150 GB budget, mixed precision")
-    summary["unit_latency"] = "s"
-    return summary
+    out = {}
+    for name, prec in (("mixed", MIXED), ("fp64", FP64)):
+        reqs = serving_requests(args.serve_requests, seed=99, rate=4.0, step_scale=args.serve_step_scale,
+                                precision=prec)
+        done, summary = Server(budget_bytes=int(args.serve_budget_gb * 2 ** 30)).run(reqs)
+        summary["workload"] = (f"{args.serve_requests} requests, seed 99, Poisson 4/s, 0.5-20 M points log-uniform, "
+                               f"steps U[200,2000] x {args.serve_step_scale}, {args.serve_budget_gb:g} GB budget, "
+                               f"{name}")
+        summary["unit_latency"] = "s"
+        out[name] = summary
+    return out
 
 
 def main():
@@ -268,8 +301,12 @@ def main():
     ap.add_argument("--no-mixed", dest="mixed", action="store_false")
     ap.add_argument("--no-batch", dest="batch", action="store_false")
     ap.add_argument("--no-serve", dest="serve", action="store_false")
-    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-step-scale", type=float, default=0.1)
+    ap.add_argument("--serve-budget-gb", type=float, default=40.0)
+    ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--batch-seq-steps", type=int, default=40)
+    ap.add_argument("--mixed-preset", default="naca0012_25m")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -330,34 +367,43 @@ def main():
         t_dev = float(tt.item())
     value = npts * cfg.nkrk * args.steps * ws / t_dev
 
-    # the mixed-precision path on the same workload, from the same start
+    # the mixed-precision path on the configuration it is quoted on (24.6 M points, 6 blocks 640 x 200 x 32), with
+    # an FP64 run of the same case for the error and the FP64-vs-mixed speed-up on that case
     from tandemproject_gb300.config import MIXED
     mixed = None
     if args.mixed:
-        cm = Case(cfg.replace(precision=MIXED))
-        for mb in range(cfg.nblocks):
-            cm.set_grid(mb, grid[mb])
-        cm.init()
-        cm.step(args.warmup)
-        barrier()
-        sm = torch.cuda.ExternalStream(cm.stream())
-        m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        m0.record(sm)
-        cm.step(args.steps)
-        m1.record(sm)
-        barrier()
-        t_mix = m0.elapsed_time(m1) / 1e3
-        if dist is not None:
-            tt = torch.tensor([t_mix], device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t_mix = float(tt.item())
+        mcfg = PRESETS[args.mixed_preset]
+        mgrid = aerofoil_grid(mcfg)
+        mn = mcfg.npoints
+        runs = {}
+        for name, prec in (("fp64", FP64), ("mixed", MIXED)):
+            cm = Case(mcfg.replace(precision=prec))
+            for mb in range(mcfg.nblocks):
+                cm.set_grid(mb, mgrid[mb])
+            cm.init()
+            cm.step(args.warmup)
+            barrier()
+            sm = torch.cuda.ExternalStream(cm.stream())
+            m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            m0.record(sm)
+            cm.step(args.steps)
+            m1.record(sm)
+            barrier()
+            t_run = m0.elapsed_time(m1) / 1e3
+            if dist is not None:
+                tt = torch.tensor([t_run], device="cuda")
+                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+                t_run = float(tt.item())
+            runs[name] = (cm, t_run)
+        (cd, t_d), (cm, t_mix) = runs["fp64"], runs["mixed"]
         num = np.zeros(5)
         den = np.zeros(5)
-        for mb in range(cfg.nblocks):
-            qd, qm = case.get_state(mb), cm.get_state(mb)
+        for mb in range(mcfg.nblocks):
+            qd, qm = cd.get_state(mb), cm.get_state(mb)
             num += np.sum((qm - qd) ** 2, axis=1)
             den += np.sum(qd ** 2, axis=1)
         den[1:4] = den[1:4].sum()
+        cd.close()
         cm.profile(True)
         cm.step(2)
         mprof = cm.profile_read()
@@ -368,29 +414,35 @@ def main():
         mdom = max(mprof, key=lambda k: mprof[k][0])
         mkind = "filter" if mdom.startswith("filter") else "deriv"
         if mdom.startswith(("deriv", "filter")):
-            munits = npts * FIELD_SWEEPS_PER_STEP[mkind] * 2 / max(mprof[mdom][1], 1)
+            munits = mn * FIELD_SWEEPS_PER_STEP[mkind] * 2 / max(mprof[mdom][1], 1)
             mt = mprof[mdom][0] / max(mprof[mdom][1], 1) / 1e3
             mach = SWEEP_BYTES_MIXED[mkind] * munits / mt / 1e9
             mroof = {"bound": "hbm", "kernel": f"k_sweep<{mdom}> in FP32, {SWEEP_BYTES_MIXED[mkind]} B per point-field",
                      "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
                      "frac": mach / measured_peaks()[0]}
-        elif mdom in POINTWISE_BYTES_MIXED and cfg.nviscous == 1:
+        elif mdom in POINTWISE_BYTES_MIXED and mcfg.nviscous == 1:
             mt = mprof[mdom][0] / max(mprof[mdom][1], 1) / 1e3
-            mach = POINTWISE_BYTES_MIXED[mdom] * npts / mt / 1e9
+            mach = POINTWISE_BYTES_MIXED[mdom] * mn / mt / 1e9
             mroof = {"bound": "hbm", "kernel": "k_flux_staged (viscous fluxes, stresses at the point), "
                                                f"{POINTWISE_BYTES_MIXED[mdom]} B per point",
                      "achieved": mach, "peak": measured_peaks()[0], "unit": "GB/s",
                      "frac": mach / measured_peaks()[0]}
         else:
             mroof = {"kernel": mdom, "note": "no algorithmic byte count for this kernel class"}
-        mixed = {"value": npts * cfg.nkrk * args.steps * ws / t_mix, "ms_per_step": t_mix / args.steps * 1e3,
+        v_mix = mn * mcfg.nkrk * args.steps * ws / t_mix
+        v_d = mn * mcfg.nkrk * args.steps * ws / t_d
+        mixed = {"workload": f"{args.mixed_preset}: NACA 0012, 6 blocks "
+                             f"{'x'.join(str(v + 1) for v in (mcfg.lxibk[0], mcfg.letbk[0], mcfg.lzebk[0]))}, "
+                             f"{mn} points, impulsive start, {args.steps} steps after {args.warmup} warm-up",
+                 "value": v_mix, "ms_per_step": t_mix / args.steps * 1e3,
+                 "fp64_same_case": {"value": v_d, "ms_per_step": t_d / args.steps * 1e3},
                  "dtype": "f32 line solves/filters/fluxes, f64 metrics, Jacobian and RK state",
-                 "speedup_vs_fp64": (npts * cfg.nkrk * args.steps * ws / t_mix) / value,
+                 "speedup_vs_fp64": v_mix / v_d,
                  "rel_l2_vs_fp64_after_steps": {"steps": args.warmup + args.steps,
                                                 "rho": float(np.sqrt(num[0] / den[0])),
                                                 "momentum": float(np.sqrt(num[1:4].sum() / den[1])),
                                                 "rhoE": float(np.sqrt(num[4] / den[4]))},
-                 "stage_hbm_frac_728B": STAGE_BYTES_MIXED * (npts * cfg.nkrk * args.steps / t_mix) / 1e9
+                 "stage_hbm_frac_728B": STAGE_BYTES_MIXED * (mn * mcfg.nkrk * args.steps / t_mix) / 1e9
                  / measured_peaks()[0],
                  "roofline": mroof,
                  "tiles": list(mtiles),

@@ -23,6 +23,7 @@
 #include "ati_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -150,6 +151,17 @@ struct orc_case {
   long n, ndt;
   double dt, dts, dte, timo;
   int inited;
+  /* inflow turbulence (no counterpart in the reference, whose eddy generator is off): the mode table of the
+   * GPU library, summed in FP64; the gust points and their velocity, held between evaluations */
+  int nmodes;
+  double *modes;          /* 8 per mode: k_x, k_y, k_z, s_x, s_y, s_z, a, psi */
+  long ngust;
+  int *gblk;              /* block of gust point q */
+  long *gl;               /* its point in the block */
+  double *gx, *gatz, *gv; /* x, y, z (3 per point), atz, velocity (3 per point) */
+  long *gidx;             /* per block, dense: gust index of each point or -1 (block offsets in goff) */
+  long *goff;
+  long steps_done;
 };
 
 #define F(ptr, np, l, m) (ptr)[(size_t)((m) - 1) * (size_t)(np) + (size_t)(l)]
@@ -554,6 +566,7 @@ void orc_destroy(orc_case *c) {
   if (c->b)
     for (int mb = 0; mb < c->nb; mb++) block_free(&c->b[mb]);
   free(c->b);
+  free(c->modes); free(c->gblk); free(c->gl); free(c->gx); free(c->gatz); free(c->gv); free(c->gidx); free(c->goff);
   free(c);
 }
 
@@ -1154,9 +1167,150 @@ int orc_init(orc_case *c) {
     }
   }
   c->n = 0; c->ndt = 0; c->dt = zero; c->dts = zero; c->dte = zero; c->timo = zero;
+  c->steps_done = 0;
   movef(c, 0, 0);
   c->inited = 1;
   return ATI_OK;
+}
+
+/* ---- inflow turbulence (new code: the reference's inflow-eddy generator is
+ * disabled, src/SingleTurbulence3D.f90:260) ---------------------------------
+ * The gust points are the sponge points of the inflow zone, x < -0.7 domlen +
+ * szth1, with the streamwise ramp atz = sin^2(min(pi (x + domlen)/szth1,
+ * pi/2)); spongego (src/SingleTurbulence3D.f90:355-372) drives them towards the
+ * isentropic target of a velocity v.  Here v is the FP64 sum of the given
+ * Fourier modes, v = sum_m 2 a_m s_m cos(k_m . x + psi_m - (k_m . U_inf) t),
+ * evaluated at the start time of the first step and of every step that takes
+ * a new dt (n % 10 == 1), held in between. */
+int orc_set_turbulence(orc_case *c, const float *modes, int nmodes) {
+  if (!c->inited || nmodes < 0 || (nmodes > 0 && !modes)) return ATI_EINVAL;
+  free(c->modes); free(c->gblk); free(c->gl); free(c->gx); free(c->gatz); free(c->gv); free(c->gidx); free(c->goff);
+  c->modes = NULL; c->gblk = NULL; c->gl = NULL; c->gx = NULL; c->gatz = NULL; c->gv = NULL; c->gidx = NULL;
+  c->goff = NULL; c->ngust = 0; c->nmodes = 0;
+  if (nmodes == 0) return ATI_OK;
+  const ati_config_t *g = &c->cfg;
+  c->nmodes = nmodes;
+  c->modes = dalloc(8 * (long)nmodes);
+  for (long q = 0; q < 8 * (long)nmodes; q++) c->modes[q] = (double)modes[q];
+  const double xg = -(double)0.7f * g->domlen + g->szth1, ra0 = pi / g->szth1;
+  long ntot = 0, ng = 0;
+  for (int mb = 0; mb < c->nb; mb++) ntot += c->b[mb].np;
+  c->goff = (long *)malloc(sizeof(long) * (c->nb + 1));
+  c->gidx = (long *)malloc(sizeof(long) * (ntot > 0 ? ntot : 1));
+  long off = 0;
+  for (int mb = 0; mb < c->nb; mb++) {
+    OBlock *b = &c->b[mb];
+    c->goff[mb] = off;
+    for (long l = 0; l < b->np; l++) {
+      const double x = F(b->xyz, b->np, l, 1);
+      c->gidx[off + l] = (b->asz[l] == 0.0 || !(x < xg)) ? -1 : ng++;
+    }
+    off += b->np;
+  }
+  c->goff[c->nb] = off;
+  c->ngust = ng;
+  c->gblk = (int *)malloc(sizeof(int) * (ng > 0 ? ng : 1));
+  c->gl = (long *)malloc(sizeof(long) * (ng > 0 ? ng : 1));
+  c->gx = dalloc(3 * (ng > 0 ? ng : 1)); c->gatz = dalloc(ng > 0 ? ng : 1); c->gv = dalloc(3 * (ng > 0 ? ng : 1));
+  for (int mb = 0; mb < c->nb; mb++) {
+    OBlock *b = &c->b[mb];
+    for (long l = 0; l < b->np; l++) {
+      const long q = c->gidx[c->goff[mb] + l];
+      if (q < 0) continue;
+      const double x = F(b->xyz, b->np, l, 1);
+      c->gblk[q] = mb; c->gl[q] = l;
+      c->gx[3 * q] = x; c->gx[3 * q + 1] = F(b->xyz, b->np, l, 2); c->gx[3 * q + 2] = F(b->xyz, b->np, l, 3);
+      const double sa = sin(fmin(ra0 * (x + g->domlen), half * pi));
+      c->gatz[q] = sa * sa;
+      c->gv[3 * q] = c->gv[3 * q + 1] = c->gv[3 * q + 2] = zero;
+    }
+  }
+  return ATI_OK;
+}
+
+/* The mode table of the inflow turbulence, restating the generator of the GPU library: nmodes = turb_modes
+ * wavenumbers log-spaced over [0.1 ke, 20 ke] (ke = 0.747 / turb_length) with amplitudes from the von Karman
+ * spectrum E(k) ~ (k/ke)^4 / (1 + (k/ke)^2)^(17/6); directions, polarisation angle and phase uniform from
+ * splitmix64 (Steele, Lea and Flood 2014) seeded by turb_seed; k_z rounded to the span's periodic lattice;
+ * polarisation normal to k; amplitudes scaled so that sum 2 a^2 = 3 (turb_intensity |U_inf|)^2.  out holds 8
+ * floats per mode (k_x, k_y, k_z, s_x, s_y, s_z, a, psi); returns the mode count (0: no turbulence). */
+typedef struct { uint64_t s; } orc_splitmix;
+static uint64_t smx_next(orc_splitmix *r) {
+  uint64_t z = (r->s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static double smx_uniform(orc_splitmix *r) { return (double)(smx_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+
+int orc_build_modes(const ati_config_t *cfg, float *out) {
+  const int n = cfg->turb_modes;
+  if (n <= 0 || cfg->turb_intensity <= 0.0) return 0;
+  if (!out) return n;
+  const double pie = acos(-1.0);
+  const double uinf = sqrt(cfg->amach1 * cfg->amach1 + cfg->amach2 * cfg->amach2 + cfg->amach3 * cfg->amach3);
+  const double urms = cfg->turb_intensity * uinf;
+  const double L = cfg->turb_length > 0 ? cfg->turb_length : 0.1;
+  const double ke = 0.747 / L, kmin = 0.1 * ke, kmax = 20.0 * ke, lr = log(kmax / kmin);
+  const double kz0 = 2.0 * pie / cfg->span;
+  orc_splitmix rng = {(uint64_t)(uint32_t)cfg->turb_seed * 0x2545F4914F6CDD1Dull + 1};
+  double *mk = dalloc(3 * (long)n), *ms = dalloc(3 * (long)n), *ma = dalloc(n), *mp = dalloc(n);
+  double e2 = 0.0;
+  for (int m = 0; m < n; m++) {
+    const double k = kmin * exp(lr * (m + 0.5) / n), dk = k * lr / n, r = k / ke;
+    const double E = r * r * r * r / pow(1.0 + r * r, 17.0 / 6.0);
+    const double ct = 1.0 - 2.0 * smx_uniform(&rng), st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    const double ph = 2.0 * pie * smx_uniform(&rng), al = 2.0 * pie * smx_uniform(&rng), psi = 2.0 * pie * smx_uniform(&rng);
+    double kv[3] = {k * st * cos(ph), k * st * sin(ph), k * ct};
+    kv[2] = kz0 * nearbyint(kv[2] / kz0);
+    const double kk = sqrt(kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+    const double kh[3] = {kv[0] / kk, kv[1] / kk, kv[2] / kk};
+    double e1[3];
+    if (fabs(kh[2]) < 0.9) { e1[0] = -kh[1]; e1[1] = kh[0]; e1[2] = 0.0; }
+    else { e1[0] = 0.0; e1[1] = -kh[2]; e1[2] = kh[1]; }
+    const double n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+    for (int q = 0; q < 3; q++) e1[q] /= n1;
+    const double e2v[3] = {kh[1] * e1[2] - kh[2] * e1[1], kh[2] * e1[0] - kh[0] * e1[2], kh[0] * e1[1] - kh[1] * e1[0]};
+    for (int q = 0; q < 3; q++) {
+      mk[3 * m + q] = kv[q];
+      ms[3 * m + q] = cos(al) * e1[q] + sin(al) * e2v[q];
+    }
+    ma[m] = sqrt(E * dk);
+    mp[m] = psi;
+    e2 += 2.0 * ma[m] * ma[m];
+  }
+  const double scale = sqrt(3.0 * urms * urms / e2);
+  for (int m = 0; m < n; m++) {
+    for (int q = 0; q < 3; q++) {
+      out[8 * m + q] = (float)mk[3 * m + q];
+      out[8 * m + 3 + q] = (float)ms[3 * m + q];
+    }
+    out[8 * m + 6] = (float)(ma[m] * scale);
+    out[8 * m + 7] = (float)mp[m];
+  }
+  free(mk); free(ms); free(ma); free(mp);
+  return n;
+}
+
+static void gust_eval(orc_case *c, double t) {
+  const long ng = c->ngust;
+  const int nm = c->nmodes;
+  const double u1 = c->uoo[1], u2 = c->uoo[2], u3 = c->uoo[3];
+#pragma omp parallel for OMP_NT
+  for (long q = 0; q < ng; q++) {
+    const double x = c->gx[3 * q], y = c->gx[3 * q + 1], z = c->gx[3 * q + 2];
+    double vx = zero, vy = zero, vz = zero;
+    for (int m = 0; m < nm; m++) {
+      const double *md = c->modes + 8 * (long)m;
+      const double w = (md[0] * u1 + md[1] * u2 + md[2] * u3) * t;
+      const double ph = md[0] * x + md[1] * y + md[2] * z + md[7] - w;
+      const double cc = two * md[6] * cos(ph);
+      vx = vx + cc * md[3];
+      vy = vy + cc * md[4];
+      vz = vz + cc * md[5];
+    }
+    c->gv[3 * q] = vx; c->gv[3 * q + 1] = vy; c->gv[3 * q + 2] = vz;
+  }
 }
 
 /* ---- the per-step filter: src/Main3D.f90:555-561 -------------------------- */
@@ -1425,15 +1579,28 @@ int orc_rk_stage(orc_case *c, int nk) {
     orc_deriv(c, 1, 1, m); orc_deriv(c, 2, 2, m); orc_deriv(c, 3, 3, m);
     divergence(c, m);
   }
+  if (c->ngust > 0 && nk == 1 && (c->n % 10 == 1 || c->steps_done == 0)) gust_eval(c, c->timo);
+  const double fctr = half * gamm1;
   for (int mb = 0; mb < c->nb; mb++) {
     OBlock *b = &c->b[mb];
     long np = b->np;
+    const long *gi = c->ngust > 0 ? c->gidx + c->goff[mb] : NULL;
 #pragma omp parallel for OMP_NT
     for (long l = 0; l < np; l++) {
       double as = b->asz[l], bs = b->bsz[l];
       if (as == 0 && bs == 0) continue; /* not a sponge point */
+      const long q = gi ? gi[l] : -1;
+      if (q >= 0) {  /* gust point: the isentropic target of v (src/SingleTurbulence3D.f90:362-372) */
+        const double *v = c->gv + 3 * q;
+        const double rr = pow(one - fctr * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]), hamm1);
+        F(b->de, np, l, 1) = F(b->de, np, l, 1) + as * (F(b->qa, np, l, 1) - rr);
+        for (int m = 2; m <= 4; m++)
+          F(b->de, np, l, m) = F(b->de, np, l, m) + as * (F(b->qa, np, l, m) - c->gatz[q] * rr * v[m - 2]);
+        F(b->de, np, l, 5) = F(b->de, np, l, 5) + bs * (b->p[l] - ham * pow(rr, gam));
+        continue;
+      }
       F(b->de, np, l, 1) = F(b->de, np, l, 1) + as * (F(b->qa, np, l, 1) - one);
-      for (int q = 2; q <= 4; q++) F(b->de, np, l, q) = F(b->de, np, l, q) + as * (F(b->qa, np, l, q) - zero);
+      for (int q2 = 2; q2 <= 4; q2++) F(b->de, np, l, q2) = F(b->de, np, l, q2) + as * (F(b->qa, np, l, q2) - zero);
       F(b->de, np, l, 5) = F(b->de, np, l, 5) + bs * (b->p[l] - ham * pow(one, gam));
     }
   }
@@ -1670,6 +1837,7 @@ int orc_step(orc_case *c, int nsteps) {
     for (int nk = 1; nk <= c->cfg.nkrk; nk++) orc_rk_stage(c, nk);
     c->n = c->n + 1;
     c->timo = c->timo + c->dt;
+    c->steps_done = c->steps_done + 1;
     if (!isfinite(c->dt)) return ATI_ENONFINITE;
   }
   return ATI_OK;

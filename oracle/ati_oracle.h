@@ -49,6 +49,12 @@ int orc_filter_step(orc_case *c);
 int orc_rk_stage(orc_case *c, int nk);
 int orc_step(orc_case *c, int nsteps);
 int orc_forces(orc_case *c, double out[2]);
+/* Inflow turbulence after orc_init: nmodes Fourier modes, 8 floats each (k_x, k_y, k_z, s_x, s_y, s_z, a, psi, the
+ * table ati_turbulence_modes returns), summed in FP64 at the inflow sponge's gust points; 0 modes turn it off. */
+int orc_set_turbulence(orc_case *c, const float *modes, int nmodes);
+/* The mode table of cfg's inflow turbulence (8 floats per mode; the GPU library's generator restated): returns the
+ * mode count, 0 for none; with out == NULL only the count. */
+int orc_build_modes(const ati_config_t *cfg, float *out);
 void orc_set_threads(int n);
 int orc_get_threads(void);
 

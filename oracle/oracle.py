@@ -34,6 +34,10 @@ def lib():
             f = getattr(L, name)
             f.argtypes = args
             f.restype = ctypes.c_int
+        L.orc_set_turbulence.argtypes = [vp, ctypes.c_void_p, i32]
+        L.orc_set_turbulence.restype = ctypes.c_int
+        L.orc_build_modes.argtypes = [vp, ctypes.c_void_p]
+        L.orc_build_modes.restype = ctypes.c_int
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_set_threads.restype = None
         L.orc_get_threads.restype = ctypes.c_int
@@ -137,6 +141,13 @@ class OracleCase:
         self._chk(lib().orc_forces(self.h, _dp(out)), "orc_forces")
         return out
 
+    def set_turbulence(self, modes):
+        """Inflow turbulence from a (nmodes, 8) float32 mode table (Case.turbulence_modes()), after init."""
+        m = np.ascontiguousarray(modes, dtype=np.float32)
+        self._modes = m
+        self._chk(lib().orc_set_turbulence(self.h, m.ctypes.data_as(ctypes.c_void_p), int(m.shape[0])),
+                  "orc_set_turbulence")
+
     def get_time(self):
         t = AtiTime()
         lib().orc_get_time(self.h, ctypes.byref(t))
@@ -164,6 +175,16 @@ class OracleCase:
         ncd = (ctypes.c_int32 * 6)()
         lib().orc_topology(self.h, mb, nbc, ncd)
         return list(nbc), list(ncd)
+
+
+def build_modes(cfg):
+    """(nmodes, 8) float32 inflow-turbulence mode table of cfg (empty without turbulence)."""
+    c = cfg.to_c()
+    n = lib().orc_build_modes(ctypes.byref(c), None)
+    out = np.zeros((n, 8), dtype=np.float32)
+    if n:
+        lib().orc_build_modes(ctypes.byref(c), out.ctypes.data_as(ctypes.c_void_p))
+    return out
 
 
 def set_threads(n):

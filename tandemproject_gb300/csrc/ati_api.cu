@@ -113,6 +113,9 @@ struct ati_handle {
   float *dmodes = nullptr, *ddelta = nullptr;
   TurbCase *dtc = nullptr;
   GustPt *dgust = nullptr;
+  // the strict mode's FP64 synthesis: the gust points in FP64 and their target changes
+  GustPt64 *dgust64 = nullptr;
+  double *ddelta64 = nullptr;
   int64_t ngust = 0;
   // surface-pressure recorder (ring buffer of wall pressure on the mid-span lines)
   int probe_cap = 0;
@@ -1014,7 +1017,8 @@ extern "C" int ati_destroy(ati_handle_t *h) {
   }
   drop_graphs(h);
   probe_free(h);
-  for (void *p : {(void *)h->dmodes, (void *)h->ddelta, (void *)h->dtc, (void *)h->dgust})
+  for (void *p : {(void *)h->dmodes, (void *)h->ddelta, (void *)h->dtc, (void *)h->dgust, (void *)h->dgust64,
+                  (void *)h->ddelta64})
     if (p) cudaFree(p);
   if (h->arena) cudaFree(h->arena);
   if (h->st) cudaStreamDestroy(h->st);
@@ -1350,14 +1354,22 @@ static int to_float(ati_handle *h, const double *src, const float *dst, int64_t 
 // the streamwise ramp atz = sin^2(min(pi (x + domlen) / szth1, pi / 2)); each
 // case's list is padded to whole CTAs of the evaluation kernel
 static int setup_gust(ati_handle *h) {
+  for (void **p : {(void **)&h->dmodes, (void **)&h->ddelta, (void **)&h->dtc, (void **)&h->dgust,
+                   (void **)&h->dgust64, (void **)&h->ddelta64}) {  // (a second ati_init)
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  h->ngust = 0;
   if (h->hmodes.empty()) return ATI_OK;
   const int64_t N = h->N;
+  const bool fp64 = h->cfg.precision == ATI_FP64_STRICT;
   std::vector<double> xyz((size_t)3 * N), asz(N);
   CK(cudaMemcpyAsync(xyz.data(), h->ss, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(asz.data(), h->ed.asz, sizeof(double) * N, cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   const double pi = std::acos(-1.0);
   std::vector<GustPt> pts;
+  std::vector<GustPt64> p64;
   const int nbc = h->nb / h->ncase;
   for (int cs = 0; cs < h->ncase; cs++) {
     if (h->htc[cs].n == 0) continue;
@@ -1371,15 +1383,21 @@ static int setup_gust(ati_handle *h) {
         if (asz[g] == 0.0 || !(x < xg)) continue;  // asz carries the sign of 1/J
         const double s = std::sin(std::fmin(ra0 * (x + cfg.domlen), 0.5 * pi));
         pts.push_back(GustPt{g, (float)x, (float)xyz[g + N], (float)xyz[g + 2 * N], (float)(s * s), cs, 0});
+        p64.push_back(GustPt64{x, xyz[g + N], xyz[g + 2 * N], s * s});
       }
     }
-    while ((pts.size() - first) % 256) pts.push_back(GustPt{-1, 0.f, 0.f, 0.f, 0.f, cs, 0});
+    while ((pts.size() - first) % 256) {
+      pts.push_back(GustPt{-1, 0.f, 0.f, 0.f, 0.f, cs, 0});
+      p64.push_back(GustPt64{0.0, 0.0, 0.0, 0.0});
+    }
   }
   h->ngust = (int64_t)pts.size();
   if (h->ngust == 0) return ATI_OK;
   auto alloc = [&](void **p, size_t n) { return cudaMalloc(p, n) == cudaSuccess; };
   if (!alloc((void **)&h->dgust, sizeof(GustPt) * pts.size()) || !alloc((void **)&h->ddelta, sizeof(float) * 5 * pts.size()) ||
-      !alloc((void **)&h->dmodes, sizeof(float) * h->hmodes.size()) || !alloc((void **)&h->dtc, sizeof(TurbCase) * h->ncase)) {
+      !alloc((void **)&h->dmodes, sizeof(float) * h->hmodes.size()) || !alloc((void **)&h->dtc, sizeof(TurbCase) * h->ncase) ||
+      (fp64 && (!alloc((void **)&h->dgust64, sizeof(GustPt64) * p64.size()) ||
+                !alloc((void **)&h->ddelta64, sizeof(double) * 5 * p64.size())))) {
     cudaGetLastError();
     return fail(h, ATI_ENOMEM, "inflow turbulence: device allocation failed");
   }
@@ -1387,6 +1405,10 @@ static int setup_gust(ati_handle *h) {
   CK(cudaMemcpyAsync(h->dmodes, h->hmodes.data(), sizeof(float) * h->hmodes.size(), cudaMemcpyHostToDevice, h->st));
   CK(cudaMemcpyAsync(h->dtc, h->htc.data(), sizeof(TurbCase) * h->ncase, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemsetAsync(h->ddelta, 0, sizeof(float) * 5 * pts.size(), h->st));
+  if (fp64) {
+    CK(cudaMemcpyAsync(h->dgust64, p64.data(), sizeof(GustPt64) * p64.size(), cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemsetAsync(h->ddelta64, 0, sizeof(double) * 5 * p64.size(), h->st));
+  }
   CK(cudaStreamSynchronize(h->st));
   return ATI_OK;
 }
@@ -1722,10 +1744,18 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
     // inflow turbulence: the gust targets of the inflow sponge, evaluated on the steps that take a new dt
     // (n % 10 == 1, and the first step) and held in between: 10 steps are a few thousandths of the eddies'
     // convective time L / U_inf, and the 2048-mode synthesis would otherwise cost more than the sponge it feeds
-    if (nk == 1 && (h->n_host % 10 == 1 || h->steps_done == 0))
-      PROF(h, ATI_K_DIV, gust_eval(st, h->dgust, h->ngust, h->dtc, h->dmodes, ed.scal, h->ddelta, h->sh.s.gam));
+    // (the strict mode, the parity mode, sums the modes in FP64 in the CPU restatement's order; the others in FP32)
+    const bool g64 = h->dgust64 != nullptr;
+    const Scheme &S0 = h->sh.s;
+    if (nk == 1 && (h->n_host % 10 == 1 || h->steps_done == 0)) {
+      if (g64)
+        PROF(h, ATI_K_DIV, gust_eval64(st, h->dgust, h->dgust64, h->ngust, h->dtc, h->dmodes, ed.scal, h->ddelta64,
+                                       S0.gam, S0.gamm1, S0.hamm1, S0.ham));
+      else PROF(h, ATI_K_DIV, gust_eval(st, h->dgust, h->ngust, h->dtc, h->dmodes, ed.scal, h->ddelta, S0.gam));
+    }
     if constexpr (std::is_same<R, float>::value)
       PROF(h, ATI_K_DIV, gust_apply_f(st, h->dgust, h->ngust, h->ddelta, ed.asz, ed.bsz, e.de, N));
+    else if (g64) PROF(h, ATI_K_DIV, gust_apply64(st, h->dgust, h->ngust, h->ddelta64, ed.asz, ed.bsz, e.de, N));
     else PROF(h, ATI_K_DIV, gust_apply_d(st, h->dgust, h->ngust, h->ddelta, ed.asz, ed.bsz, e.de, N));
   }
   // characteristic boundary conditions (src/Main3D.f90:780-869)

@@ -159,6 +159,68 @@ __global__ void k_gust_apply(const GustPt *pts, int64_t npts, const float *delta
   de[g + 4 * N] = (R)((double)de[g + 4 * N] + bs * d[4]);
 }
 
+// The FP64 synthesis of the strict mode.  The mode sum and the target use explicitly rounded operations (no
+// multiply-add contraction) in the order of the CPU restatement, so the two differ only through cos and pow.
+__global__ void __launch_bounds__(GT) k_gust_eval64(const GustPt *pts, const GustPt64 *p64, const TurbCase *tc,
+                                                    const float *modes, const Scalars *scal, double *delta,
+                                                    double gam, double gamm1, double hamm1, double ham) {
+  __shared__ double sm[8 * GT], sw[GT];
+  const int64_t i = (int64_t)blockIdx.x * GT + threadIdx.x;
+  const GustPt P = pts[i];
+  const GustPt64 Q = p64[i];
+  const int cs = pts[(int64_t)blockIdx.x * GT].cs;
+  const TurbCase C = tc[cs];
+  const double t = scal[cs].timo;
+  double vx = 0.0, vy = 0.0, vz = 0.0;
+  for (int m0 = 0; m0 < C.n; m0 += GT) {
+    const int nm = min(GT, C.n - m0);
+    __syncthreads();
+    for (int q = threadIdx.x; q < nm; q += blockDim.x) {
+      // k, s, 2 a, psi of the mode, and its time phase (k . U_inf) t
+      const float *md = modes + 8 * ((int64_t)C.off + m0 + q);
+      double *d = sm + 8 * q;
+      for (int c = 0; c < 8; c++) d[c] = (double)md[c];
+      d[6] = __dmul_rn(2.0, d[6]);
+      sw[q] = __dmul_rn(__dadd_rn(__dadd_rn(__dmul_rn(d[0], C.u[0]), __dmul_rn(d[1], C.u[1])), __dmul_rn(d[2], C.u[2])),
+                        t);
+    }
+    __syncthreads();
+    for (int m = 0; m < nm; m++) {
+      const double *d = sm + 8 * m;
+      const double ph = __dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(d[0], Q.x), __dmul_rn(d[1], Q.y)),
+                                                      __dmul_rn(d[2], Q.z)), d[7]), sw[m]);
+      const double c = __dmul_rn(d[6], cos(ph));
+      vx = __dadd_rn(vx, __dmul_rn(c, d[3]));
+      vy = __dadd_rn(vy, __dmul_rn(c, d[4]));
+      vz = __dadd_rn(vz, __dmul_rn(c, d[5]));
+    }
+  }
+  if (P.g < 0) return;
+  // isentropic target of spongego (src/SingleTurbulence3D.f90:362-372), as changes of the rest targets
+  const double s2 = __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz));
+  const double rho = pow(__dsub_rn(1.0, __dmul_rn(__dmul_rn(0.5, gamm1), s2)), hamm1);
+  const double a = __dmul_rn(Q.atz, rho);
+  double *dl = delta + 5 * i;
+  dl[0] = __dsub_rn(1.0, rho);
+  dl[1] = -__dmul_rn(a, vx); dl[2] = -__dmul_rn(a, vy); dl[3] = -__dmul_rn(a, vz);
+  dl[4] = __dsub_rn(ham, __dmul_rn(ham, pow(rho, gam)));
+}
+
+__global__ void k_gust_apply64(const GustPt *pts, int64_t npts, const double *delta, const double *asz,
+                               const double *bsz, double *de, int64_t N) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npts) return;
+  const int64_t g = pts[i].g;
+  if (g < 0) return;
+  const double *d = delta + 5 * i;
+  const double as = asz[g], bs = bsz[g];
+  de[g] = __dadd_rn(de[g], __dmul_rn(as, d[0]));
+  de[g + N] = __dadd_rn(de[g + N], __dmul_rn(as, d[1]));
+  de[g + 2 * N] = __dadd_rn(de[g + 2 * N], __dmul_rn(as, d[2]));
+  de[g + 3 * N] = __dadd_rn(de[g + 3 * N], __dmul_rn(as, d[3]));
+  de[g + 4 * N] = __dadd_rn(de[g + 4 * N], __dmul_rn(bs, d[4]));
+}
+
 __global__ void __launch_bounds__(GT) k_turb_sample(const TurbCase *tc, int cs, const float *modes, double t,
                                                     int64_t n, const double *xyz, double *v) {
   __shared__ float sm[8 * GT];
@@ -196,6 +258,17 @@ void gust_apply_f(cudaStream_t st, const GustPt *pts, int64_t npts, const float 
                   const double *bsz, float *de, int64_t N) {
   if (npts == 0) return;
   k_gust_apply<float><<<(unsigned)((npts + 255) / 256), 256, 0, st>>>(pts, npts, delta, asz, bsz, de, N);
+}
+void gust_eval64(cudaStream_t st, const GustPt *pts, const GustPt64 *p64, int64_t npts, const TurbCase *tc,
+                 const float *modes, const Scalars *scal, double *delta, double gam, double gamm1, double hamm1,
+                 double ham) {
+  if (npts == 0) return;
+  k_gust_eval64<<<(unsigned)(npts / GT), GT, 0, st>>>(pts, p64, tc, modes, scal, delta, gam, gamm1, hamm1, ham);
+}
+void gust_apply64(cudaStream_t st, const GustPt *pts, int64_t npts, const double *delta, const double *asz,
+                  const double *bsz, double *de, int64_t N) {
+  if (npts == 0) return;
+  k_gust_apply64<<<(unsigned)((npts + 255) / 256), 256, 0, st>>>(pts, npts, delta, asz, bsz, de, N);
 }
 void turb_sample(cudaStream_t st, const TurbCase *tc, int cs, const float *modes, double t, int64_t n,
                  const double *xyz, double *v) {

@@ -17,6 +17,11 @@ struct GustPt {
   int cs, pad;
 };
 
+// the same point in FP64 (coordinates and ramp), for the FP64 synthesis of the strict arithmetic mode
+struct GustPt64 {
+  double x, y, z, atz;
+};
+
 // modes of one case in the concatenated table, and its freestream velocity
 struct TurbCase {
   int off, n;
@@ -32,6 +37,13 @@ void gust_apply_d(cudaStream_t st, const GustPt *pts, int64_t npts, const float 
                   const double *bsz, double *de, int64_t N);
 void gust_apply_f(cudaStream_t st, const GustPt *pts, int64_t npts, const float *delta, const double *asz,
                   const double *bsz, float *de, int64_t N);
+// the FP64 synthesis (ATI_FP64_STRICT, the parity mode): every operation of the mode sum and of the target
+// rounded as written, in the order of the CPU restatement; delta holds 5 doubles per gust point
+void gust_eval64(cudaStream_t st, const GustPt *pts, const GustPt64 *p64, int64_t npts, const TurbCase *tc,
+                 const float *modes, const Scalars *scal, double *delta, double gam, double gamm1, double hamm1,
+                 double ham);
+void gust_apply64(cudaStream_t st, const GustPt *pts, int64_t npts, const double *delta, const double *asz,
+                  const double *bsz, double *de, int64_t N);
 void turb_sample(cudaStream_t st, const TurbCase *tc, int cs, const float *modes, double t, int64_t n,
                  const double *xyz, double *v);
 

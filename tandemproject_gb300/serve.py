@@ -43,38 +43,56 @@ class Server:
         self.make_grid = make_grid
         self.footprint = footprint
         self.peak_bytes = 0
+        self.bound = False  # some request waited for memory (admission held it back)
 
     def run(self, requests, log=None):
         """Serve the requests (arrival times in seconds from the start);
-        return one record per request and the run summary."""
+        return one record per request and the run summary.
+
+        The issuing loop never waits for a case to be set up: host grids are
+        built from arrival on (prefetch pool), and an admitted case is created
+        and initialised (device arrays, metrics, tile timing) on a set-up
+        thread while the loop keeps issuing steps to the running cases.  Its
+        memory counts against the budget from admission on."""
         pending = sorted(requests, key=lambda r: r.arrival)
-        waiting, active, done = [], [], []
+        waiting, starting, active, done = [], [], [], []
         used = 0
         grids = {}
         pool = cf.ThreadPoolExecutor(max_workers=self.prefetch)
+        setup = cf.ThreadPoolExecutor(max_workers=1)
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
-        while pending or waiting or active:
+
+        def create(r):
+            cfg, grid = grids.pop(r.rid).result()
+            return cfg, self.make_case(cfg, grid)
+
+        while pending or waiting or starting or active:
             t = now()
             while pending and pending[0].arrival <= t:
                 r = pending.pop(0)
                 waiting.append(r)
                 grids[r.rid] = pool.submit(self.make_grid, r.cfg)  # host-side grid, ahead of admission
-            # admit in arrival order while the footprint fits
+            # admit in arrival order while the footprint fits; the set-up runs off the issuing loop
             while waiting:
                 r = waiting[0]
                 fp = self.footprint(r.cfg)
-                if used + fp > self.budget and active:
+                if used + fp > self.budget and (active or starting):
+                    self.bound = True
                     break
                 waiting.pop(0)
-                cfg, grid = grids.pop(r.rid).result()
-                c = self.make_case(cfg, grid)
                 used += fp
                 self.peak_bytes = max(self.peak_bytes, used)
-                active.append({"req": r, "case": c, "left": r.steps, "fp": fp, "admitted": now(), "npts": cfg.npoints})
+                starting.append({"req": r, "fp": fp, "admitted": now(), "job": setup.submit(create, r)})
                 if log:
-                    log(f"t={now():7.2f}s admit #{r.rid} {cfg.npoints / 1e6:.2f} M pts x {r.steps} steps, "
+                    log(f"t={now():7.2f}s admit #{r.rid} {r.cfg.npoints / 1e6:.2f} M pts x {r.steps} steps, "
                         f"{used / 2**30:.1f} GiB in use")
+            for s in list(starting):
+                if s["job"].done():
+                    cfg, c = s["job"].result()
+                    starting.remove(s)
+                    active.append({"req": s["req"], "case": c, "left": s["req"].steps, "fp": s["fp"],
+                                   "admitted": s["admitted"], "started": now(), "npts": cfg.npoints})
             # one chunk of steps for every running case, issued without waiting
             for a in active:
                 if a["left"] > 0 and a["case"].idle():
@@ -87,8 +105,8 @@ class Server:
                     c = a["case"]
                     c.check()
                     rec = {"id": a["req"].rid, "points": a["npts"], "steps": a["req"].steps,
-                           "arrival": a["req"].arrival, "admitted": a["admitted"], "done": now(),
-                           "forces": c.forces().tolist()}
+                           "arrival": a["req"].arrival, "admitted": a["admitted"], "started": a["started"],
+                           "done": now(), "forces": c.forces().tolist()}
                     if self.keep_state:
                         rec["state"] = [c.get_state(mb) for mb in range(c.cfg.nblocks)]
                     rec["latency"] = rec["done"] - rec["arrival"]
@@ -98,17 +116,21 @@ class Server:
                     done.append(rec)
                     if log:
                         log(f"t={now():7.2f}s done  #{rec['id']} latency {rec['latency']:.2f} s")
-            if not pending and not waiting and active:
+            if not pending and not waiting and (active or starting):
                 time.sleep(0.0005)
-            elif pending and not waiting and not active:
+            elif pending and not waiting and not active and not starting:
                 time.sleep(max(0.0, min(pending[0].arrival - now(), 0.05)))
         pool.shutdown()
+        setup.shutdown()
         makespan = now()
         lat = np.array([d["latency"] for d in done])
+        wait = np.array([d["admitted"] - d["arrival"] for d in done])
         work = sum(d["points"] * 4 * d["steps"] for d in done)
         summary = {"requests": len(done), "makespan_s": makespan,
                    "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
                                  "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+                   "admission_wait_s": {"p50": float(np.percentile(wait, 50)), "max": float(wait.max())},
+                   "admission_bound": self.bound,
                    "updates_per_s": work / makespan, "peak_resident_gib": self.peak_bytes / 2**30}
         return done, summary
 
