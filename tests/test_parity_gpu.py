@@ -218,10 +218,15 @@ def test_naca0012_0p6m_hundred_steps(ati_lib, oracle_lib):
 @pytest.mark.parametrize("precision", ["fp64", "strict"])
 def test_les_branch_steps(ati_lib, oracle_lib, precision):
     """The Smagorinsky branch of the stresses (les = 1, src/Main3D.f90:656-678):
-    19 steps against the oracle's restatement of the same branch."""
+    19 steps against the oracle's restatement of the same branch.  The model
+    constants are raised far above the deck's (0.16, 0.0066) so that the eddy
+    viscosity changes the answer within these steps (by ~2e-7 on momentum; with
+    the deck's constants by ~3e-14): the test is on the branch's arithmetic,
+    not on the physics."""
     from tandemproject_gb300.config import FP64, FP64_STRICT
     prec = FP64_STRICT if precision == "strict" else FP64
-    cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), les=1, precision=prec)
+    cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), les=1, precision=prec, smago1=400.0,
+                     smago2=40.0)
     gpu, orc = pair(cfg)
     gpu.step(19)
     assert orc.step(19) == 0
@@ -232,14 +237,16 @@ def test_les_branch_steps(ati_lib, oracle_lib, precision):
     cfg0 = cfg.replace(les=0)
     gpu0, _ = pair(cfg0)
     gpu0.step(19)
-    assert np.any(state_errors(gpu0, orc) > 1e-12)
+    diff = state_errors(gpu0, orc)
+    print("LES on vs off after 19 steps", diff)
+    assert np.any(diff > 1e-9)
 
 
 def test_les_branch_mixed(ati_lib):
     """The mixed path's FP32 Smagorinsky branch tracks the FP64 one."""
     from tandemproject_gb300.config import MIXED
     from tandemproject_gb300.solver import setup_case
-    cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), les=1)
+    cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), les=1, smago1=400.0, smago2=40.0)
     d, m = setup_case(cfg), setup_case(cfg.replace(precision=MIXED))
     d.step(19)
     m.step(19)
