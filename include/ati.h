@@ -303,6 +303,34 @@ int ati_tiles(ati_handle_t *h, int32_t out[4]);
  * 256 in [256, 4096].  Waits for the steps in flight and re-captures the step
  * graphs at the next step. */
 int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
+/* Kernel options (no counterpart in the reference; results do not depend on
+ * them, only timings do).  Both are on by default.
+ *  ATI_OPT_TMA: the mixed path's segmented eta and zeta derivative sweeps
+ *    stage each tile of 32 lines into shared memory with one tensor copy
+ *    (TMA, cp.async.bulk.tensor) on every direction whose blocks' FP32 planes
+ *    a tensor map can describe (plane bases and row or plane sizes multiples
+ *    of 16 bytes, lines of at most 256 points); off, or elsewhere, with
+ *    per-thread asynchronous copies.
+ *  ATI_OPT_FUSED_FACES: the face and scalar work around the RK update of a
+ *    stage (src/Main3D.f90:780-952) runs as two cooperative launches whose
+ *    phases are ordered by grid barriers with bounded waits (see
+ *    ati_set_spin_limit), instead of one launch per face kind and direction.
+ * *active (may be NULL) gets the options in effect, plus ATI_OPT_TMA_ETA and
+ * ATI_OPT_TMA_ZETA for the directions staged by TMA.  Waits for the steps in
+ * flight; the step graphs are captured again. */
+#define ATI_OPT_TMA 1
+#define ATI_OPT_FUSED_FACES 2
+#define ATI_OPT_TMA_ETA 4
+#define ATI_OPT_TMA_ZETA 8
+int ati_set_options(ati_handle_t *h, int flags, int32_t *active);
+/* Device-side waits are bounded (no counterpart in the reference): a grid
+ * barrier of the fused face chains gives up after this many polls (0 = the
+ * default, 2^24, seconds), marks every case of the handle, and the next
+ * ati_step / ati_check / ati_case_check returns ATI_ETIMEDOUT.  The state is
+ * then not valid: set it (or call ati_init) before stepping on.  The TMA tile
+ * waits of the segmented sweeps have their own fixed bound and report the
+ * same way. */
+int ati_set_spin_limit(ati_handle_t *h, int64_t polls);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their
  * own work or events against the solver's. */
 void *ati_stream(ati_handle_t *h);

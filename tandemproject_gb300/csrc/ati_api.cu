@@ -10,6 +10,7 @@
 // rr/ss for the granular calls, and the FP64 stage intermediates) always
 // exists; a case created with ATI_MIXED also owns an FP32 set of stage
 // intermediates, metrics, face buffers and coefficients.
+#include <cuda.h>  // CUtensorMap and its enumerations (the encoder itself is fetched from the driver at run time)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,6 +40,7 @@ struct TaskRange {
 constexpr int SPG_PER_BLOCK = 14;
 
 thread_local std::string g_create_err;
+thread_local std::string g_tma_err;  // a tensor-map encoding failure at creation
 
 }  // namespace
 
@@ -55,6 +57,17 @@ struct ati_handle {
   std::vector<int> case_b0;
   std::vector<TaskRange> tl_force_c;
   bool any_cfl = false;  // some case takes its dt from the CFL condition (dto < 0)
+  bool tma[4] = {false, false, false, false};  // tensor maps exist for the mixed path's eta/zeta sweeps
+  std::vector<TmaMap> htmaps;                   // host copy of the tensor maps (kept for the upload)
+  bool fused = true;                            // fused face chains (ati_set_options)
+  unsigned spin_limit = 1u << 24;               // polls a device barrier wait may take (ati_set_spin_limit)
+  int64_t *dcum = nullptr;                      // running face-line counts of the task list (fused chains)
+  unsigned *dbar = nullptr;                     // grid-barrier counters of the fused chains
+  int64_t task_lines(int off, int n) const {    // face lines of a task range
+    int64_t t = 0;
+    for (int q = off; q < off + n; q++) t += htasks[q].nline;
+    return t;
+  }
   std::vector<PTile> hpt;
   std::vector<LTile> hlt[4];
   std::vector<LTile> hlts[4];  // tiles of the segmented sweeps (mixed path), by class (segc)
@@ -486,6 +499,80 @@ static int upload_tiles(ati_handle *h) {
   return ATI_OK;
 }
 
+// cuTensorMapEncodeTiled, fetched through the runtime (the library has no link-time dependency on the driver)
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiled encode_tiled() {
+  static EncodeTiled fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiled) nullptr;
+    }
+    return (EncodeTiled)p;
+  }();
+  return fn;
+}
+
+// Can every block's FP32 planes of direction nn (2: eta, 3: zeta) be described by a tensor map?  The base of each
+// block's plane and every stride must be a multiple of 16 bytes (N, the block offsets and the row or plane sizes
+// multiples of 4 floats), and a box spans the whole line (at most 256 points).
+static bool tma_geometry(const ati_handle *h, int nn) {
+  if (!h->mixed || h->N % 4 != 0) return false;
+  for (int b = 0; b < h->nb; b++) {
+    const BlockDev &B = h->blk[b];
+    const int64_t nx = B.lxi + 1, ny = B.let + 1, nz = B.lze + 1;
+    if (B.off % 4 != 0) return false;
+    if (nn == 2 && (nx % 4 != 0 || ny > 256)) return false;
+    if (nn == 3 && ((nx * ny) % 4 != 0 || nz > 256)) return false;
+  }
+  return encode_tiled() != nullptr;
+}
+
+// The tensor maps of the mixed path's eta/zeta derivative sweeps: per array (0: the four primitive planes u, v, w,
+// T, plane stride N; 1: the five flux planes of direction nn, stride 3 N), direction and block.  eta lines of a
+// block: 4-D (xi, eta, zeta, field), box 32 x ny x 1 x 1; zeta lines: 3-D (xi-eta plane, zeta, field), box 32 x nz
+// x 1.  Tile-mode boxes, no swizzle, out-of-bounds points read as zero.
+static int encode_tmaps(ati_handle *h, std::vector<TmaMap> &out) {
+  const int64_t N = h->N;
+  out.assign((size_t)4 * h->nb, TmaMap{});
+  EncodeTiled enc = encode_tiled();
+  for (int arr = 0; arr < 2; arr++)
+    for (int nn = 2; nn <= 3; nn++) {
+      if (!h->tma[nn]) continue;
+      const int nf = arr == 0 ? 4 : 5;
+      const int64_t fs = arr == 0 ? N : 3 * N;
+      float *plane = arr == 0 ? h->ef.prim : h->ef.flx + (nn - 1) * N;
+      for (int b = 0; b < h->nb; b++) {
+        const BlockDev &B = h->blk[b];
+        const uint64_t nx = B.lxi + 1, ny = B.let + 1, nz = B.lze + 1;
+        void *g = plane + B.off;
+        CUtensorMap *m = reinterpret_cast<CUtensorMap *>(&out[(size_t)(arr * 2 + nn - 2) * h->nb + b]);
+        CUresult r;
+        if (nn == 2) {
+          const cuuint64_t dim[4] = {nx, ny, nz, (cuuint64_t)nf};
+          const cuuint64_t str[3] = {nx * 4, nx * ny * 4, (cuuint64_t)fs * 4};
+          const cuuint32_t box[4] = {(cuuint32_t)SEG_LINES, (cuuint32_t)ny, 1, 1}, es[4] = {1, 1, 1, 1};
+          r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, g, dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        } else {
+          const cuuint64_t dim[3] = {nx * ny, nz, (cuuint64_t)nf};
+          const cuuint64_t str[2] = {nx * ny * 4, (cuuint64_t)fs * 4};
+          const cuuint32_t box[3] = {(cuuint32_t)SEG_LINES, (cuuint32_t)nz, 1}, es[3] = {1, 1, 1};
+          r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, g, dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        }
+        if (r != CUDA_SUCCESS)
+          return fail(h, ATI_ECUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ") for block " +
+                                        std::to_string(b) + ", direction " + std::to_string(nn));
+      }
+    }
+  return ATI_OK;
+}
+
 static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<double> &facf, std::vector<double> &spg) {
   int64_t off = 0, face = 0, fac = 0;
   spg.assign((size_t)SPG_PER_BLOCK * h->nb, 0.0);
@@ -620,6 +707,7 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
   for (int c = 0; c < 3; c++) point_tiles(h, PT_CAND[c], h->hptc[c]);
   for (int nn = 1; nn <= 3; nn++) h->max_lt[nn] = h->hlt[nn].size();
   make_tiles(h, SG_DEFAULT, SG_DEFAULT, PT_DEFAULT);
+  for (int nn = 2; nn <= 3; nn++) h->tma[nn] = tma_geometry(h, nn);
   for (int nn = 1; nn <= 3; nn++) {
     if (h->mixed && h->maxlen[nn] > SEG_LMAX)
       return fail(h, ATI_EINVAL, "mixed precision: lines of up to " + std::to_string(SEG_LMAX) + " points");
@@ -643,7 +731,15 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
       C.groups = seg_groups(C.maxlen);
       for (int gb = 0; gb < h->nb; gb++) {
         if (cls(len(h->blk[gb])) != c) continue;
-        for (int t0 = 0; t0 < h->blk[gb].nbsize[nn]; t0 += SEG_LINES * C.groups) h->hlts[nn].push_back(LTile{gb, t0});
+        const BlockDev &B = h->blk[gb];
+        if (nn == 2 && h->tma[2]) {
+          // TMA eta tiles: the lines of one grid row (fixed zeta), from a multiple of 32 points along xi
+          for (int ze = 0; ze <= B.lze; ze++)
+            for (int xi0 = 0; xi0 <= B.lxi; xi0 += SEG_LINES * C.groups)
+              h->hlts[nn].push_back(LTile{gb, ze * (B.lxi + 1) + xi0});
+          continue;
+        }
+        for (int t0 = 0; t0 < B.nbsize[nn]; t0 += SEG_LINES * C.groups) h->hlts[nn].push_back(LTile{gb, t0});
       }
       C.n = (int)h->hlts[nn].size() - C.off;
       h->segc[nn][c] = C;
@@ -821,6 +917,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_spg = take(spg.size() * D8), o_blk = take(sizeof(BlockDev) * h->nb),
                o_sc = take(sizeof(Scheme) * ncase), o_cfd = take(sizeof(Coef<double>)),
                o_scal = take(sizeof(Scalars) * ncase), o_task = take(sizeof(FaceTask) * h->htasks.size()),
+               o_cum = take(sizeof(int64_t) * (h->htasks.size() + 1)), o_bar = take(sizeof(unsigned) * 2),
                o_jn = take(sizeof(JunctionDev) * 2 * ncase), o_woff = take(nforce * sizeof(int64_t)),
                o_pt = take(sizeof(PTile) * h->max_pt), o_ptc0 = take(sizeof(PTile) * h->hptc[0].size()),
                o_ptc1 = take(sizeof(PTile) * h->hptc[1].size()), o_ptc2 = take(sizeof(PTile) * h->hptc[2].size()),
@@ -829,7 +926,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_facud = take((size_t)h->nfac * FU_RT * D8), o_facuf = take((size_t)h->nfac * FU_RT * D8);
   // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(3 x 5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
-         o_frpex = 0, o_cff = 0, o_fdrvm = 0, o_lts[4] = {0, 0, 0, 0}, o_segd = 0, o_segf = 0;
+         o_frpex = 0, o_cff = 0, o_fdrvm = 0, o_lts[4] = {0, 0, 0, 0}, o_segd = 0, o_segf = 0, o_tmap = 0;
   const int np32 = 5 + 4 + 1 + 1 + 12 + 9 + 15 + 15 + 9 + 1 + 1 + 1 + 3;
   if (h->mixed) {
     o_ff = take((size_t)np32 * N * F4);
@@ -842,6 +939,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     // (SEG_PAD rows of padding before and after: the kernel reads a few rows ahead of its segment)
     o_segd = take((size_t)(h->nfac + 2 * SEG_PAD) * SEG_RT * F4);
     o_segf = take((size_t)(h->nfac + 2 * SEG_PAD) * SEG_RT * F4);
+    o_tmap = take(sizeof(TmaMap) * 4 * (size_t)h->nb);
   }
   cudaError_t e = cudaMalloc(&h->arena, bytes);
   if (e != cudaSuccess) {
@@ -880,6 +978,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   d.facud = D(o_facud); d.facuf = D(o_facuf);
   h->area = D(o_area); h->wnor = D(o_wnor); h->dforce = D(o_frc); h->dspg = D(o_spg);
   h->dtasks = (FaceTask *)(h->arena + o_task);
+  h->dcum = (int64_t *)(h->arena + o_cum);
+  h->dbar = (unsigned *)(h->arena + o_bar);
   h->djn = (JunctionDev *)(h->arena + o_jn);
   h->dwoff = (int64_t *)(h->arena + o_woff);
   if (h->mixed) {
@@ -905,6 +1005,10 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
       for (int c = 0; c < SEG_NCLASS; c++) m.segc[nn][c] = h->segc[nn][c];
     }
     m.segd = Fp(o_segd) + SEG_PAD * SEG_RT; m.segf = Fp(o_segf) + SEG_PAD * SEG_RT;
+    m.tmaps = (const TmaMap *)(h->arena + o_tmap);
+    m.nblk = h->nb;
+    for (int nn = 0; nn < 4; nn++) m.tma[nn] = h->tma[nn];
+    m.eta_rowtiles = h->tma[2];
   }
   // junctions (src/SingleTurbulence3D.f90:386-398), bkx = 3, bky = 2, per case
   std::vector<JunctionDev> jn;
@@ -961,6 +1065,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   up(dsc, schemes.data(), sizeof(Scheme) * ncase);
   up(d.cf, &cfd, sizeof(cfd));
   up(h->dtasks, h->htasks.data(), sizeof(FaceTask) * h->htasks.size());
+  std::vector<int64_t> cum(h->htasks.size() + 1, 0);
+  for (size_t q = 0; q < h->htasks.size(); q++) cum[q + 1] = cum[q] + h->htasks[q].nline;
+  up(h->dcum, cum.data(), sizeof(int64_t) * cum.size());
   up(h->djn, jn.data(), sizeof(JunctionDev) * jn.size());
   up(h->dwoff, woff.data(), sizeof(int64_t) * woff.size());
   up(dpt, h->hpt.data(), sizeof(PTile) * h->hpt.size());
@@ -972,12 +1079,21 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     up(h->ef.facf, facf32.data(), facf32.size() * F4);
     up(h->ef.segd, segd32.data(), segd32.size() * F4);
     up(h->ef.segf, segf32.data(), segf32.size() * F4);
+    if (h->tma[2] || h->tma[3]) {
+      if (encode_tmaps(h, h->htmaps) != ATI_OK) {
+        if (e == cudaSuccess) e = cudaErrorInvalidValue;
+        g_tma_err = h->err;
+      } else {
+        up(h->ef.tmaps, h->htmaps.data(), sizeof(TmaMap) * h->htmaps.size());
+      }
+    }
     for (int nn = 1; nn <= 3; nn++) up(h->ef.lts[nn], h->hlts[nn].data(), sizeof(LTile) * h->hlts[nn].size());
     if (e == cudaSuccess) e = fast::seg_init();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   if (e != cudaSuccess) {
-    g_create_err = std::string("set-up copy: ") + cudaGetErrorString(e);
+    g_create_err = g_tma_err.empty() ? std::string("set-up copy: ") + cudaGetErrorString(e) : g_tma_err;
+    g_tma_err.clear();
     cudaFree(h->arena);
     delete h;
     return ATI_ECUDA;
@@ -1280,6 +1396,27 @@ extern "C" int ati_set_tiles(ati_handle_t *h, const int32_t in[4]) {
   std::fill(h->pw_pt, h->pw_pt + PW_KINDS, 0);  // every pointwise kernel on the pinned tiles
   apply_pw_tiles(h);
   drop_graphs(h);  // the step graphs hold the old grid shapes
+  return ATI_OK;
+}
+
+extern "C" int ati_set_options(ati_handle_t *h, int flags, int32_t *active) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
+  if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES)) return fail(h, ATI_EINVAL, "ati_set_options: unknown flag");
+  CK(cudaStreamSynchronize(h->st));
+  drop_graphs(h);
+  for (int nn = 2; nn <= 3; nn++) h->ef.tma[nn] = (flags & ATI_OPT_TMA) != 0 && h->tma[nn];
+  h->fused = (flags & ATI_OPT_FUSED_FACES) != 0;
+  if (active)
+    *active = (h->ef.tma[2] || h->ef.tma[3] ? ATI_OPT_TMA : 0) | (h->fused ? ATI_OPT_FUSED_FACES : 0) |
+              (h->ef.tma[2] ? ATI_OPT_TMA_ETA : 0) | (h->ef.tma[3] ? ATI_OPT_TMA_ZETA : 0);
+  return ATI_OK;
+}
+
+extern "C" int ati_set_spin_limit(ati_handle_t *h, int64_t polls) {
+  if (!h || polls < 0 || polls > 0xffffffffLL) return fail(h, ATI_EINVAL, "ati_set_spin_limit: bad argument");
+  CK(cudaStreamSynchronize(h->st));
+  drop_graphs(h);  // (the limit is a launch argument captured in the step graphs)
+  h->spin_limit = polls == 0 ? (1u << 24) : (unsigned)polls;
   return ATI_OK;
 }
 
@@ -1696,6 +1833,12 @@ static int filter_step_t(ati_handle *h, const Eng<R> &e) {
 }
 
 template <typename R>
+static cudaError_t face_pre(bool strict, const Eng<R> &e, cudaStream_t st, const FaceChain &c) {
+  if constexpr (std::is_same<R, float>::value) return fast::face_pre_f(e, st, c);
+  else return strict ? strict::face_pre_d(e, st, c) : fast::face_pre_d(e, st, c);
+}
+
+template <typename R>
 static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
   using C = EngineCalls<R>;
   const bool strict = h->cfg.precision == ATI_FP64_STRICT;
@@ -1758,6 +1901,36 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
     else if (g64) PROF(h, ATI_K_DIV, gust_apply64(st, h->dgust, h->ngust, h->ddelta64, ed.asz, ed.bsz, e.de, N));
     else PROF(h, ATI_K_DIV, gust_apply_d(st, h->dgust, h->ngust, h->ddelta, ed.asz, ed.bsz, e.de, N));
   }
+  if (h->fused) {
+    // the face chains fused: one cooperative launch before the RK update (characteristic boundaries of every
+    // direction, frame update) and one after it (wall, junctions, interface averaging), phases ordered by bounded
+    // grid barriers (src/Main3D.f90:780-952)
+    auto span = [&](const TaskRange &r) { return TaskSpan{tp(h, r), h->dcum + r.off, r.n, h->task_lines(r.off, r.n)}; };
+    FaceChain pre{}, post{};
+    pre.prep = span(h->tl_gcbc);
+    for (int d = 1; d <= 3; d++) pre.dir[d] = span(h->tl_gcbc_dir[d]);
+    pre.bar = h->dbar;
+    pre.limit = h->spin_limit;
+    pre.nk = nk;
+    post.prep = span(h->tl_wall);
+    post.pack = span(h->tl_pack);
+    for (int d = 1; d <= 3; d++) post.dir[d] = span(h->tl_avg_dir[d]);
+    post.jn = h->djn;
+    post.njct = h->njct;
+    post.jnk = h->jnk;
+    post.bar = h->dbar + 1;
+    post.limit = h->spin_limit;
+    post.nk = nk;
+    CK(cudaMemsetAsync(h->dbar, 0, sizeof(unsigned) * 2, st));
+    cudaError_t ce = cudaSuccess;
+    PROF(h, ATI_K_GCBC, ce = face_pre<R>(strict, e, st, pre));
+    if (ce != cudaSuccess) return fail(h, ATI_ECUDA, std::string("fused face chain: ") + cudaGetErrorString(ce));
+    PROF(h, ATI_K_RK, C::pw(strict, e, st, PW_RK));
+    PROF(h, ATI_K_AVERAGE, ce = (strict ? strict::face_post : fast::face_post)(ed, st, post));
+    if (ce != cudaSuccess) return fail(h, ATI_ECUDA, std::string("fused face chain: ") + cudaGetErrorString(ce));
+    CKL();
+    return ATI_OK;
+  }
   // characteristic boundary conditions (src/Main3D.f90:780-869)
   if (h->tl_gcbc.n) PROF(h, ATI_K_GCBC, C::face(strict, e, st, FK_GCBC_PREP, tp(h, h->tl_gcbc), h->tl_gcbc.n, h->tl_gcbc.maxline));
   for (int d = 1; d <= 3; d++)
@@ -1808,13 +1981,22 @@ static int read_flags(ati_handle *h, std::vector<Scalars> &sc) {
   return ATI_OK;
 }
 
+// the status a case's device flag stands for
+static int flag_status(ati_handle *h, int c, int flag) {
+  if (flag & FLAG_TIMEOUT)
+    return fail(h, ATI_ETIMEDOUT, "a bounded device wait of case " + std::to_string(c) + " gave up (flag " +
+                                      std::to_string(flag) + ")");
+  if (flag)
+    return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state of case " +
+                                       std::to_string(c) + " (flag " + std::to_string(flag) + ")");
+  return ATI_OK;
+}
+
 static int check_flag(ati_handle *h) {
   std::vector<Scalars> sc;
   if (int rc = read_flags(h, sc)) return rc;
   for (int c = 0; c < h->ncase; c++)
-    if (sc[c].flag)
-      return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state of case " +
-                                         std::to_string(c) + " (flag " + std::to_string(sc[c].flag) + ")");
+    if (sc[c].flag) return flag_status(h, c, sc[c].flag);
   return ATI_OK;
 }
 
@@ -1823,10 +2005,7 @@ extern "C" int ati_case_check(ati_handle_t *h, int cs) {
   if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
   std::vector<Scalars> sc;
   if (int rc = read_flags(h, sc)) return rc;
-  if (sc[cs].flag)
-    return fail(h, ATI_ENONFINITE, "non-finite or non-positive density/pressure in the state of case " +
-                                       std::to_string(cs) + " (flag " + std::to_string(sc[cs].flag) + ")");
-  return ATI_OK;
+  return flag_status(h, cs, sc[cs].flag);
 }
 
 extern "C" int ati_filter_step(ati_handle_t *h) {

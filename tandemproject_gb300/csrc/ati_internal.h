@@ -80,8 +80,11 @@ struct Scalars {
   double dtk;             // RK update factor of the current stage
   double aoa;
   unsigned long long cflmax[2];  // max reductions (bit patterns of doubles >= 0)
-  int flag;               // non-finite / non-positive state seen
+  int flag;               // bits 1, 2, 4: non-finite or non-positive state, CFL maxima or dt; FLAG_TIMEOUT: a bounded
+                          // device wait gave up
 };
+
+constexpr int FLAG_TIMEOUT = 256;
 
 // One face work item: (block, direction, side).
 struct FaceTask {

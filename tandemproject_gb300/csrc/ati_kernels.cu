@@ -12,10 +12,14 @@
 
 #include <cmath>
 #include <cstdint>
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
 
 #include "ati_convert.h"
 #include "ati_kernels.h"
+#include "ati_tma.h"
 
 #ifndef ATI_KNS
 #error "compile with -DATI_KNS=fast or -DATI_KNS=strict"
@@ -419,6 +423,9 @@ struct SweepArgs {
   int64_t recv_fs;
   TC *drva;
   const double *facu;  // FP64 fast path: scaled-factor rows (FU_RT per row)
+  const TmaMap *tmap;  // TMA staging (segmented eta/zeta sweeps): this array's tensor map of block b at tmap[b]
+  Scalars *scal;       // per-case flags (a bounded wait that gave up sets FLAG_TIMEOUT)
+  bool rowtiles;       // segmented eta tiles end with their grid row
 };
 
 // eta and zeta lines: one thread per line; consecutive threads own
@@ -718,15 +725,20 @@ __global__ void __launch_bounds__(XC_NL) k_sweep_xc(SweepArgs<TI, TO, TC> a) {
 // once, with no forward-value scratch.  The results differ from the
 // sequential solve by rounding only, and depend on the line length alone.
 // ---------------------------------------------------------------------------
-template <int NN, bool FILT, typename TI, typename TO>
+// TMA (eta and zeta derivative sweeps over FP32 inputs, blocks whose geometry a tensor map can describe): the
+// tile of each line group comes in as one tensor copy, [point][line] rows of SEG_LINES floats; eta tiles then
+// hold lines of one grid row only (the work queue's eta tiles start at row starts and multiples of 32 points)
+template <int NN, bool FILT, bool TMA, typename TI, typename TO>
 __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, TO, float> a, const float *rtab,
                                                                   int groups) {
+  static_assert(!TMA || (NN != 1 && std::is_same<TI, float>::value), "TMA staging: eta/zeta lines of FP32 inputs");
   extern __shared__ __align__(16) unsigned char seg_smem[];
-  constexpr int RS = SEG_LINES + 1;  // tile row stride in words: a warp's column reads and row reads are conflict-free
+  // tile row stride in words: with per-thread copies a warp writes a column (xi) or a row, so one word of padding
+  // keeps both conflict-free; a TMA tile is dense (lanes read rows of 32 consecutive words, conflict-free)
+  constexpr int RS = TMA ? SEG_LINES : SEG_LINES + 1;
   constexpr bool ASYNC = std::is_same<TI, float>::value;
+  __shared__ uint64_t tbar[SEG_GROUPS];  // TMA completion, one barrier per line group
   const int nwarp = (int)(blockDim.x >> 5);
-  float2 *cf = reinterpret_cast<float2 *>(seg_smem);  // [segment][line] values a segment passes on
-  float2 *cx = cf + nwarp * SEG_LINES;                 // [segment][line] values a segment receives
   const LTile LT = a.lt[blockIdx.x];
   const BlockDev &B = a.blk[LT.b];
   const int f = blockIdx.y;
@@ -736,8 +748,23 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   // its own tile; otherwise the CTA is one group and warp w solves segment w of its lines
   const int gsz = groups > 1 ? 1 : nwarp, grp = w / gsz, wl = w - grp * gsz;
   const int t0 = LT.t0 + grp * SEG_LINES;
-  const int nl = min(SEG_LINES, (int)B.nbsize[NN] - t0);  // (no lines: the group idles)
-  float *tile = reinterpret_cast<float *>(cx + nwarp * SEG_LINES) + (int64_t)grp * L * (SEG_LINES + 1);
+  // lines of the group (none: the group idles); an eta tile built for TMA ends with its grid row
+  const int nx = B.lxi + 1;
+  const int nl = (NN == 2 && a.rowtiles) ? min(SEG_LINES, nx - LT.t0 % nx - grp * SEG_LINES)
+                                         : min(SEG_LINES, (int)B.nbsize[NN] - t0);
+  // shared memory: the groups' tiles (TMA: first, 128-byte aligned), then the segment carries
+  float *tiles;
+  if constexpr (TMA) {
+    const uint32_t pad = (128u - (smem_u32(seg_smem) & 127u)) & 127u;
+    tiles = reinterpret_cast<float *>(seg_smem + pad);
+  } else {
+    tiles = reinterpret_cast<float *>(seg_smem + (size_t)nwarp * SEG_LINES * 2 * sizeof(float2));
+  }
+  const int ngrp = groups > 1 ? groups : 1;
+  float2 *cf = TMA ? reinterpret_cast<float2 *>(tiles + (int64_t)ngrp * L * RS)
+                   : reinterpret_cast<float2 *>(seg_smem);  // [segment][line] values a segment passes on
+  float2 *cx = cf + nwarp * SEG_LINES;                       // [segment][line] values a segment receives
+  float *tile = tiles + (int64_t)grp * L * RS;
   int64_t base = 0, stride = 1;
   int jk = 0, Lg = 0;
   line_geom<NN>(B, t0 + lane, base, stride, jk, Lg);
@@ -746,11 +773,32 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
 
   // 1. stage the lines (inputs wider than FP32 lose their offset and are rounded on the way in);
   // source and destination pointers walk by constant steps
+  bool tma_ok = true;
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < ngrp; q++) mbar_init(&tbar[q], 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (nl > 0) {
+      if (wl == 0 && lane == 0) {
+        const TmaMap *tm = a.tmap + LT.b;
+        tmap_acquire(tm);
+        mbar_expect_tx(&tbar[grp], (uint32_t)(L * SEG_LINES * sizeof(float)));
+        if constexpr (NN == 2) tma_load_4d(tile, tm, LT.t0 % nx + grp * SEG_LINES, 0, LT.t0 / nx, f, &tbar[grp]);
+        else tma_load_3d(tile, tm, t0, 0, f, &tbar[grp]);
+      }
+      tma_ok = mbar_wait_bounded(&tbar[grp], 0);
+      if (!tma_ok && lane == 0) atomicOr(&a.scal[B.cs].flag, FLAG_TIMEOUT);
+    }
+  }
   auto stage = [&](float *dst, const TI *src) {
     if constexpr (ASYNC) cp_async<4>(dst, src);
     else *dst = cvt_in<TI, float>(__ldg(src), ofs);
   };
-  if constexpr (NN == 1) {
+  if constexpr (TMA) {
+    // (staged by the tensor copy above)
+  } else if constexpr (NN == 1) {
     // xi lines are contiguous: a warp copies one line at a time, lanes along the line
     const TI *src0 = in + B.off + (int64_t)t0 * L;
     for (int ln = wl; ln < nl; ln += gsz) {
@@ -776,7 +824,7 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   __syncthreads();
 
   const int S = seg_count(L);
-  const bool act = wl < S && lane < nl;
+  const bool act = wl < S && lane < nl && tma_ok;  // (a group whose tile never landed computes nothing)
   const int s0 = seg_start(wl, L, S), s1 = seg_start(wl + 1, L, S);
   float *col = tile + lane;
   // the block's row table, SEG_RT floats per row (layout at SEG_RT)
@@ -1059,6 +1107,11 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
       }
       for (; i < L; i += 32) wr(lb + i, tile[i * RS + ln], FILT ? in[lb + i] : (TI)0);
     }
+  }
+  if constexpr (TMA) {
+    // a tile copy that did not land in time: wait once more (bounded) so that no copy into this CTA's shared
+    // memory is left in flight when it exits
+    if (!tma_ok) (void)mbar_wait_bounded(&tbar[grp], 0);
   }
 }
 
@@ -1829,10 +1882,7 @@ __device__ __forceinline__ void face_point(const BlockDev &B, int nn, int ip, in
 
 // drva = X * (J * (ra0*drva + ra1*de)) (src/Main3D.f90:780-795)
 template <typename R>
-__global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
-  const FaceTask T = tasks[blockIdx.y];
-  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jk >= T.nline) return;
+__device__ __forceinline__ void gcbc_prep_item(const Eng<R> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const Scheme &S = e.sc[B.cs];
   const Scalars &SC = e.scal[B.cs];
@@ -1874,14 +1924,18 @@ __global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
   }
 }
 
+template <typename R>
+__global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
+  const FaceTask T = tasks[blockIdx.y];
+  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk < T.nline) gcbc_prep_item<R>(e, T, jk);
+}
+
 // GCBC/GCIC application for the faces of one direction (src/Main3D.f90:817-869),
 // launched once per direction in the reference's order so that edge points
 // touched by faces of two directions accumulate in the same order
 template <typename R>
-__global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
-  const FaceTask T = tasks[blockIdx.y];
-  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jk >= T.nline) return;
+__device__ __forceinline__ void gcbc_apply_item(const Eng<R> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const Scheme &S = e.sc[B.cs];
   const Scalars &SC = e.scal[B.cs];
@@ -1952,11 +2006,15 @@ __global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
   }
 }
 
-// wall temperature and velocity (src/Main3D.f90:886-895), FP64 state
-__global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
+template <typename R>
+__global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jk >= T.nline) return;
+  if (jk < T.nline) gcbc_apply_item<R>(e, T, jk);
+}
+
+// wall temperature and velocity (src/Main3D.f90:886-895), FP64 state
+__device__ __forceinline__ void wall_item(const Eng<double> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const Scheme &S = e.sc[B.cs];
   const Scalars &SC = e.scal[B.cs];
@@ -1977,14 +2035,15 @@ __global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
   e.qa[g + 4 * N] = rp * q5 + ra2 * (ra0 * q1 + 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
 }
 
+__global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
+  const FaceTask T = tasks[blockIdx.y];
+  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk < T.nline) wall_item(e, T, jk);
+}
+
 // junction averaging of the corner lines shared by four blocks
 // (src/SingleTurbulence3D.f90:378-443)
-__global__ void k_junction(Eng<double> e, const JunctionDev *jn, int njct) {
-  const int jx = blockIdx.y;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jx >= njct) return;
-  const JunctionDev J = jn[jx];
-  if (k >= J.nk) return;
+__device__ __forceinline__ void junction_item(const Eng<double> &e, const JunctionDev &J, int k) {
   const int64_t N = e.N;
   int64_t g[4];
 #pragma unroll
@@ -2002,12 +2061,17 @@ __global__ void k_junction(Eng<double> e, const JunctionDev *jn, int njct) {
     for (int m = 0; m < 5; m++) e.qa[g[q] + m * N] = avg[m];
 }
 
+__global__ void k_junction(Eng<double> e, const JunctionDev *jn, int njct) {
+  const int jx = blockIdx.y;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jx >= njct) return;
+  const JunctionDev J = jn[jx];
+  if (k < J.nk) junction_item(e, J, k);
+}
+
 // interface averaging: pack qa of every BC 30/35/45 face (src/Main3D.f90:908-914)
 // into the FP64 face buffer drva of the set-up engine
-__global__ void k_pack(Eng<double> e, const FaceTask *tasks) {
-  const FaceTask T = tasks[blockIdx.y];
-  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jk >= T.nline) return;
+__device__ __forceinline__ void pack_item(const Eng<double> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   int i, j, k;
   face_point(B, T.nn, T.ip, jk, i, j, k);
@@ -2021,11 +2085,14 @@ __global__ void k_pack(Eng<double> e, const FaceTask *tasks) {
   e.cnt[g] = 1.0;
 }
 
-// interface averaging of the faces of one direction (src/Main3D.f90:926-952)
-__global__ void k_avg(Eng<double> e, const FaceTask *tasks) {
+__global__ void k_pack(Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jk >= T.nline) return;
+  if (jk < T.nline) pack_item(e, T, jk);
+}
+
+// interface averaging of the faces of one direction (src/Main3D.f90:926-952)
+__device__ __forceinline__ void avg_item(const Eng<double> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const BlockDev &Bn = e.blk[T.nb_b];
   int i, j, k;
@@ -2049,6 +2116,12 @@ __global__ void k_avg(Eng<double> e, const FaceTask *tasks) {
     drvb[jk + nbs * (q + 5 * T.ip)] = dv[q];
     e.qa[g + q * N] = w * ((cnt - 1.0) * qv[q] + dv[q]);
   }
+}
+
+__global__ void k_avg(Eng<double> e, const FaceTask *tasks) {
+  const FaceTask T = tasks[blockIdx.y];
+  const int jk = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jk < T.nline) avg_item(e, T, jk);
 }
 
 // ---------------------------------------------------------------------------
@@ -2088,11 +2161,7 @@ __device__ void d_movef(const Scheme &S, Scalars &s, double dtko, double dtk) {
   }
 }
 
-__global__ void k_scalar(const Scheme *sc, Scalars *scal, int ncase, int op, int nk) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;  // one thread per case
-  if (c >= ncase) return;
-  const Scheme &S = sc[c];
-  Scalars &s = scal[c];
+__device__ void scalar_op(const Scheme &S, Scalars &s, int op, int nk) {
   const int nkrk = S.nkrk;
   if (op == SC_MOVEF_A) {
     const double dtko = s.dt * min(max(nk - 2, 0), 1) / (nkrk - nk + 3);
@@ -2127,6 +2196,137 @@ __global__ void k_scalar(const Scheme *sc, Scalars *scal, int ncase, int op, int
   } else if (op == SC_INIT) {
     d_movef(S, s, 0.0, 0.0);
   }
+}
+
+__global__ void k_scalar(const Scheme *sc, Scalars *scal, int ncase, int op, int nk) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;  // one thread per case
+  if (c < ncase) scalar_op(sc[c], scal[c], op, nk);
+}
+
+// ---------------------------------------------------------------------------
+// Fused face chains.  The face and scalar work around the RK update is a chain of short, latency-bound steps
+// (src/Main3D.f90:780-952): GCBC preparation, the application of each direction in turn, the frame update; then,
+// after the update, the wall, the junctions, the face packing and the averaging of each direction.  Each chain is
+// one cooperative launch (all CTAs resident) whose phases are separated by grid barriers.  A barrier's wait is
+// bounded: after `limit` polls the CTA gives up, stops working, and every case of the handle gets FLAG_TIMEOUT
+// (the host returns ATI_ETIMEDOUT); the other CTAs then time out at the same or the next barrier, so the launch
+// always ends.  The items are those of the per-face kernels, in the same order per point, so the results are
+// bit-identical to the unfused chain.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// arrive at the grid barrier (count: CTA arrivals so far) and wait until `target` arrivals, at most `limit`
+// polls; true if all arrived
+__device__ bool grid_barrier(unsigned *count, unsigned target, unsigned limit) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // this CTA's writes before its arrival
+    atomicAdd(count, 1u);
+    int ok = 1;
+    for (unsigned k = 0; ld_acquire_u32(count) < target; k++) {
+      if (k >= limit) {
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// the face lines of a task range as one index space: item idx lies in task q with cum[q] - cum[0] <= idx
+__device__ __forceinline__ int span_find(const TaskSpan &sp, int64_t idx) {
+  const int64_t base = sp.cum[0];
+  int lo = 0, hi = sp.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sp.cum[mid] - base <= idx) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+template <class F>
+__device__ __forceinline__ void span_for(const TaskSpan &sp, F &&f) {
+  const int64_t gs = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < sp.total; idx += gs) {
+    const int q = span_find(sp, idx);
+    f(sp.t[q], (int)(idx - (sp.cum[q] - sp.cum[0])));
+  }
+}
+
+__device__ __forceinline__ void flag_all_timeout(Scalars *scal, int ncase) {
+  if (threadIdx.x == 0)
+    for (int c = 0; c < ncase; c++) atomicOr(&scal[c].flag, FLAG_TIMEOUT);
+}
+
+// before the RK update: GCBC preparation, application per direction, frame update (SC_MOVEF_B)
+template <typename R>
+__global__ void __launch_bounds__(256) k_face_pre(Eng<R> e, FaceChain c) {
+  unsigned target = 0;
+  bool ok = true;
+  auto sync = [&]() {
+    target += gridDim.x;
+    ok = grid_barrier(c.bar, target, c.limit);
+  };
+  if (c.prep.total) {
+    span_for(c.prep, [&](const FaceTask &T, int jk) { gcbc_prep_item<R>(e, T, jk); });
+    sync();
+  }
+  for (int d = 1; d <= 3 && ok; d++) {
+    if (!c.dir[d].total) continue;
+    span_for(c.dir[d], [&](const FaceTask &T, int jk) { gcbc_apply_item<R>(e, T, jk); });
+    sync();
+  }
+  if (!ok) {
+    flag_all_timeout(e.scal, e.ncase);
+    return;
+  }
+  if (blockIdx.x == 0)
+    for (int cs = threadIdx.x; cs < e.ncase; cs += blockDim.x) scalar_op(e.sc[cs], e.scal[cs], SC_MOVEF_B, c.nk);
+}
+
+// after the RK update: wall, junctions, face packing, averaging per direction
+__global__ void __launch_bounds__(256) k_face_post(Eng<double> e, FaceChain c) {
+  unsigned target = 0;
+  bool ok = true;
+  auto sync = [&]() {
+    target += gridDim.x;
+    ok = grid_barrier(c.bar, target, c.limit);
+  };
+  if (c.prep.total) {  // (the wall faces)
+    span_for(c.prep, [&](const FaceTask &T, int jk) { wall_item(e, T, jk); });
+    sync();
+  }
+  if (ok && c.njct) {
+    const int64_t gs = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)c.njct * c.jnk; idx += gs) {
+      const JunctionDev J = c.jn[idx / c.jnk];
+      const int k = (int)(idx % c.jnk);
+      if (k < J.nk) junction_item(e, J, k);
+    }
+    sync();
+  }
+  if (ok && c.pack.total) {
+    span_for(c.pack, [&](const FaceTask &T, int jk) { pack_item(e, T, jk); });
+    sync();
+  }
+  int last = 0;
+  for (int d = 1; d <= 3; d++)
+    if (c.dir[d].total) last = d;
+  for (int d = 1; d <= 3 && ok; d++) {
+    if (!c.dir[d].total) continue;
+    span_for(c.dir[d], [&](const FaceTask &T, int jk) { avg_item(e, T, jk); });
+    if (d != last) sync();
+  }
+  if (!ok) flag_all_timeout(e.scal, e.ncase);
 }
 
 // metrics (src/Main3D.f90:378-413): non-conservative cross products and J from
@@ -2221,9 +2421,13 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   a.recv = e.recv;
   a.recv_fs = e.F * 6;
   a.drva = e.drva;
+  a.tmap = nullptr;
+  a.scal = e.scal;
+  a.rowtiles = false;
   if constexpr (std::is_same<TC, float>::value) {
     // the mixed path: segmented solves over tiles of SEG_LINES lines
     const float *seg = filt ? e.segf : e.segd;
+    a.rowtiles = e.eta_rowtiles;
     if (seg && e.nsegc[nn] > 0 && (filt || !io.out2)) {  // (a derivative with a second output: sequential kernels)
       for (int c = 0; c < e.nsegc[nn]; c++) {  // one launch per class of equal segment counts
         const SegClass &C = e.segc[nn][c];
@@ -2233,7 +2437,18 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
         const int nt = SEG_LINES * (G > 1 ? G : seg_count(C.maxlen));
         const size_t smem = seg_smem_bytes(C.maxlen, G);
         const dim3 g(C.n, io.nf);
-#define ATI_SEG(D, F) k_sweep_seg<D, F, TI, TO><<<g, nt, smem, st>>>(a, seg, G)
+#define ATI_SEG(D, F) k_sweep_seg<D, F, false, TI, TO><<<g, nt, smem, st>>>(a, seg, G)
+        if constexpr (std::is_same<TI, float>::value) {
+          // eta/zeta derivative sweeps of an array with tensor maps: tiles staged by TMA
+          const int arr = io.in == e.prim ? 0 : (io.in == e.flx + (int64_t)(nn - 1) * e.N ? 1 : -1);
+          if (!filt && nn >= 2 && e.tma[nn] && arr >= 0) {
+            a.tmap = e.tmaps + (int64_t)(arr * 2 + nn - 2) * e.nblk;
+            const size_t sm = smem + 128;  // (alignment of the tensor copies' destination)
+            if (nn == 2) k_sweep_seg<2, false, true, TI, TO><<<g, nt, sm, st>>>(a, seg, G);
+            else k_sweep_seg<3, false, true, TI, TO><<<g, nt, sm, st>>>(a, seg, G);
+            continue;
+          }
+        }
         if (!filt) { if (nn == 1) ATI_SEG(1, false); else if (nn == 2) ATI_SEG(2, false); else ATI_SEG(3, false); }
         else { if (nn == 1) ATI_SEG(1, true); else if (nn == 2) ATI_SEG(2, true); else ATI_SEG(3, true); }
 #undef ATI_SEG
@@ -2265,17 +2480,30 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   }
 }
 
-// the segmented sweeps may take more than the default 48 KB of dynamic shared memory
+// the segmented sweeps may take more than the default 48 KB of dynamic shared memory: each kernel may use what the
+// device allows a block beyond the kernel's own static shared memory
+template <typename K>
+static cudaError_t seg_attr_one(K kernel) {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  cudaFuncAttributes fa{};
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+}
 template <typename TI, typename TO>
 static cudaError_t seg_attr() {
-  const int v = (int)SEG_SMEM_MAX;
-  const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  cudaError_t e = cudaFuncSetAttribute(k_sweep_seg<1, false, TI, TO>, A, v);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<2, false, TI, TO>, A, v);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<3, false, TI, TO>, A, v);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<1, true, TI, TO>, A, v);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<2, true, TI, TO>, A, v);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sweep_seg<3, true, TI, TO>, A, v);
+  cudaError_t e = seg_attr_one(k_sweep_seg<1, false, false, TI, TO>);
+  if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<2, false, false, TI, TO>);
+  if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<3, false, false, TI, TO>);
+  if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<1, true, false, TI, TO>);
+  if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<2, true, false, TI, TO>);
+  if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<3, true, false, TI, TO>);
+  if constexpr (std::is_same<TI, float>::value) {
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<2, false, true, TI, TO>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<3, false, true, TI, TO>);
+  }
   return e;
 }
 // the mixed path's kernels with more than 48 KB of dynamic shared memory: the segmented sweeps and the staged
@@ -2373,6 +2601,60 @@ void face_f(const Eng<float> &e, cudaStream_t st, int which, const FaceTask *tas
     case FK_GCBC_APPLY: k_gcbc_apply<float><<<grid, tpb, 0, st>>>(e, tasks); break;
     default: break;  // wall, pack and averaging act on the FP64 state: face_d
   }
+}
+
+// cooperative launch of a fused chain: at most one CTA of 256 threads per SM (the chains' work is a few lines per
+// thread), never more than the kernel can keep resident at once
+static int coop_cap(const void *kernel) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, int> cap;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cap.find({dev, kernel});
+  if (it != cap.end()) return it->second;
+  int nsm = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess) {
+    cudaGetLastError();
+    per_sm = 0;
+  }
+  const int c = per_sm >= 1 ? (nsm > 0 ? nsm : 1) : 0;  // one CTA per SM (0: the kernel cannot run)
+  cap[{dev, kernel}] = c;
+  return c;
+}
+template <typename K, typename... A>
+static cudaError_t coop_launch(K kernel, int want, cudaStream_t st, A... args) {
+  const int cap = coop_cap((const void *)kernel);
+  if (cap < 1) return cudaErrorCooperativeLaunchTooLarge;
+  const int g = want < 1 ? 1 : (want < cap ? want : cap);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+static int chain_ctas(const FaceChain &c) {
+  int64_t items = c.prep.total;
+  for (int d = 1; d <= 3; d++) items = items > c.dir[d].total ? items : c.dir[d].total;
+  items = items > c.pack.total ? items : c.pack.total;
+  items = items > (int64_t)c.njct * c.jnk ? items : (int64_t)c.njct * c.jnk;
+  return (int)((items + 255) / 256);
+}
+cudaError_t face_pre_d(const Eng<double> &e, cudaStream_t st, const FaceChain &c) {
+  return coop_launch(k_face_pre<double>, chain_ctas(c), st, e, c);
+}
+cudaError_t face_pre_f(const Eng<float> &e, cudaStream_t st, const FaceChain &c) {
+  return coop_launch(k_face_pre<float>, chain_ctas(c), st, e, c);
+}
+cudaError_t face_post(const Eng<double> &e, cudaStream_t st, const FaceChain &c) {
+  return coop_launch(k_face_post, chain_ctas(c), st, e, c);
 }
 
 void metric_divergence(const Eng<double> &e, cudaStream_t st, const double *d3, float *gm) {

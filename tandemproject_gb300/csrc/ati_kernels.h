@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "ati_internal.h"
+#include "ati_tma.h"
 
 namespace ati {
 
@@ -80,6 +81,13 @@ struct Eng {
   // mixed path only (the fluxes there are taken relative to the freestream):
   const R *gm;          // metric divergence sum_d D_d(metric_d) per component (3 planes)
   const R *drvm;        // its line-end values per direction, drva layout (components 0..2)
+  // TMA staging of the segmented eta/zeta derivative sweeps (mixed path): tensor maps of the primitive (array 0)
+  // and flux (array 1) planes per direction and block, tmaps[(array * 2 + nn - 2) * nblk + b]; tma[nn] when
+  // every block's geometry allows them and the option is on
+  const TmaMap *tmaps;
+  int nblk;
+  bool tma[4];
+  bool eta_rowtiles;    // the segmented eta tiles hold the lines of one grid row each (built for TMA staging)
 };
 
 // The mixed path (R = float) works on deviations from the freestream
@@ -135,7 +143,7 @@ constexpr size_t SG_SMEM_FW = 48 * 1024;
 // the line length alone, so a block's results do not depend on the other
 // blocks or cases of a handle.  Lines up to SEG_LMAX points fit the tile.
 constexpr int SEG_LINES = 32, SEG_ROWS = 48, SEG_MAX = 16, SEG_LMAX = 1600;
-constexpr size_t SEG_SMEM_MAX = 227 * 1024;
+constexpr size_t SEG_SMEM_MAX = 227 * 1024 - 64;  // (a few bytes of static shared memory per kernel)
 __host__ __device__ inline int seg_count(int L) {
   const int s = (L + SEG_ROWS - 1) / SEG_ROWS;
   return s < 1 ? 1 : (s > SEG_MAX ? SEG_MAX : s);
@@ -176,6 +184,26 @@ inline size_t seg_smem_bytes(int maxlen, int groups) {
   return (size_t)nwarp * SEG_LINES * 2 * 2 * sizeof(float) + (size_t)groups * maxlen * (SEG_LINES + 1) * sizeof(float);
 }
 
+// The face lines of a range of face tasks as one index space (fused face chains): tasks t[0..n), cum[q] the
+// running count of lines before task q (cum[n] - cum[0] = total).
+struct TaskSpan {
+  const FaceTask *t;
+  const int64_t *cum;
+  int n;
+  int64_t total;
+};
+// One fused face chain launch: before the RK update prep = the GCBC faces, dir[d] = the GCBC faces of direction d;
+// after it prep = the wall faces, pack = the averaged faces, dir[d] = the averaged faces of direction d, plus the
+// junction lines.  bar: the grid-barrier counter (zero at launch), limit: polls a barrier wait may take.
+struct FaceChain {
+  TaskSpan prep, pack, dir[4];
+  const JunctionDev *jn;
+  int njct, jnk;
+  unsigned *bar;
+  unsigned limit;
+  int nk;
+};
+
 // per-field offsets of a closure (mpigo) over a wider input type
 template <typename TI>
 struct FieldOfs {
@@ -206,6 +234,9 @@ struct FieldOfs {
   void junction(const Eng<double> &e, cudaStream_t st, const JunctionDev *jn, int njct, int nk);                   \
   void scalar(const Eng<double> &e, cudaStream_t st, int op, int nk);                                             \
   void metrics(const Eng<double> &e, cudaStream_t st, const double *xyz_d);                                       \
+  cudaError_t face_pre_d(const Eng<double> &e, cudaStream_t st, const FaceChain &c);                               \
+  cudaError_t face_pre_f(const Eng<float> &e, cudaStream_t st, const FaceChain &c);                                \
+  cudaError_t face_post(const Eng<double> &e, cudaStream_t st, const FaceChain &c);                                \
   void forces_d(const Eng<double> &e, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area,       \
                 const double *wnor, const int64_t *woff, double *out);                                             \
   void forces_f(const Eng<float> &e, cudaStream_t st, const FaceTask *tasks, int ntask, const double *area,        \

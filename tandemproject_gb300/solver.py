@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libati.so")
 ATI_OK, ATI_EINVAL, ATI_ENOMEM, ATI_ECUDA, ATI_ENONFINITE, ATI_ETIMEDOUT, ATI_ESTATE = range(7)
 F_QA, F_QO, F_DE, F_RR, F_SS, F_XIM, F_ETM, F_ZEM, F_P, F_YACO, F_STRESS, F_SPONGE, F_CP = range(13)
 FACE_DRVA, FACE_DRVB, FACE_RECV, FACE_CM = range(4)
+OPT_TMA, OPT_FUSED_FACES, OPT_TMA_ETA, OPT_TMA_ZETA = 1, 2, 4, 8
 NCOMP = {F_QA: 5, F_QO: 5, F_DE: 5, F_RR: 3, F_SS: 3, F_XIM: 3, F_ETM: 3, F_ZEM: 3, F_P: 1, F_YACO: 1,
          F_STRESS: 9, F_SPONGE: 2, F_CP: 1}
 
@@ -77,6 +78,8 @@ SIGNATURES = {
     "ati_jacobian_sign": ([_vp, _vp], ctypes.c_int),
     "ati_tiles": ([_vp, _vp], ctypes.c_int),
     "ati_set_tiles": ([_vp, _vp], ctypes.c_int),
+    "ati_set_options": ([_vp, _i32, _vp], ctypes.c_int),
+    "ati_set_spin_limit": ([_vp, ctypes.c_int64], ctypes.c_int),
     "ati_check_conversions": ([ctypes.c_int64, _vp], ctypes.c_int),
     "ati_check_recip": ([ctypes.c_int64, _dp], ctypes.c_int),
     "ati_turbulence_modes": ([_vp, _i32, _vp, _vp], ctypes.c_int),
@@ -279,6 +282,20 @@ class Case:
         """Pin the eta/zeta lines per CTA and points per tile (0 keeps the current one)."""
         t = (ctypes.c_int32 * 4)(0, eta, zeta, points)
         self._chk(self.L.ati_set_tiles(self.h, t))
+
+    def set_options(self, tma=True, fused_faces=True):
+        """Kernel options (results do not depend on them): TMA staging of the mixed path's segmented eta/zeta
+        sweeps, fused face chains.  Returns the options in effect as a dict."""
+        a = ctypes.c_int32()
+        self._chk(self.L.ati_set_options(self.h, (OPT_TMA if tma else 0) | (OPT_FUSED_FACES if fused_faces else 0),
+                                         ctypes.byref(a)))
+        v = a.value
+        return {"tma_eta": bool(v & OPT_TMA_ETA), "tma_zeta": bool(v & OPT_TMA_ZETA),
+                "fused_faces": bool(v & OPT_FUSED_FACES)}
+
+    def set_spin_limit(self, polls):
+        """Polls a device-side barrier wait may take before it gives up (0: the default)."""
+        self._chk(self.L.ati_set_spin_limit(self.h, int(polls)))
 
     def jacobian_sign(self):
         """Per block: bit 0 some J > 0, bit 1 some J < 0, bit 2 J zero or not finite."""

@@ -92,3 +92,48 @@ def test_wait_timeout_rejects_bad_values(ati_lib):
         with pytest.raises(AtiError):
             c.set_wait_timeout(v)
     c.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_fused_face_chains_bit_identical(ati_lib, precision):
+    """The fused face chains (two cooperative launches a stage) give the per-face
+    kernels' results bit for bit, on a batch of uneven cases."""
+    from tandemproject_gb300.config import FP64, MIXED
+    from tandemproject_gb300.solver import setup_batch
+    prec = MIXED if precision == "mixed" else FP64
+    cfgs = [c.replace(precision=prec) for c in _cases()]
+    a = setup_batch(cfgs)
+    b = setup_batch(cfgs)
+    assert a.set_options(fused_faces=True)["fused_faces"]
+    assert not b.set_options(fused_faces=False)["fused_faces"]
+    a.step(9)
+    b.step(9)
+    for blk in range(sum(c.nblocks for c in cfgs)):
+        assert np.array_equal(a.get_state(blk), b.get_state(blk)), blk
+    a.close()
+    b.close()
+
+
+def test_device_barrier_wait_times_out(ati_lib):
+    """A grid barrier of the fused face chains gives up after the handle's spin
+    limit: with a limit of one poll the waiting CTAs stop, every case is marked
+    and the step returns ATI_ETIMEDOUT; the handle stays usable (re-initialised,
+    it steps normally)."""
+    from tandemproject_gb300.config import small_case
+    from tandemproject_gb300.solver import AtiError, setup_case
+    c = setup_case(small_case())
+    assert c.set_options(fused_faces=True)["fused_faces"]
+    c.step(2)
+    c.set_spin_limit(1)
+    with pytest.raises(AtiError) as ei:
+        c.step(4)
+    assert ei.value.code == ATI_ETIMEDOUT
+    with pytest.raises(AtiError) as ei:
+        c.check()
+    assert ei.value.code == ATI_ETIMEDOUT
+    c.set_spin_limit(0)
+    c.init()
+    c.step(3)
+    c.check()
+    assert np.all(np.isfinite(c.get_state(0)))
+    c.close()
