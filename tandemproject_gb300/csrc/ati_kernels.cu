@@ -1789,6 +1789,14 @@ __global__ void k_rk(Eng<R> e) {
 // (src/Subroutines3D.f90:235-324) and the GCBC/GCIC loops of
 // src/Main3D.f90:780-869
 // ---------------------------------------------------------------------------
+// Reads of the arrays the face items modify (de, the face buffers, qa and the visit counts) bypass the SM's L1
+// cache (ld.global.cg): in a fused face chain a phase reads values that other SMs wrote in an earlier phase of the
+// same launch, and a line this SM cached before could be stale.  The per-face kernels read the same way.
+template <typename T>
+__device__ __forceinline__ T ldm(const T *p) {
+  return __ldcg(p);
+}
+
 template <typename R>
 struct Elem {
   R rhoi, ao, aoi, ve[3], hv2, vn, vs;
@@ -1912,8 +1920,9 @@ __device__ __forceinline__ void gcbc_prep_item(const Eng<R> &e, const FaceTask &
   const R yac = e.yaco[g];
 #pragma unroll
   for (int q = 0; q < 5; q++) {
-    if constexpr (Freestream<R>::on) v[q] = yac * (ra0 * (drva[jk + nbs * (q + 5 * ip)] + dinf[q]) + ra1 * e.de[g + q * N]);
-    else v[q] = yac * (ra0 * drva[jk + nbs * (q + 5 * ip)] + ra1 * e.de[g + q * N]);
+    if constexpr (Freestream<R>::on)
+      v[q] = yac * (ra0 * (ldm(drva + jk + nbs * (q + 5 * ip)) + dinf[q]) + ra1 * ldm(e.de + g + q * N));
+    else v[q] = yac * (ra0 * ldm(drva + jk + nbs * (q + 5 * ip)) + ra1 * ldm(e.de + g + q * N));
   }
 #pragma unroll
   for (int r = 0; r < 5; r++) {
@@ -1952,7 +1961,7 @@ __device__ __forceinline__ void gcbc_apply_item(const Eng<R> &e, const FaceTask 
   eleme(S, e, g, cm, umf, el);
   R cha[5], d0[5];
 #pragma unroll
-  for (int q = 0; q < 5; q++) { d0[q] = drva[jk + nbs * (q + 5 * ip)]; cha[q] = d0[q]; }
+  for (int q = 0; q < 5; q++) { d0[q] = ldm(drva + jk + nbs * (q + 5 * ip)); cha[q] = d0[q]; }
   if (np == 10) {
     if (ra0 * (el.vn + el.vs + el.ao) > (R)0) cha[3] = 0;
     if (ra0 * (el.vn + el.vs - el.ao) > (R)0) cha[4] = 0;
@@ -1968,7 +1977,7 @@ __device__ __forceinline__ void gcbc_apply_item(const Eng<R> &e, const FaceTask 
     R dha[5];
 #pragma unroll
     for (int q = 0; q < 5; q++) {
-      dha[q] = nbr[jk + nbs * (q + 5 * (1 - ip))];
+      dha[q] = ldm(nbr + jk + nbs * (q + 5 * (1 - ip)));
       drvb[jk + nbs * (q + 5 * ip)] = dha[q];
     }
     if (ra0 * (el.vn + el.vs) > (R)0) { cha[0] = dha[0]; cha[1] = dha[1]; cha[2] = dha[2]; }
@@ -1996,7 +2005,7 @@ __device__ __forceinline__ void gcbc_apply_item(const Eng<R> &e, const FaceTask 
   for (int ii = 0; ii <= MBCI; ii++) {
     g2[ii] = B.off + idx3(B.lxi, B.let, i + iq * ii, j, k, nn);
 #pragma unroll
-    for (int q = 0; q < 5; q++) dv[ii][q] = e.de[g2[ii] + q * N];
+    for (int q = 0; q < 5; q++) dv[ii][q] = ldm(e.de + g2[ii] + q * N);
   }
 #pragma unroll
   for (int ii = 0; ii <= MBCI; ii++) {
@@ -2026,7 +2035,8 @@ __device__ __forceinline__ void wall_item(const Eng<double> &e, const FaceTask &
   const double rp = e.rpex[T.wall_off + jk];
   const double ra2 = 1.0 - rp, ra3 = 1.0 - ra1 * ra2;
   // the point's state read before any store (rho is not written here)
-  const double q1 = e.qa[g], m2 = e.qa[g + N], m3 = e.qa[g + 2 * N], m4 = e.qa[g + 3 * N], q5 = e.qa[g + 4 * N];
+  const double q1 = ldm(e.qa + g), m2 = ldm(e.qa + g + N), m3 = ldm(e.qa + g + 2 * N), m4 = ldm(e.qa + g + 3 * N),
+               q5 = ldm(e.qa + g + 4 * N);
   const double fctr = (1.0 - ra3) * q1;
   const double q2 = ra3 * m2 - fctr * SC.umf[1];
   const double q3 = ra3 * m3 - fctr * SC.umf[2];
@@ -2051,9 +2061,10 @@ __device__ __forceinline__ void junction_item(const Eng<double> &e, const Juncti
   double avg[5];
 #pragma unroll
   for (int m = 0; m < 5; m++) {
-    const double d1 = e.qa[g[0] + m * N], d2 = e.qa[g[1] + m * N], d3 = e.qa[g[2] + m * N], d4 = e.qa[g[3] + m * N];
+    const double d1 = ldm(e.qa + g[0] + m * N), d2 = ldm(e.qa + g[1] + m * N), d3 = ldm(e.qa + g[2] + m * N),
+                 d4 = ldm(e.qa + g[3] + m * N);
     if (m == 0 || m == 4) avg[m] = 0.25 * (d1 + d2 + d3 + d4);
-    else avg[m] = 0.5 * (e.qa[g[J.pa - 1] + m * N] + e.qa[g[J.pb - 1] + m * N]);
+    else avg[m] = 0.5 * (ldm(e.qa + g[J.pa - 1] + m * N) + ldm(e.qa + g[J.pb - 1] + m * N));
   }
 #pragma unroll
   for (int q = 0; q < 4; q++)
@@ -2079,7 +2090,7 @@ __device__ __forceinline__ void pack_item(const Eng<double> &e, const FaceTask &
   double *drva = e.drva + B.face_off[T.nn] * 10;
   double qv[5];
 #pragma unroll
-  for (int q = 0; q < 5; q++) qv[q] = e.qa[g + q * N];  // (the reads first, then the stores)
+  for (int q = 0; q < 5; q++) qv[q] = ldm(e.qa + g + q * N);  // (the reads first, then the stores)
 #pragma unroll
   for (int q = 0; q < 5; q++) drva[jk + nbs * (q + 5 * T.ip)] = qv[q];
   e.cnt[g] = 1.0;
@@ -2104,10 +2115,10 @@ __device__ __forceinline__ void avg_item(const Eng<double> &e, const FaceTask &T
   double dv[5], qv[5];
 #pragma unroll
   for (int q = 0; q < 5; q++) {
-    dv[q] = nbr[jk + nbs * (q + 5 * (1 - T.ip))];
-    qv[q] = e.qa[g + q * N];
+    dv[q] = ldm(nbr + jk + nbs * (q + 5 * (1 - T.ip)));
+    qv[q] = ldm(e.qa + g + q * N);
   }
-  const double cnt = e.cnt[g] + 1.0;
+  const double cnt = ldm(e.cnt + g) + 1.0;
   e.cnt[g] = cnt;
   const double w = 1.0 / cnt;
   e.cnt[g + N] = w;

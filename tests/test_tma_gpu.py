@@ -14,8 +14,8 @@ pytestmark = pytest.mark.gpu
 
 def _aligned_case(**kw):
     from tandemproject_gb300.config import MIXED, small_case
-    # 6 blocks of 32/64/32 x 16 x 12 points: every row and plane a multiple of 4 floats
-    return small_case(lxibk=(31, 63, 31), letbk=(15, 15), lzebk=(11,), precision=MIXED, **kw)
+    # 6 blocks of 32/64/32 x 16 x 16 points: every row and plane a multiple of 4 floats
+    return small_case(lxibk=(31, 63, 31), letbk=(15, 15), lzebk=(15,), precision=MIXED, **kw)
 
 
 def test_tma_staging_bit_identical_to_async_copies(ati_lib):
