@@ -151,8 +151,10 @@ def _oracle_flags():
     return ob.CFLAGS
 
 
-def cpu_baseline(cfg, grid, sample_steps=2, warm_steps=1):
-    """The CPU restatement of the reference, all host threads, on the same case."""
+def cpu_baseline(cfg, grid, sample_steps=10, warm_steps=2):
+    """The CPU restatement of the reference, all host threads, on the same case: a bounded sample of ten steps
+    (about 15-20 s on 16 cores) after two warm-up steps, so that it holds one of the turbulence evaluations that
+    come every ten steps, as the timed GPU steps do."""
     from oracle import oracle as orc
     o = orc.OracleCase(cfg)
     for mb in range(cfg.nblocks):
@@ -167,7 +169,7 @@ def cpu_baseline(cfg, grid, sample_steps=2, warm_steps=1):
     o.close()
     return {"value": cfg.npoints * cfg.nkrk * sample_steps / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{sample_steps} time steps ({sample_steps * cfg.nkrk} RK stages) of the full "
-                      f"{cfg.npoints}-point case after {warm_steps} warm-up step, CPU restatement (oracle/), "
+                      f"{cfg.npoints}-point case after {warm_steps} warm-up steps, CPU restatement (oracle/), "
                       f"OpenMP over lines, {cores} threads, gcc {' '.join(_oracle_flags())}{turb}"}
 
 

@@ -1789,6 +1789,8 @@ __global__ void k_rk(Eng<R> e) {
 // (src/Subroutines3D.f90:235-324) and the GCBC/GCIC loops of
 // src/Main3D.f90:780-869
 // ---------------------------------------------------------------------------
+// The face items (one face line or corner-line point each) are real functions, not inlined: the per-face kernels and
+// the fused face chains call the same compiled code, so the two give the same roundings bit for bit.
 // Reads of the arrays the face items modify (de, the face buffers, qa and the visit counts) bypass the SM's L1
 // cache (ld.global.cg): in a fused face chain a phase reads values that other SMs wrote in an earlier phase of the
 // same launch, and a line this SM cached before could be stale.  The per-face kernels read the same way.
@@ -1890,7 +1892,7 @@ __device__ __forceinline__ void face_point(const BlockDev &B, int nn, int ip, in
 
 // drva = X * (J * (ra0*drva + ra1*de)) (src/Main3D.f90:780-795)
 template <typename R>
-__device__ __forceinline__ void gcbc_prep_item(const Eng<R> &e, const FaceTask &T, int jk) {
+__device__ __noinline__ void gcbc_prep_item(const Eng<R> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const Scheme &S = e.sc[B.cs];
   const Scalars &SC = e.scal[B.cs];
@@ -1934,7 +1936,7 @@ __device__ __forceinline__ void gcbc_prep_item(const Eng<R> &e, const FaceTask &
 }
 
 template <typename R>
-__global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
+__global__ void k_gcbc_prep(const __grid_constant__ Eng<R> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk < T.nline) gcbc_prep_item<R>(e, T, jk);
@@ -1944,7 +1946,7 @@ __global__ void k_gcbc_prep(Eng<R> e, const FaceTask *tasks) {
 // launched once per direction in the reference's order so that edge points
 // touched by faces of two directions accumulate in the same order
 template <typename R>
-__device__ __forceinline__ void gcbc_apply_item(const Eng<R> &e, const FaceTask &T, int jk) {
+__device__ __noinline__ void gcbc_apply_item(const Eng<R> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const Scheme &S = e.sc[B.cs];
   const Scalars &SC = e.scal[B.cs];
@@ -2016,14 +2018,14 @@ __device__ __forceinline__ void gcbc_apply_item(const Eng<R> &e, const FaceTask 
 }
 
 template <typename R>
-__global__ void k_gcbc_apply(Eng<R> e, const FaceTask *tasks) {
+__global__ void k_gcbc_apply(const __grid_constant__ Eng<R> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk < T.nline) gcbc_apply_item<R>(e, T, jk);
 }
 
 // wall temperature and velocity (src/Main3D.f90:886-895), FP64 state
-__device__ __forceinline__ void wall_item(const Eng<double> &e, const FaceTask &T, int jk) {
+__device__ __noinline__ void wall_item(const Eng<double> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const Scheme &S = e.sc[B.cs];
   const Scalars &SC = e.scal[B.cs];
@@ -2045,7 +2047,7 @@ __device__ __forceinline__ void wall_item(const Eng<double> &e, const FaceTask &
   e.qa[g + 4 * N] = rp * q5 + ra2 * (ra0 * q1 + 0.5 * (q2 * q2 + q3 * q3 + q4 * q4) / q1);
 }
 
-__global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
+__global__ void k_wall(const __grid_constant__ Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk < T.nline) wall_item(e, T, jk);
@@ -2053,7 +2055,7 @@ __global__ void k_wall(Eng<double> e, const FaceTask *tasks) {
 
 // junction averaging of the corner lines shared by four blocks
 // (src/SingleTurbulence3D.f90:378-443)
-__device__ __forceinline__ void junction_item(const Eng<double> &e, const JunctionDev &J, int k) {
+__device__ __noinline__ void junction_item(const Eng<double> &e, const JunctionDev &J, int k) {
   const int64_t N = e.N;
   int64_t g[4];
 #pragma unroll
@@ -2072,7 +2074,7 @@ __device__ __forceinline__ void junction_item(const Eng<double> &e, const Juncti
     for (int m = 0; m < 5; m++) e.qa[g[q] + m * N] = avg[m];
 }
 
-__global__ void k_junction(Eng<double> e, const JunctionDev *jn, int njct) {
+__global__ void k_junction(const __grid_constant__ Eng<double> e, const JunctionDev *jn, int njct) {
   const int jx = blockIdx.y;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (jx >= njct) return;
@@ -2082,7 +2084,7 @@ __global__ void k_junction(Eng<double> e, const JunctionDev *jn, int njct) {
 
 // interface averaging: pack qa of every BC 30/35/45 face (src/Main3D.f90:908-914)
 // into the FP64 face buffer drva of the set-up engine
-__device__ __forceinline__ void pack_item(const Eng<double> &e, const FaceTask &T, int jk) {
+__device__ __noinline__ void pack_item(const Eng<double> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   int i, j, k;
   face_point(B, T.nn, T.ip, jk, i, j, k);
@@ -2096,14 +2098,14 @@ __device__ __forceinline__ void pack_item(const Eng<double> &e, const FaceTask &
   e.cnt[g] = 1.0;
 }
 
-__global__ void k_pack(Eng<double> e, const FaceTask *tasks) {
+__global__ void k_pack(const __grid_constant__ Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk < T.nline) pack_item(e, T, jk);
 }
 
 // interface averaging of the faces of one direction (src/Main3D.f90:926-952)
-__device__ __forceinline__ void avg_item(const Eng<double> &e, const FaceTask &T, int jk) {
+__device__ __noinline__ void avg_item(const Eng<double> &e, const FaceTask &T, int jk) {
   const BlockDev &B = e.blk[T.b];
   const BlockDev &Bn = e.blk[T.nb_b];
   int i, j, k;
@@ -2129,7 +2131,7 @@ __device__ __forceinline__ void avg_item(const Eng<double> &e, const FaceTask &T
   }
 }
 
-__global__ void k_avg(Eng<double> e, const FaceTask *tasks) {
+__global__ void k_avg(const __grid_constant__ Eng<double> e, const FaceTask *tasks) {
   const FaceTask T = tasks[blockIdx.y];
   const int jk = blockIdx.x * blockDim.x + threadIdx.x;
   if (jk < T.nline) avg_item(e, T, jk);
@@ -2280,7 +2282,7 @@ __device__ __forceinline__ void flag_all_timeout(Scalars *scal, int ncase) {
 
 // before the RK update: GCBC preparation, application per direction, frame update (SC_MOVEF_B)
 template <typename R>
-__global__ void __launch_bounds__(256) k_face_pre(Eng<R> e, FaceChain c) {
+__global__ void __launch_bounds__(256) k_face_pre(const __grid_constant__ Eng<R> e, const __grid_constant__ FaceChain c) {
   unsigned target = 0;
   bool ok = true;
   auto sync = [&]() {
@@ -2305,7 +2307,8 @@ __global__ void __launch_bounds__(256) k_face_pre(Eng<R> e, FaceChain c) {
 }
 
 // after the RK update: wall, junctions, face packing, averaging per direction
-__global__ void __launch_bounds__(256) k_face_post(Eng<double> e, FaceChain c) {
+__global__ void __launch_bounds__(256) k_face_post(const __grid_constant__ Eng<double> e,
+                                                   const __grid_constant__ FaceChain c) {
   unsigned target = 0;
   bool ok = true;
   auto sync = [&]() {

@@ -23,7 +23,7 @@ if ROOT not in sys.path:
 
 
 def main():
-    from oracle.oracle import OracleCase, build_modes, get_threads
+    from oracle.oracle import OracleCase, build_modes, get_threads, set_threads
     from tandemproject_gb300.config import FP64, FP64_STRICT, PRESETS
     from tandemproject_gb300.grid import aerofoil_grid
     from tandemproject_gb300.solver import setup_case
@@ -32,7 +32,10 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--every", type=int, default=100)
     ap.add_argument("--precision", choices=["fp64", "strict"], default="strict")
+    ap.add_argument("--threads", type=int, default=0, help="oracle threads (0: all host cores)")
     args = ap.parse_args()
+    if args.threads > 0:
+        set_threads(args.threads)
     cfg = PRESETS[args.preset].replace(precision=FP64_STRICT if args.precision == "strict" else FP64)
     grid = aerofoil_grid(cfg)
     gpu = setup_case(cfg, grid=grid)
