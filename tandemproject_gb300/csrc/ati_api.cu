@@ -732,14 +732,24 @@ static int build_tables(ati_handle *h, std::vector<double> &facd, std::vector<do
       for (int gb = 0; gb < h->nb; gb++) {
         if (cls(len(h->blk[gb])) != c) continue;
         const BlockDev &B = h->blk[gb];
+        // tiles of one-group CTAs come in runs of even length (a padding tile past the block's lines, on which
+        // every CTA idles, evens an odd run): the paired sweeps take two consecutive tiles of a run a CTA
+        auto even_run = [&](size_t start) {
+          if (C.groups == 1 && (h->hlts[nn].size() - start) % 2) h->hlts[nn].push_back(LTile{gb, (int)B.nbsize[nn]});
+        };
         if (nn == 2 && h->tma[2]) {
           // TMA eta tiles: the lines of one grid row (fixed zeta), from a multiple of 32 points along xi
-          for (int ze = 0; ze <= B.lze; ze++)
+          for (int ze = 0; ze <= B.lze; ze++) {
+            const size_t start = h->hlts[nn].size();
             for (int xi0 = 0; xi0 <= B.lxi; xi0 += SEG_LINES * C.groups)
               h->hlts[nn].push_back(LTile{gb, ze * (B.lxi + 1) + xi0});
+            even_run(start);
+          }
           continue;
         }
+        const size_t start = h->hlts[nn].size();
         for (int t0 = 0; t0 < B.nbsize[nn]; t0 += SEG_LINES * C.groups) h->hlts[nn].push_back(LTile{gb, t0});
+        even_run(start);
       }
       C.n = (int)h->hlts[nn].size() - C.off;
       h->segc[nn][c] = C;
@@ -1009,6 +1019,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     m.nblk = h->nb;
     for (int nn = 0; nn < 4; nn++) m.tma[nn] = h->tma[nn];
     m.eta_rowtiles = h->tma[2];
+    m.pairs = true;
   }
   // junctions (src/SingleTurbulence3D.f90:386-398), bkx = 3, bky = 2, per case
   std::vector<JunctionDev> jn;
@@ -1401,14 +1412,17 @@ extern "C" int ati_set_tiles(ati_handle_t *h, const int32_t in[4]) {
 
 extern "C" int ati_set_options(ati_handle_t *h, int flags, int32_t *active) {
   if (!h) return fail(h, ATI_EINVAL, "null handle");
-  if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES)) return fail(h, ATI_EINVAL, "ati_set_options: unknown flag");
+  if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES | ATI_OPT_PAIRED_LINES))
+    return fail(h, ATI_EINVAL, "ati_set_options: unknown flag");
   CK(cudaStreamSynchronize(h->st));
   drop_graphs(h);
   for (int nn = 2; nn <= 3; nn++) h->ef.tma[nn] = (flags & ATI_OPT_TMA) != 0 && h->tma[nn];
   h->fused = (flags & ATI_OPT_FUSED_FACES) != 0;
+  h->ef.pairs = (flags & ATI_OPT_PAIRED_LINES) != 0;
   if (active)
     *active = (h->ef.tma[2] || h->ef.tma[3] ? ATI_OPT_TMA : 0) | (h->fused ? ATI_OPT_FUSED_FACES : 0) |
-              (h->ef.tma[2] ? ATI_OPT_TMA_ETA : 0) | (h->ef.tma[3] ? ATI_OPT_TMA_ZETA : 0);
+              (h->ef.tma[2] ? ATI_OPT_TMA_ETA : 0) | (h->ef.tma[3] ? ATI_OPT_TMA_ZETA : 0) |
+              (h->ef.pairs ? ATI_OPT_PAIRED_LINES : 0);
   return ATI_OK;
 }
 

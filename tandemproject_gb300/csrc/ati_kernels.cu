@@ -748,10 +748,12 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
   // its own tile; otherwise the CTA is one group and warp w solves segment w of its lines
   const int gsz = groups > 1 ? 1 : nwarp, grp = w / gsz, wl = w - grp * gsz;
   const int t0 = LT.t0 + grp * SEG_LINES;
-  // lines of the group (none: the group idles); an eta tile built for TMA ends with its grid row
+  // lines of the group (none: the group idles, as on a padding tile past the block's lines); an eta tile built
+  // for TMA ends with its grid row
   const int nx = B.lxi + 1;
-  const int nl = (NN == 2 && a.rowtiles) ? min(SEG_LINES, nx - LT.t0 % nx - grp * SEG_LINES)
-                                         : min(SEG_LINES, (int)B.nbsize[NN] - t0);
+  const int nl = LT.t0 >= B.nbsize[NN] ? 0
+                 : (NN == 2 && a.rowtiles) ? min(SEG_LINES, nx - LT.t0 % nx - grp * SEG_LINES)
+                                           : min(SEG_LINES, (int)B.nbsize[NN] - t0);
   // shared memory: the groups' tiles (TMA: first, 128-byte aligned), then the segment carries
   float *tiles;
   if constexpr (TMA) {
@@ -1112,6 +1114,444 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
     // a tile copy that did not land in time: wait once more (bounded) so that no copy into this CTA's shared
     // memory is left in flight when it exits
     if (!tma_ok) (void)mbar_wait_bounded(&tbar[grp], 0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Paired segmented derivative solves (mixed path, FP32 inputs and outputs).  A
+// CTA takes two consecutive groups of SEG_LINES lines (two halves) of one block,
+// and lane l solves line l of both: the row-table loads, the loop and address
+// arithmetic and the segment carries' control flow are spent once for two
+// lines.  Each line's arithmetic is that of k_sweep_seg, expression for
+// expression, so both kernels give the same results.
+//   single != 0: the lines are one segment long; the CTA (one warp) takes the
+//     tile of 2 SEG_LINES lines at lt[blockIdx.x].
+//   single == 0: the CTA (one warp per segment) takes the tiles at
+//     lt[2 blockIdx.x] and the one after it: the host pads every block's run of
+//     tiles (every grid row's, for eta row tiles) to an even count, so the two
+//     are consecutive lines and the padding tile lies past the run's lines.
+// The halves' tiles lie one after the other in shared memory ([point][line]
+// rows, as in k_sweep_seg); with TMA each half comes in as one tensor copy, both
+// counted on one mbarrier.
+// ---------------------------------------------------------------------------
+template <int NN, bool TMA>
+__global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<float, float, float> a, const float *rtab,
+                                                                   int single) {
+  extern __shared__ __align__(16) unsigned char seg_smem[];
+  constexpr int RS = TMA ? SEG_LINES : SEG_LINES + 1;
+  __shared__ uint64_t tbar;
+  const int nwarp = (int)(blockDim.x >> 5);
+  const LTile LT = a.lt[single ? blockIdx.x : 2 * blockIdx.x];
+  const BlockDev &B = a.blk[LT.b];
+  const int f = blockIdx.y;
+  const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5);
+  const int nx = B.lxi + 1, ny = B.let + 1;
+  const int L = NN == 1 ? nx : (NN == 2 ? ny : B.lze + 1);
+  const int T0 = LT.t0;
+  const int64_t nbs = B.nbsize[NN];
+  // lines of each half (none past the block's lines or, for eta row tiles, past the grid row)
+  const int lim = T0 >= nbs ? 0 : ((NN == 2 && a.rowtiles) ? nx - T0 % nx : (int)(nbs - T0));
+  const int nl0 = max(0, min(SEG_LINES, lim)), nl1 = max(0, min(SEG_LINES, lim - SEG_LINES));
+  const int HS = L * RS;  // offset of the second half's tile
+  float *tiles;
+  if constexpr (TMA) {
+    const uint32_t pad = (128u - (smem_u32(seg_smem) & 127u)) & 127u;
+    tiles = reinterpret_cast<float *>(seg_smem + pad);
+  } else {
+    tiles = reinterpret_cast<float *>(seg_smem + (size_t)nwarp * SEG_LINES * 2 * sizeof(float4));
+  }
+  // [segment][lane] values a segment passes on / receives, both halves' lines in one float4
+  float4 *cf = TMA ? reinterpret_cast<float4 *>(tiles + 2 * (int64_t)HS) : reinterpret_cast<float4 *>(seg_smem);
+  float4 *cx = cf + nwarp * SEG_LINES;
+  const int64_t stride = NN == 1 ? 1 : (NN == 2 ? (int64_t)nx : (int64_t)nx * ny);
+  int64_t base0 = 0, base1 = 0, sdum = 0;
+  int jk0 = 0, jk1 = 0, Lg = 0;
+  line_geom<NN>(B, T0 + lane, base0, sdum, jk0, Lg);
+  line_geom<NN>(B, T0 + SEG_LINES + lane, base1, sdum, jk1, Lg);
+  const float *in = a.io.in + f * a.io.in_fs;
+
+  // 1. stage both halves
+  bool tma_ok = true;
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      mbar_init(&tbar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (nl0 > 0) {
+      if (threadIdx.x == 0) {
+        const TmaMap *tm = a.tmap + LT.b;
+        tmap_acquire(tm);
+        mbar_expect_tx(&tbar, (uint32_t)(L * SEG_LINES * sizeof(float)) * (nl1 > 0 ? 2u : 1u));
+        for (int hh = 0; hh < 2; hh++) {
+          if (hh == 1 && nl1 == 0) break;
+          const int t0 = T0 + hh * SEG_LINES;
+          if constexpr (NN == 2) tma_load_4d(tiles + hh * HS, tm, t0 % nx, 0, t0 / nx, f, &tbar);
+          else tma_load_3d(tiles + hh * HS, tm, t0, 0, f, &tbar);
+        }
+      }
+      tma_ok = mbar_wait_bounded(&tbar, 0);
+      if (!tma_ok && lane == 0) atomicOr(&a.scal[B.cs].flag, FLAG_TIMEOUT);
+    }
+  } else {
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+      const int nl = hh ? nl1 : nl0;
+      float *tile = tiles + hh * HS;
+      if constexpr (NN == 1) {
+        // xi lines are contiguous: a warp copies one line at a time, lanes along the line
+        const float *src0 = in + B.off + (int64_t)(T0 + hh * SEG_LINES) * L;
+        for (int ln = w; ln < nl; ln += nwarp) {
+          const float *src = src0 + (int64_t)ln * L + lane;
+          float *dst = tile + lane * RS + ln;
+#pragma unroll 4
+          for (int i = lane; i < L; i += 32, src += 32, dst += 32 * RS) cp_async<4>(dst, src);
+        }
+      } else if (lane < nl) {
+        // consecutive eta/zeta lines are consecutive points of a row: a warp copies one row at a time
+        const float *src = in + (hh ? base1 : base0) + (int64_t)w * stride;
+        float *dst = tile + w * RS + lane;
+#pragma unroll 4
+        for (int i = w; i < L; i += nwarp, src += nwarp * stride, dst += nwarp * RS) cp_async<4>(dst, src);
+      }
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+  }
+  __syncthreads();
+
+  const int S = seg_count(L);
+  // (half 1's lines of a lane are a subset of half 0's: lane < nl1 implies lane < nl0)
+  const bool act0 = w < S && lane < nl0 && tma_ok, act1 = w < S && lane < nl1 && tma_ok;
+  const bool act = act0;
+  const int s0 = seg_start(w, L, S), s1 = seg_start(w + 1, L, S);
+  float *col = tiles + lane;  // half 0; half 1 at col + HS
+  const float *rt = rtab + (int64_t)B.fac_off[NN] * SEG_RT;
+  auto row = [&](int i) { return rt + i * SEG_RT; };
+  const Coef<float> &C = *a.cf;
+  const float k1 = C.aa, k2 = C.ab, k3 = C.ac;
+  auto rhs = [&](float x0, float x1, float x2, float x3, float x4, float x5, float x6) {
+    return k1 * (x4 - x2) + k2 * (x5 - x1) + k3 * (x6 - x0);
+  };
+  const int ilo = max(s0, 3), ihi = min(s1, L - 3);
+  // 2. what a segment reads outside its own rows, before any row is overwritten (per half, as in k_sweep_seg)
+  float sbs0[2] = {0, 0}, sbs1[2] = {0, 0}, sbs2[2] = {0, 0}, sbe0[2] = {0, 0}, sbe1[2] = {0, 0}, sbe2[2] = {0, 0};
+  float a0[2] = {0, 0}, a1[2] = {0, 0}, a2[2] = {0, 0}, a3[2] = {0, 0}, a4[2] = {0, 0}, a5[2] = {0, 0};
+  float h0[2] = {0, 0}, h1[2] = {0, 0}, h2[2] = {0, 0};
+  if (act) {
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+      const float *ch = col + hh * HS;
+      auto sld = [&](int i) { return ch[i * RS]; };
+      if ((hh == 0 || act1) && (w == 0 || w == S - 1)) {
+        const int jk = hh ? jk1 : jk0;
+        const float *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
+        auto closure = [&](int r0, int dir, float *o) {
+          float c0 = 0, c1 = 0, sap0 = 0;
+          for (int i = 0; i <= LMD; i++) {
+            const float v = sld(r0 + i * dir);
+            if (i == 0) sap0 = v;
+            c0 += C.pbco[0][0][i] * v;
+            c1 += C.pbco[0][1][i] * v;
+          }
+          o[0] = c0; o[1] = c1; o[2] = sap0;
+        };
+        float rl[6];
+        for (int ip = 0; ip <= 1; ip++) {
+          if (B.ndf[ip][NN] != 1) continue;
+          if (B.nbc[ip][NN] == 45 && B.ncd[ip][NN] == LT.b) closure(ip == 0 ? L - 2 : 1, ip == 0 ? -1 : 1, rl + 3 * ip);
+          else for (int q = 0; q < 3; q++) rl[3 * ip + q] = rcv[jk + nbs * (3 * ip + q)];
+        }
+        line_ends<false, float>(C, L, B.ndf[0][NN], B.ndf[1][NN], rl, 1, 0, sld, sbs0[hh], sbs1[hh], sbs2[hh],
+                                sbe0[hh], sbe1[hh], sbe2[hh]);
+      }
+      if (ilo < ihi) {
+        a0[hh] = sld(ilo - 3); a1[hh] = sld(ilo - 2); a2[hh] = sld(ilo - 1);
+        a3[hh] = sld(ilo); a4[hh] = sld(ilo + 1); a5[hh] = sld(ilo + 2);
+      }
+      if (w < S - 1) { h0[hh] = sld(s1); h1[hh] = sld(s1 + 1); h2[hh] = sld(s1 + 2); }
+    }
+  }
+  __syncthreads();
+
+  // 3. forward elimination of the segment from zero incoming values, in place, both halves
+  float pm2[2] = {0, 0}, pm1[2] = {0, 0};
+  if (act) {
+    auto fwd = [&](int i, float r0, float r1) {
+      const float2 l = __ldg(reinterpret_cast<const float2 *>(row(i)));  // masked l0, l1
+      const float p0 = r0 - l.x * pm2[0] - l.y * pm1[0];
+      const float p1 = r1 - l.x * pm2[1] - l.y * pm1[1];
+      col[i * RS] = p0;
+      col[HS + i * RS] = p1;
+      pm2[0] = pm1[0]; pm1[0] = p0;
+      pm2[1] = pm1[1]; pm1[1] = p1;
+    };
+    int i = s0;
+    for (; i < min(s1, 3); i++) {
+      const float r0 = i == 0 ? sbs0[0] : (i == 1 ? sbs1[0] : sbs2[0]);
+      const float r1 = i == 0 ? sbs0[1] : (i == 1 ? sbs1[1] : sbs2[1]);
+      fwd(i, r0, r1);
+    }
+    const int iown = min(ihi, s1 - 3);
+    {
+      float *pc = col + i * RS;
+      const float *tr = row(i);
+      auto l2 = [](const float *t) { return __ldg(reinterpret_cast<const float2 *>(t)); };
+      float2 m0 = l2(tr), m1 = l2(tr + SEG_RT), m2 = l2(tr + 2 * SEG_RT), m3 = l2(tr + 3 * SEG_RT);
+      for (; i + 3 < iown; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
+        float b0[2], b1[2], b2[2], b3[2];
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+          const float *q = pc + hh * HS;
+          b0[hh] = q[3 * RS]; b1[hh] = q[4 * RS]; b2[hh] = q[5 * RS]; b3[hh] = q[6 * RS];
+        }
+        const float2 n0 = l2(tr + 4 * SEG_RT), n1 = l2(tr + 5 * SEG_RT), n2 = l2(tr + 6 * SEG_RT);
+        const float2 n3 = l2(tr + 7 * SEG_RT);
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+          float *q = pc + hh * HS;
+          float p, &pa = pm2[hh], &pb = pm1[hh];
+          p = rhs(a0[hh], a1[hh], a2[hh], a3[hh], a4[hh], a5[hh], b0[hh]) - m0.x * pa - m0.y * pb; q[0] = p; pa = pb; pb = p;
+          p = rhs(a1[hh], a2[hh], a3[hh], a4[hh], a5[hh], b0[hh], b1[hh]) - m1.x * pa - m1.y * pb; q[RS] = p; pa = pb; pb = p;
+          p = rhs(a2[hh], a3[hh], a4[hh], a5[hh], b0[hh], b1[hh], b2[hh]) - m2.x * pa - m2.y * pb; q[2 * RS] = p; pa = pb; pb = p;
+          p = rhs(a3[hh], a4[hh], a5[hh], b0[hh], b1[hh], b2[hh], b3[hh]) - m3.x * pa - m3.y * pb; q[3 * RS] = p; pa = pb; pb = p;
+          a0[hh] = a4[hh]; a1[hh] = a5[hh]; a2[hh] = b0[hh]; a3[hh] = b1[hh]; a4[hh] = b2[hh]; a5[hh] = b3[hh];
+        }
+        m0 = n0; m1 = n1; m2 = n2; m3 = n3;
+      }
+    }
+    auto shift = [&](const float *a6) {
+#pragma unroll
+      for (int hh = 0; hh < 2; hh++) {
+        a0[hh] = a1[hh]; a1[hh] = a2[hh]; a2[hh] = a3[hh]; a3[hh] = a4[hh]; a4[hh] = a5[hh]; a5[hh] = a6[hh];
+      }
+    };
+    for (; i < iown; i++) {
+      const float a6[2] = {col[(i + 3) * RS], col[HS + (i + 3) * RS]};
+      fwd(i, rhs(a0[0], a1[0], a2[0], a3[0], a4[0], a5[0], a6[0]), rhs(a0[1], a1[1], a2[1], a3[1], a4[1], a5[1], a6[1]));
+      shift(a6);
+    }
+    for (; i < ihi; i++) {  // windows reaching into the next segment: its first rows, read before the barrier
+      const int d = i + 3 - s1;
+      const float a6[2] = {d == 0 ? h0[0] : (d == 1 ? h1[0] : h2[0]), d == 0 ? h0[1] : (d == 1 ? h1[1] : h2[1])};
+      fwd(i, rhs(a0[0], a1[0], a2[0], a3[0], a4[0], a5[0], a6[0]), rhs(a0[1], a1[1], a2[1], a3[1], a4[1], a5[1], a6[1]));
+      shift(a6);
+    }
+    for (; i < s1; i++) {
+      const float r0 = i == L - 1 ? sbe0[0] : (i == L - 2 ? sbe1[0] : sbe2[0]);
+      const float r1 = i == L - 1 ? sbe0[1] : (i == L - 2 ? sbe1[1] : sbe2[1]);
+      fwd(i, r0, r1);
+    }
+    cf[w * SEG_LINES + lane] = make_float4(pm2[0], pm1[0], pm2[1], pm1[1]);  // rows s1-2, s1-1
+  }
+  const bool multi = S > 1;
+  if (multi) {
+    __syncthreads();
+    // 4. incoming values of every segment, carried by warp 0 (segment 0 receives zeros)
+    if (w == 0 && lane < nl0) {
+      float2 x = make_float2(0.f, 0.f), y = make_float2(0.f, 0.f);
+      cx[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 1; k < S; k++) {
+        const int e = seg_start(k, L, S);
+        const float4 c = cf[(k - 1) * SEG_LINES + lane];
+        const float2 t2 = __ldg(reinterpret_cast<const float2 *>(row(e - 2) + 4));  // g, h
+        const float2 t1 = __ldg(reinterpret_cast<const float2 *>(row(e - 1) + 4));
+        x = make_float2(c.x + t2.x * x.x + t2.y * x.y, c.y + t1.x * x.x + t1.y * x.y);
+        y = make_float2(c.z + t2.x * y.x + t2.y * y.y, c.w + t1.x * y.x + t1.y * y.y);
+        cx[k * SEG_LINES + lane] = make_float4(x.x, x.y, y.x, y.y);
+      }
+    }
+    __syncthreads();
+  }
+  float *out = a.io.out + f * a.io.out_fs;
+  float *drv = a.io.drva ? a.drva + B.face_off[NN] * 10 : nullptr;
+  const int m = a.io.m0 + f;
+  // 5. the segment's forward values, then its back substitution from zero values beyond its end; with one
+  // segment that gives the results, which eta/zeta lines write straight to DRAM (a warp writes a row)
+  if (act) {
+    const float4 xx = multi ? cx[w * SEG_LINES + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 x[2] = {make_float2(xx.x, xx.y), make_float2(xx.z, xx.w)};
+    float q1[2] = {0, 0}, q2[2] = {0, 0};  // rows i+1, i+2
+    int i = s1 - 1;
+    float *pc = col + i * RS;
+    const float *tr = row(i);
+    float *po0 = out + base0 + (int64_t)i * stride, *po1 = out + base1 + (int64_t)i * stride;
+    auto sweep = [&](auto direct) {
+      constexpr bool D = decltype(direct)::value;
+      auto l4 = [](const float *t) { return __ldg(reinterpret_cast<const float4 *>(t + 4)); };
+      auto l1 = [](const float *t) { return __ldg(t + 10); };
+      auto bwd = [&](float *c, const float4 g, const float c4) {
+        float q[2];
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) {
+          const float v = c[hh * HS] + g.x * x[hh].x + g.y * x[hh].y;
+          q[hh] = g.z * v - g.w * q1[hh] - c4 * q2[hh];
+        }
+        if constexpr (D) {
+          *po0 = q[0];
+          if (act1) *po1 = q[1];
+          po0 -= stride;
+          po1 -= stride;
+        } else {
+          c[0] = q[0];
+          c[HS] = q[1];
+        }
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) { q2[hh] = q1[hh]; q1[hh] = q[hh]; }
+      };
+      float4 g0 = l4(tr), g1 = l4(tr - SEG_RT), g2 = l4(tr - 2 * SEG_RT), g3 = l4(tr - 3 * SEG_RT);
+      float c0 = l1(tr), c1 = l1(tr - SEG_RT), c2 = l1(tr - 2 * SEG_RT), c3 = l1(tr - 3 * SEG_RT);
+      for (; i - 3 >= s0; i -= 4, pc -= 4 * RS, tr -= 4 * SEG_RT) {
+        const float4 n0 = l4(tr - 4 * SEG_RT), n1 = l4(tr - 5 * SEG_RT), n2 = l4(tr - 6 * SEG_RT);
+        const float4 n3 = l4(tr - 7 * SEG_RT);
+        const float j0 = l1(tr - 4 * SEG_RT), j1 = l1(tr - 5 * SEG_RT), j2 = l1(tr - 6 * SEG_RT);
+        const float j3 = l1(tr - 7 * SEG_RT);
+        bwd(pc, g0, c0);
+        bwd(pc - RS, g1, c1);
+        bwd(pc - 2 * RS, g2, c2);
+        bwd(pc - 3 * RS, g3, c3);
+        g0 = n0; g1 = n1; g2 = n2; g3 = n3;
+        c0 = j0; c1 = j1; c2 = j2; c3 = j3;
+      }
+      for (; i >= s0; i--, pc -= RS, tr -= SEG_RT) bwd(pc, l4(tr), l1(tr));
+    };
+    if (!multi && NN != 1) {
+      sweep(std::true_type{});
+      if (drv) {
+        drv[jk0 + nbs * ((m - 1) + 5 * 0)] = q1[0];  // drva(jk,m,0) = sb(is): row 0, the last one solved
+        drv[jk0 + nbs * ((m - 1) + 5 * 1)] = out[base0 + (int64_t)(L - 1) * stride];  // drva(jk,m,1) = sb(ie)
+        if (act1) {
+          drv[jk1 + nbs * ((m - 1) + 5 * 0)] = q1[1];
+          drv[jk1 + nbs * ((m - 1) + 5 * 1)] = out[base1 + (int64_t)(L - 1) * stride];
+        }
+      }
+    } else {
+      sweep(std::false_type{});
+      if (multi) {
+        cf[w * SEG_LINES + lane] = make_float4(q1[0], q2[0], q1[1], q2[1]);  // rows s0, s0+1
+      } else if (drv) {
+        drv[jk0 + nbs * ((m - 1) + 5 * 0)] = col[0];
+        drv[jk0 + nbs * ((m - 1) + 5 * 1)] = col[(L - 1) * RS];
+        if (act1) {
+          drv[jk1 + nbs * ((m - 1) + 5 * 0)] = col[HS];
+          drv[jk1 + nbs * ((m - 1) + 5 * 1)] = col[HS + (L - 1) * RS];
+        }
+      }
+    }
+  }
+  if (multi) {
+    __syncthreads();
+    // 6. values beyond every segment's end, carried backwards by warp 0 (the last segment receives zeros)
+    if (w == 0 && lane < nl0) {
+      float2 x = make_float2(0.f, 0.f), y = make_float2(0.f, 0.f);
+      cx[(S - 1) * SEG_LINES + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = S - 2; k >= 0; k--) {
+        const int e = seg_start(k + 1, L, S);
+        const float4 c = cf[(k + 1) * SEG_LINES + lane];
+        const float2 t0 = __ldg(reinterpret_cast<const float2 *>(row(e) + 8));  // G, H
+        const float2 t1 = __ldg(reinterpret_cast<const float2 *>(row(e + 1) + 8));
+        x = make_float2(c.x + t0.x * x.x + t0.y * x.y, c.y + t1.x * x.x + t1.y * x.y);
+        y = make_float2(c.z + t0.x * y.x + t0.y * y.y, c.w + t1.x * y.x + t1.y * y.y);
+        cx[k * SEG_LINES + lane] = make_float4(x.x, x.y, y.x, y.y);
+      }
+    }
+    __syncthreads();
+    // 7. results: eta/zeta rows go straight to DRAM (a warp writes a contiguous row), xi lines through the tile
+    if (act) {
+      const float4 yy = cx[w * SEG_LINES + lane];
+      const float2 y[2] = {make_float2(yy.x, yy.y), make_float2(yy.z, yy.w)};
+      auto fv = [&](const float *c, const float *t, int hh) {
+        const float2 g = __ldg(reinterpret_cast<const float2 *>(t));
+        return *c + g.x * y[hh].x + g.y * y[hh].y;
+      };
+      auto l2 = [](const float *t) { return __ldg(reinterpret_cast<const float2 *>(t)); };
+      if (drv) {
+        if (w == 0) {
+          drv[jk0 + nbs * ((m - 1) + 5 * 0)] = fv(col, row(0) + 8, 0);  // drva(jk,m,0) = sb(is)
+          if (act1) drv[jk1 + nbs * ((m - 1) + 5 * 0)] = fv(col + HS, row(0) + 8, 1);
+        }
+        if (w == S - 1) {
+          drv[jk0 + nbs * ((m - 1) + 5 * 1)] = fv(col + (L - 1) * RS, row(L - 1) + 8, 0);
+          if (act1) drv[jk1 + nbs * ((m - 1) + 5 * 1)] = fv(col + HS + (L - 1) * RS, row(L - 1) + 8, 1);
+        }
+      }
+      int i = s0;
+      float *pc = col + i * RS;
+      const float *tr = row(i) + 8;
+      float2 e0 = l2(tr), e1 = l2(tr + SEG_RT), e2 = l2(tr + 2 * SEG_RT), e3 = l2(tr + 3 * SEG_RT);
+      // one row of both halves: r[hh] = the row's value plus the carried correction
+      auto fg2 = [&](const float *c, const float2 g, float r[2]) {
+#pragma unroll
+        for (int hh = 0; hh < 2; hh++) r[hh] = c[hh * HS] + g.x * y[hh].x + g.y * y[hh].y;
+      };
+      if constexpr (NN == 1) {
+        for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
+          const float2 n0 = l2(tr + 4 * SEG_RT), n1 = l2(tr + 5 * SEG_RT), n2 = l2(tr + 6 * SEG_RT);
+          const float2 n3 = l2(tr + 7 * SEG_RT);
+          float r0[2], r1[2], r2[2], r3[2];
+          fg2(pc, e0, r0); fg2(pc + RS, e1, r1); fg2(pc + 2 * RS, e2, r2); fg2(pc + 3 * RS, e3, r3);
+#pragma unroll
+          for (int hh = 0; hh < 2; hh++) {
+            float *q = pc + hh * HS;
+            q[0] = r0[hh]; q[RS] = r1[hh]; q[2 * RS] = r2[hh]; q[3 * RS] = r3[hh];
+          }
+          e0 = n0; e1 = n1; e2 = n2; e3 = n3;
+        }
+        for (; i < s1; i++, pc += RS, tr += SEG_RT) {
+          float r[2];
+          fg2(pc, l2(tr), r);
+          pc[0] = r[0];
+          pc[HS] = r[1];
+        }
+      } else {
+        // walking output pointers: one 64-bit add per row and half
+        float *po0 = out + base0 + (int64_t)i * stride, *po1 = out + base1 + (int64_t)i * stride;
+        auto put = [&](const float r[2]) {
+          *po0 = r[0];
+          if (act1) *po1 = r[1];
+          po0 += stride;
+          po1 += stride;
+        };
+        for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
+          const float2 n0 = l2(tr + 4 * SEG_RT), n1 = l2(tr + 5 * SEG_RT), n2 = l2(tr + 6 * SEG_RT);
+          const float2 n3 = l2(tr + 7 * SEG_RT);
+          float r0[2], r1[2], r2[2], r3[2];
+          fg2(pc, e0, r0); fg2(pc + RS, e1, r1); fg2(pc + 2 * RS, e2, r2); fg2(pc + 3 * RS, e3, r3);
+          put(r0); put(r1); put(r2); put(r3);
+          e0 = n0; e1 = n1; e2 = n2; e3 = n3;
+        }
+        for (; i < s1; i++, pc += RS, tr += SEG_RT) {
+          float r[2];
+          fg2(pc, l2(tr), r);
+          put(r);
+        }
+      }
+    }
+  }
+  if constexpr (NN == 1) {
+    __syncthreads();
+    // both halves' lines back to DRAM through the tiles, a warp along one line at a time
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+      const int nl = hh ? nl1 : nl0;
+      const float *tile = tiles + hh * HS;
+      const int64_t o0 = B.off + (int64_t)(T0 + hh * SEG_LINES) * L;
+      for (int ln = w; ln < nl; ln += nwarp) {
+        const int64_t lb = o0 + (int64_t)ln * L;
+        int i = lane;
+        for (; i + 96 < L; i += 128) {
+          out[lb + i] = tile[i * RS + ln];
+          out[lb + i + 32] = tile[(i + 32) * RS + ln];
+          out[lb + i + 64] = tile[(i + 64) * RS + ln];
+          out[lb + i + 96] = tile[(i + 96) * RS + ln];
+        }
+        for (; i < L; i += 32) out[lb + i] = tile[i * RS + ln];
+      }
+    }
+  }
+  if constexpr (TMA) {
+    // a tile copy that did not land in time: wait once more (bounded) before the CTA exits
+    if (!tma_ok) (void)mbar_wait_bounded(&tbar, 0);
   }
 }
 
@@ -2455,7 +2895,22 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
         if constexpr (std::is_same<TI, float>::value) {
           // eta/zeta derivative sweeps of an array with tensor maps: tiles staged by TMA
           const int arr = io.in == e.prim ? 0 : (io.in == e.flx + (int64_t)(nn - 1) * e.N ? 1 : -1);
-          if (!filt && nn >= 2 && e.tma[nn] && arr >= 0) {
+          const bool tma = !filt && nn >= 2 && e.tma[nn] && arr >= 0;
+          // paired lines: a CTA solves two groups of lines, lane l line l of each
+          const size_t psm = pair_smem_bytes(C.maxlen, G > 1) + 128;
+          if (!filt && e.pairs && psm <= SEG_SMEM_MAX) {
+            const int single = G > 1 ? 1 : 0;
+            const dim3 gp(single ? C.n : C.n / 2, io.nf);
+            const int ntp = SEG_LINES * (single ? 1 : seg_count(C.maxlen));
+            if (tma) a.tmap = e.tmaps + (int64_t)(arr * 2 + nn - 2) * e.nblk;
+#define ATI_PAIR(D, T) k_sweep_pair<D, T><<<gp, ntp, psm, st>>>(a, seg, single)
+            if (nn == 1) ATI_PAIR(1, false);
+            else if (nn == 2) { if (tma) ATI_PAIR(2, true); else ATI_PAIR(2, false); }
+            else { if (tma) ATI_PAIR(3, true); else ATI_PAIR(3, false); }
+#undef ATI_PAIR
+            continue;
+          }
+          if (tma) {
             a.tmap = e.tmaps + (int64_t)(arr * 2 + nn - 2) * e.nblk;
             const size_t sm = smem + 128;  // (alignment of the tensor copies' destination)
             if (nn == 2) k_sweep_seg<2, false, true, TI, TO><<<g, nt, sm, st>>>(a, seg, G);
@@ -2517,6 +2972,11 @@ static cudaError_t seg_attr() {
   if constexpr (std::is_same<TI, float>::value) {
     if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<2, false, true, TI, TO>);
     if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<3, false, true, TI, TO>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<1, false>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, false>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, false>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, true>);
   }
   return e;
 }
@@ -2617,8 +3077,8 @@ void face_f(const Eng<float> &e, cudaStream_t st, int which, const FaceTask *tas
   }
 }
 
-// cooperative launch of a fused chain: at most one CTA of 256 threads per SM (the chains' work is a few lines per
-// thread), never more than the kernel can keep resident at once
+// cooperative launch of a fused chain: CTAs of 256 threads, as many as the kernel can keep resident at once (the
+// chains' items are chains of dependent loads: the more of them in flight, the shorter each phase)
 static int coop_cap(const void *kernel) {
   static std::mutex mu;
   static std::map<std::pair<int, const void *>, int> cap;
@@ -2633,7 +3093,7 @@ static int coop_cap(const void *kernel) {
     cudaGetLastError();
     per_sm = 0;
   }
-  const int c = per_sm >= 1 ? (nsm > 0 ? nsm : 1) : 0;  // one CTA per SM (0: the kernel cannot run)
+  const int c = per_sm >= 1 ? per_sm * (nsm > 0 ? nsm : 1) : 0;  // (0: the kernel cannot run)
   cap[{dev, kernel}] = c;
   return c;
 }

@@ -88,6 +88,7 @@ struct Eng {
   int nblk;
   bool tma[4];
   bool eta_rowtiles;    // the segmented eta tiles hold the lines of one grid row each (built for TMA staging)
+  bool pairs;           // segmented derivative sweeps of FP32 arrays solve two line groups a CTA (k_sweep_pair)
 };
 
 // The mixed path (R = float) works on deviations from the freestream
@@ -182,6 +183,11 @@ inline int seg_groups(int maxlen) { return seg_count(maxlen) == 1 ? SEG_GROUPS :
 inline size_t seg_smem_bytes(int maxlen, int groups) {
   const int nwarp = groups > 1 ? groups : seg_count(maxlen);
   return (size_t)nwarp * SEG_LINES * 2 * 2 * sizeof(float) + (size_t)groups * maxlen * (SEG_LINES + 1) * sizeof(float);
+}
+// ... and of a paired sweep (k_sweep_pair: two line groups, one warp per segment, or one warp when single)
+inline size_t pair_smem_bytes(int maxlen, bool single) {
+  const int nwarp = single ? 1 : seg_count(maxlen);
+  return (size_t)nwarp * SEG_LINES * 2 * 4 * sizeof(float) + (size_t)2 * maxlen * (SEG_LINES + 1) * sizeof(float);
 }
 
 // The face lines of a range of face tasks as one index space (fused face chains): tasks t[0..n), cum[q] the

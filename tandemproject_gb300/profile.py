@@ -3,26 +3,39 @@ profiling calls (ati_profile_enable / ati_profile_read: CUDA events around
 every launch on the case's stream).
 
 The case first steps `--warmup` times through its CUDA graph, then `--steps`
-times with the events; the table gives per class the time per launch, the
-launches and the share of the profiled time.
+times through the graph (wall clock around the steps: the graph-timed step),
+then `--steps` times with the events; the table gives per class the time per
+launch, the launches and the share of the profiled time.  `--no-fused`,
+`--no-tma` and `--no-pairs` switch the fused face chains, the TMA staging and
+the paired-line sweeps off (ati_set_options).
 
     python -m tandemproject_gb300.profile [--preset NAME] [--precision fp64|mixed|strict]
-                                          [--steps K] [--warmup W] [--json]
+                                          [--steps K] [--warmup W] [--no-fused] [--no-tma] [--no-pairs] [--json]
 """
 import argparse
 import json
 import sys
+import time
 
 
-def profile_case(preset="naca0012_8p8m", precision="fp64", steps=10, warmup=3):
-    """{class: (microseconds per launch, launches, share)}, tiles, ms per step."""
+def profile_case(preset="naca0012_8p8m", precision="fp64", steps=10, warmup=3, fused=True, tma=True, pairs=True,
+                 timing=None):
+    """{class: (microseconds per launch, launches, share)}, tiles, ms per step.  `timing` (a dict) receives the
+    graph-timed milliseconds per step and the options in effect."""
     from .config import FP64, FP64_STRICT, MIXED, PRESETS
     from .solver import setup_case
     prec = {"fp64": FP64, "mixed": MIXED, "strict": FP64_STRICT}[precision]
     case = setup_case(PRESETS[preset].replace(precision=prec))
     try:
+        opts = case.set_options(tma=tma, fused_faces=fused, paired_lines=pairs)
         case.step(warmup)
         case.synchronize()
+        t0 = time.perf_counter()
+        case.step(steps)
+        case.synchronize()
+        if timing is not None:
+            timing["graph_ms_per_step"] = 1000.0 * (time.perf_counter() - t0) / steps
+            timing["options"] = opts
         case.profile(True)
         case.step(steps)
         prof = case.profile_read()
@@ -41,15 +54,22 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "strict"])
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--no-fused", action="store_true")
+    ap.add_argument("--no-tma", action="store_true")
+    ap.add_argument("--no-pairs", action="store_true")
     ap.add_argument("--json", action="store_true")
     a = ap.parse_args(argv)
-    rows, tiles, ms_step = profile_case(a.preset, a.precision, a.steps, a.warmup)
+    tm = {}
+    rows, tiles, ms_step = profile_case(a.preset, a.precision, a.steps, a.warmup, not a.no_fused, not a.no_tma,
+                                        not a.no_pairs, tm)
     if a.json:
         print(json.dumps({"preset": a.preset, "precision": a.precision, "tiles": tiles, "ms_per_step": ms_step,
+                          "graph_ms_per_step": tm["graph_ms_per_step"], "options": tm["options"],
                           "classes": {k: {"us_per_launch": v[0], "launches": v[1], "share": v[2]}
                                       for k, v in rows.items()}}))
         return 0
-    print(f"{a.preset} {a.precision}: tiles {tiles}, {ms_step:.3f} ms per profiled step")
+    print(f"{a.preset} {a.precision}: tiles {tiles}, options {tm['options']}, "
+          f"{tm['graph_ms_per_step']:.3f} ms per graph step, {ms_step:.3f} ms per profiled step")
     for k, (us, n, share) in rows.items():
         print(f"  {k:<14s} {us:9.1f} us/launch {n:6d} launches {100 * share:6.1f} %")
     return 0
