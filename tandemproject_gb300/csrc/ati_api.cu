@@ -1223,8 +1223,16 @@ static double *field_base(ati_handle *h, int field, int &ncomp, const float **f3
 // The mixed path's step takes the viscous stresses inside its flux kernel and keeps no stress planes: the
 // forces and the stress output rebuild the last stage's planes (k_visc) from the derivative planes, viscosity
 // and primitives that stage left, which nothing changes until the next stage.
+// The step's viscous fluxes take the stresses at the point (no stress planes in a stage): the mixed path, and the
+// FP64 fast path without the LES term (whose stresses read rho of the stage's state)
+static bool stress_at_point(const ati_handle *h) {
+  return h->cfg.nviscous == 1 && (h->mixed || (h->cfg.precision == ATI_FP64 && h->cfg.les != 1));
+}
+// ... the stress planes are then made on demand, from the last stage's derivative planes
 static void stress_planes(ati_handle *h) {
-  if (h->mixed && h->cfg.nviscous == 1) fast::pointwise_f(h->ef, h->st, PW_VISC);
+  if (!stress_at_point(h)) return;
+  if (h->mixed) fast::pointwise_f(h->ef, h->st, PW_VISC);
+  else fast::pointwise_d(h->ed, h->st, PW_VISC);
 }
 
 static int copy_field(ati_handle *h, int blk, int field, double *host, bool to_dev) {
@@ -1776,9 +1784,9 @@ static int autotune_t(ati_handle *h, Eng<R> &e) {
   set_tiles(sg2, sg3, PT_DEFAULT);
   // point tiles, per pointwise kernel: their best sizes differ (the tile's set-up is a chain of dependent loads
   // that small tiles repeat for every point; large tiles leave a partial last wave of CTAs)
-  const int flux_kind = h->mixed && h->cfg.nviscous == 1 ? PW_FLUX_STRESS : PW_FLUX;
+  const int flux_kind = stress_at_point(h) ? PW_FLUX_STRESS : PW_FLUX;
   std::vector<int> kinds{PW_PRIM, flux_kind, PW_DIV, PW_RK};
-  if (!h->mixed && h->cfg.nviscous == 1) kinds.push_back(PW_VISC);
+  if (!stress_at_point(h) && h->cfg.nviscous == 1) kinds.push_back(PW_VISC);
   // the RK update rewrites qa from qo and de: qa is kept aside and put back (de and the stage planes written
   // here are recomputed before they are read)
   double *keep = h->ed.fw;
@@ -1884,11 +1892,11 @@ static int rk_stage_t(ati_handle *h, const Eng<R> &e, int nk) {
       SweepIO<R, R> io{e.prim, N, e.dv + (nn - 1) * N, 3 * N, nullptr, 4, 2, true};
       PROF(h, ATI_K_DERIV_XI + nn - 1, C::sweep(strict, e, s, nn, false, io));
     });
-    if (!Freestream<R>::on) PROF(h, ATI_K_VISC, C::pw(strict, e, st, PW_VISC));
+    if (!stress_at_point(h)) PROF(h, ATI_K_VISC, C::pw(strict, e, st, PW_VISC));
   }
-  // fluxes and their derivatives (src/Main3D.f90:710-768): five fields per launch; the mixed path takes the
-  // stresses inside the flux kernel and leaves the stress planes to stress_planes()
-  const bool fused = Freestream<R>::on && h->cfg.nviscous == 1;
+  // fluxes and their derivatives (src/Main3D.f90:710-768): five fields per launch; the mixed path and the FP64
+  // fast path take the stresses inside the flux kernel and leave the stress planes to stress_planes()
+  const bool fused = stress_at_point(h);
   PROF(h, ATI_K_FLUX, C::pw(strict, e, st, fused ? PW_FLUX_STRESS : PW_FLUX));
   PROF(h, ATI_K_MPIGO, C::mpigo(strict, e, st, tp(h, mpt), mpt.n, mpt.maxline, 0, e.flx,
                                 e.flx + N, e.flx + 2 * N, 3 * N, 5));
@@ -2118,10 +2126,8 @@ extern "C" int ati_case_forces(ati_handle_t *h, int cs, double out[2]) {
   if (!h->inited) return fail(h, ATI_ESTATE, "ati_init not called");
   const TaskRange &r = h->tl_force_c[cs];
   const int q0 = r.off - h->tl_force.off;  // position in the wall-face list
-  if (h->mixed) {
-    stress_planes(h);
-    strict::forces_f(h->ef, h->st, tp(h, r), r.n, h->area, h->wnor, h->dwoff + q0, h->dforce + 2 * q0);
-  }
+  stress_planes(h);
+  if (h->mixed) strict::forces_f(h->ef, h->st, tp(h, r), r.n, h->area, h->wnor, h->dwoff + q0, h->dforce + 2 * q0);
   else strict::forces_d(h->ed, h->st, tp(h, r), r.n, h->area, h->wnor, h->dwoff + q0, h->dforce + 2 * q0);
   CKL();
   std::vector<double> part((size_t)2 * r.n);

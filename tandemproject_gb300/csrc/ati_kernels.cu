@@ -1912,15 +1912,24 @@ __global__ void k_visc(Eng<R> e) {
 // combined, sigma = p I - tau, and the energy flux as
 // (rhoE + p) U - grad(xi) . (p u_inf + h).  VISC is a template argument so
 // that only one variant's operations are issued (a branch inside the point
-// loop was predicated, both sides executed).
-template <bool VISC>
+// loop was predicated, both sides executed).  AT_POINT: the stresses are taken
+// at the point (stress_point, the operations of k_visc) instead of read from
+// the stress planes, which then are neither written nor read in a stage.
+template <bool VISC, bool AT_POINT = false>
 __device__ __forceinline__ void flux_fast_point(const Eng<double> &e, int64_t N, int64_t g, double u1, double u2,
-                                                double u3) {
-  const double *t = e.tau;
+                                                double u3, const ViscConst<double> *V = nullptr) {
+  const double *tp = e.tau;
   double *F = e.flx;
   const double x1 = e.xim[g], x2 = e.xim[g + N], x3 = e.xim[g + 2 * N];
   const double e1 = e.etm[g], e2 = e.etm[g + N], e3 = e.etm[g + 2 * N];
   const double z1 = e.zem[g], z2 = e.zem[g + N], z3 = e.zem[g + 2 * N];
+  double tv[9];
+  if constexpr (VISC && AT_POINT) {
+    stress_point<double>(PlaneIn<double>{e, N, g}, *V, x1, x2, x3, e1, e2, e3, z1, z2, z3, tv);
+  } else if constexpr (VISC) {
+#pragma unroll
+    for (int k = 0; k < 9; k++) tv[k] = tp[g + k * N];
+  }
   const double pp = e.p[g];
   const double r1 = e.prim[g] + u1, r2 = e.prim[g + N] + u2, r3 = e.prim[g + 2 * N] + u3;
   const double s1 = x1 * r1 + x2 * r2 + x3 * r3;
@@ -1930,11 +1939,11 @@ __device__ __forceinline__ void flux_fast_point(const Eng<double> &e, int64_t N,
   F[g] = q * s1; F[g + N] = q * s2; F[g + 2 * N] = q * s3;
   double w1, w2, w3, sg[3][3];
   if constexpr (VISC) {
-    const double txx = t[g], tyy = t[g + N], tzz = t[g + 2 * N];
-    const double txy = t[g + 3 * N], tyz = t[g + 4 * N], tzx = t[g + 5 * N];
+    const double txx = tv[0], tyy = tv[1], tzz = tv[2];
+    const double txy = tv[3], tyz = tv[4], tzx = tv[5];
     sg[0][0] = pp - txx; sg[1][1] = pp - tyy; sg[2][2] = pp - tzz;
     sg[0][1] = sg[1][0] = -txy; sg[1][2] = sg[2][1] = -tyz; sg[0][2] = sg[2][0] = -tzx;
-    w1 = fma(pp, u1, t[g + 6 * N]); w2 = fma(pp, u2, t[g + 7 * N]); w3 = fma(pp, u3, t[g + 8 * N]);
+    w1 = fma(pp, u1, tv[6]); w2 = fma(pp, u2, tv[7]); w3 = fma(pp, u3, tv[8]);
   } else {
     w1 = pp * u1; w2 = pp * u2; w3 = pp * u3;
   }
@@ -2053,6 +2062,23 @@ __global__ void __launch_bounds__(256, Freestream<R>::on ? 5 : 1) k_flux(Eng<R> 
         }
         F[g + 12 * N] = a; F[g + 13 * N] = b; F[g + 14 * N] = c;
       }
+    }
+  }
+}
+
+// the FP64 fast path's viscous fluxes with the stresses taken at the point (k_visc and k_flux in one pass: the
+// nine stress planes are neither written nor read)
+__global__ void __launch_bounds__(256) k_flux_visc(Eng<double> e) {
+  const int64_t N = e.N;
+  TILE_LOOP(e, T) {
+    const Scheme &S = e.sc[T.cs];
+    const Scalars &SC = e.scal[T.cs];
+    const double u1 = SC.umf[1], u2 = SC.umf[2], u3 = SC.umf[3];
+    if (S.nviscous == 1) {
+      const ViscConst<double> V(S);
+      POINT_LOOP(T, g) flux_fast_point<true, true>(e, N, g, u1, u2, u3, &V);
+    } else {
+      POINT_LOOP(T, g) flux_fast_point<false>(e, N, g, u1, u2, u3);
     }
   }
 }
@@ -3044,8 +3070,9 @@ static void pointwise_t(const Eng<R> &eng, cudaStream_t st, int which) {
     case PW_CFL: k_cfl<R><<<g, t, 0, st>>>(e); break;
     case PW_VISC: k_visc<R><<<g, t, 0, st>>>(e); break;
     case PW_FLUX: k_flux<R><<<g, t, 0, st>>>(e); break;
-    case PW_FLUX_STRESS:  // the mixed path's viscous fluxes (the FP64 path writes the stress planes)
+    case PW_FLUX_STRESS:  // viscous fluxes with the stresses taken at the point (the strict FP64 path: k_visc)
       if constexpr (Freestream<R>::on) k_flux_staged<<<g, t, flux_staged_smem(t), st>>>(e);
+      else if constexpr (kFast) k_flux_visc<<<g, t, 0, st>>>(e);
       break;
     case PW_DIV: k_div<R><<<g, t, 0, st>>>(e); break;
     case PW_RK: k_rk<R><<<g, t, 0, st>>>(e); break;
