@@ -8,7 +8,11 @@ case, steps issued in chunks without waiting).
     python -m tandemproject_gb300.serve --requests 16 --step-scale 0.1
 
 Each request's result (final state, forces) is the same as when it runs
-alone: cases share nothing on the device.
+alone: cases share nothing on the device.  A request whose state turns
+non-finite (ATI_ENONFINITE after one of its chunks: the compact scheme has no
+shock capturing, and the upper corner of the parameter ranges can diverge) is
+retired as failed, with the steps it had run, and its memory goes to the
+others; the latency percentiles are those of the completed requests.
 """
 import argparse
 import concurrent.futures as cf
@@ -18,6 +22,8 @@ import time
 import numpy as np
 
 from .workloads import fold_free_case, footprint_bytes, relax, serving_requests, valid_grid
+
+ATI_ENONFINITE = 4
 
 
 def _gpu_case(cfg, grid):
@@ -55,7 +61,7 @@ class Server:
         thread while the loop keeps issuing steps to the running cases.  Its
         memory counts against the budget from admission on."""
         pending = sorted(requests, key=lambda r: r.arrival)
-        waiting, starting, active, done = [], [], [], []
+        waiting, starting, active, done, failed = [], [], [], [], []
         used = 0
         grids = {}
         pool = cf.ThreadPoolExecutor(max_workers=self.prefetch)
@@ -92,18 +98,38 @@ class Server:
                     cfg, c = s["job"].result()
                     starting.remove(s)
                     active.append({"req": s["req"], "case": c, "left": s["req"].steps, "fp": s["fp"],
-                                   "admitted": s["admitted"], "started": now(), "npts": cfg.npoints})
+                                   "admitted": s["admitted"], "started": now(), "npts": cfg.npoints,
+                                   "issued": 0, "checked": 0})
+            # a case whose last chunk is done: its status (a diverged request is retired as failed)
+            for a in list(active):
+                if a["issued"] > a["checked"] and a["case"].idle():
+                    try:
+                        a["case"].check()
+                        a["checked"] = a["issued"]
+                    except Exception as err:
+                        if getattr(err, "code", None) != ATI_ENONFINITE:
+                            raise
+                        r = a["req"]
+                        rec = {"id": r.rid, "points": a["npts"], "steps": r.steps, "steps_run": a["issued"],
+                               "arrival": r.arrival, "failed_at": now(), "error": str(err),
+                               "params": {k: getattr(r.cfg, k) for k in ("mach", "aoa_deg", "thick", "turb_intensity")}}
+                        a["case"].close()
+                        used -= a["fp"]
+                        active.remove(a)
+                        failed.append(rec)
+                        if log:
+                            log(f"t={now():7.2f}s FAILED #{r.rid} after {a['issued']} of {r.steps} steps: {err}")
             # one chunk of steps for every running case, issued without waiting
             for a in active:
-                if a["left"] > 0 and a["case"].idle():
+                if a["left"] > 0 and a["case"].idle() and a["checked"] == a["issued"]:
                     k = min(self.chunk, a["left"])
                     a["case"].step_async(k)
                     a["left"] -= k
+                    a["issued"] += k
             # retire finished cases
             for a in list(active):
-                if a["left"] == 0 and a["case"].idle():
+                if a["left"] == 0 and a["case"].idle() and a["checked"] == a["issued"]:
                     c = a["case"]
-                    c.check()
                     rec = {"id": a["req"].rid, "points": a["npts"], "steps": a["req"].steps,
                            "arrival": a["req"].arrival, "admitted": a["admitted"], "started": a["started"],
                            "done": now(), "forces": c.forces().tolist()}
@@ -123,15 +149,18 @@ class Server:
         pool.shutdown()
         setup.shutdown()
         makespan = now()
-        lat = np.array([d["latency"] for d in done])
-        wait = np.array([d["admitted"] - d["arrival"] for d in done])
+        lat = np.array([d["latency"] for d in done] or [np.nan])
+        wait = np.array([d["admitted"] - d["arrival"] for d in done] or [np.nan])
         work = sum(d["points"] * 4 * d["steps"] for d in done)
         summary = {"requests": len(done), "makespan_s": makespan,
                    "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
                                  "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
                    "admission_wait_s": {"p50": float(np.percentile(wait, 50)), "max": float(wait.max())},
                    "admission_bound": self.bound,
-                   "updates_per_s": work / makespan, "peak_resident_gib": self.peak_bytes / 2**30}
+                   "updates_per_s": work / makespan, "peak_resident_gib": self.peak_bytes / 2**30,
+                   "failed": len(failed),
+                   "failed_requests": [{k: f[k] for k in ("id", "points", "steps", "steps_run", "params")}
+                                       for f in failed]}
         return done, summary
 
 

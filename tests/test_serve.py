@@ -90,3 +90,29 @@ def test_results_same_alone_and_in_the_mix(ati_lib):
             np.testing.assert_array_equal(q, alone.get_state(mb))
         np.testing.assert_array_equal(d["forces"], alone.forces())
         alone.close()
+
+
+class DivergingCase(FakeCase):
+    """A stand-in whose state turns non-finite after `bad_after` steps (the cases with aoa_deg > 5)."""
+
+    def check(self):
+        from tandemproject_gb300.solver import AtiError
+        if self.cfg.aoa_deg > 5 and self.steps >= 20:
+            raise AtiError(4, "non-finite or non-positive density/pressure in the state of case 0")
+
+
+def test_scheduler_retires_a_diverged_request_and_serves_the_rest():
+    from tandemproject_gb300.config import small_case
+    from tandemproject_gb300.serve import Server
+    reqs = [Request(i, small_case(aoa_deg=8.0 if i in (2, 5) else 0.0), 40 + i, 0.001 * i, {}) for i in range(8)]
+    srv = Server(budget_bytes=30, chunk=7, make_case=DivergingCase, make_grid=lambda cfg: (cfg, None),
+                 footprint=lambda cfg: 10)
+    FakeCase.live = FakeCase.peak = 0
+    done, summary = srv.run(reqs)
+    assert sorted(d["id"] for d in done) == [0, 1, 3, 4, 6, 7]
+    assert summary["failed"] == 2 and sorted(f["id"] for f in summary["failed_requests"]) == [2, 5]
+    for f in summary["failed_requests"]:
+        assert f["steps_run"] == 21 and f["params"]["aoa_deg"] == 8.0  # retired after the chunk that diverged
+    assert FakeCase.live == 0  # every case closed, the failed ones too
+    for d in done:
+        assert d["forces"][0] == d["steps"]
