@@ -65,6 +65,15 @@ FIELD_SWEEPS_PER_STEP = {"deriv": 4 * (4 + 5), "filter": 5}
 # 3.54 M-point case: 489.35 MB for 17.69 M units); the kernel streams, so the
 # traffic of a launch scales with the units it processes
 SWEEP_TRAFFIC_PER_UNIT = {"deriv_xi": 489.35e6 / (5 * 3538944)}
+# DRAM bytes per point of k_flux_visc measured with ncu on the 3.54 M-point case (None: not captured)
+FLUX_TRAFFIC_PER_POINT = None
+# algorithmic bytes per point of the FP64 fast path's viscous flux kernel k_flux_visc (the stresses of k_visc taken
+# at the point): it reads the metrics (72 B), the twelve derivative planes of u, v, w, T (96 B), Jacobian and
+# viscosity (16 B), velocity (24 B), pressure (8 B) and the state (40 B), and writes 15 fluxes (120 B)
+FLUX_BYTES_FP64 = 376
+# its FP64 flops per point (an FMA counts two): 101 for the stresses, 115 for the fluxes, counted from the kernel's
+# expressions
+FLUX_FLOPS_FP64 = 216
 # canonical bytes per grid-point-stage of the whole stage: 141 FP64 words, or
 # the mixed data flow with FP32 intermediates and FP64 state/metrics
 STAGE_BYTES_FP64 = 1128
@@ -477,36 +486,61 @@ def main():
     case.profile(False)
     tot = sum(v[0] for v in prof.values())
     dom = max(prof, key=lambda k: prof[k][0])
-    dom_ms, dom_n = prof[dom]
-    kind = "filter" if dom.startswith("filter") else "deriv"
     hbm_peak, peak_src = measured_peaks()
-    # units (point x field) one launch of this class processes, on average over the profiled steps
-    units = npts * FIELD_SWEEPS_PER_STEP[kind] * 2 / max(dom_n, 1)
-    t_launch = dom_ms / max(dom_n, 1) / 1e3
-    achieved = SWEEP_BYTES[kind] * units / t_launch / 1e9
     fp64_peak = probe_fma_tflops(True)
-    fp64_ach = SWEEP_FLOPS[kind] * units / t_launch / 1e12
-    traffic = SWEEP_TRAFFIC_PER_UNIT[dom] * units if dom in SWEEP_TRAFFIC_PER_UNIT else None
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": traffic,
+
+    def sweep_roofline(cls):
+        """roofline of one line-sweep class: units (point x field) one launch processes, on average over the
+        profiled steps, at that class's average launch duration"""
+        ms, n = prof[cls]
+        kind = "filter" if cls.startswith("filter") else "deriv"
+        units = npts * FIELD_SWEEPS_PER_STEP[kind] * 2 / max(n, 1)
+        t = ms / max(n, 1) / 1e3
+        ach = SWEEP_BYTES[kind] * units / t / 1e9
+        ach64 = SWEEP_FLOPS[kind] * units / t / 1e12
+        return {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+                "traffic": SWEEP_TRAFFIC_PER_UNIT[cls] * units if cls in SWEEP_TRAFFIC_PER_UNIT else None,
                 "traffic_source": "ncu DRAM bytes per unit of one launch on the 3.54 M-point case, scaled by units",
-                "kernel": f"k_sweep<{dom}>: one launch = every line of one direction over all blocks for "
+                "kernel": f"k_sweep<{cls}>: one launch = every line of one direction over all blocks for "
                           f"{units / npts:.1f} fields on average ({units:.3e} point-fields), "
                           f"{SWEEP_BYTES[kind]} B and {SWEEP_FLOPS[kind]} flop per point-field",
-                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak,
-                         "peak_source": "measured FP64 FMA throughput of this GPU (ati_probe_fma_tflops)"},
-                "limit": "the FP64 pipe (ncu: 89-92 % busy in the line sweeps and k_flux at 12-34 % of HBM); "
-                         "frac is against HBM, fp64.frac against the FP64 FMA peak",
-                "stage_hbm_frac": STAGE_BYTES_FP64 * value / ws / 1e9 / hbm_peak,
-                "kernel_share": {k: round(v[0] / tot, 4) for k, v in prof.items() if v[1]}}
+                "fp64": {"achieved_tflops": ach64, "peak_tflops": fp64_peak, "frac": ach64 / fp64_peak}}
+
+    sweep_cls = max((k for k in prof if k.startswith(("deriv", "filter")) and prof[k][1]), key=lambda k: prof[k][0])
+    if dom == "flux" and cfg.nviscous == 1:
+        # the viscous flux kernel with the stresses at the point (k_flux_visc): one launch covers every point
+        ms, n = prof["flux"]
+        t = ms / max(n, 1) / 1e3
+        achieved = FLUX_BYTES_FP64 * npts / t / 1e9
+        fp64_ach = FLUX_FLOPS_FP64 * npts / t / 1e12
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": achieved / hbm_peak,
+                    "traffic": FLUX_TRAFFIC_PER_POINT * npts if FLUX_TRAFFIC_PER_POINT else None,
+                    "traffic_source": "ncu DRAM bytes per point of one launch on the 3.54 M-point case, scaled by "
+                                      "points",
+                    "kernel": f"k_flux_visc (viscous fluxes with the stresses at the point): one launch = every point "
+                              f"({npts}), {FLUX_BYTES_FP64} B and {FLUX_FLOPS_FP64} FP64 flop per point",
+                    "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak}}
+    else:
+        roofline = sweep_roofline(dom)
+    roofline["fp64"]["peak_source"] = "measured FP64 FMA throughput of this GPU (ati_probe_fma_tflops)"
+    roofline.update({
+        "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+        "limit": "the FP64 pipe (ncu: 89-92 % busy in the line sweeps and the flux kernel at 12-34 % of HBM); "
+                 "frac is against HBM, fp64.frac against the FP64 FMA peak",
+        "stage_hbm_frac": STAGE_BYTES_FP64 * value / ws / 1e9 / hbm_peak,
+        "kernel_share": {k: round(v[0] / tot, 4) for k, v in prof.items() if v[1]}})
+    if dom != sweep_cls:
+        roofline["largest_sweep"] = sweep_roofline(sweep_cls)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: NACA 0012 grid from the reference's grid generator (restated), uniform freestream "
-                    "initial state, impulsive start (nsmf = 1); seeded von Karman inflow turbulence when the "
-                    "preset has it (2.5 % of U_inf, L = 0.1 c, 2048 modes, seed 1234)",
+                    "initial state, " + ("impulsive start (nsmf = 1)" if cfg.nsmf == 1 else
+                                         f"the reference deck's smooth start (nsmf = 0, timf = {cfg.timf:g})") +
+                    "; seeded von Karman inflow turbulence when the preset has it (2.5 % of U_inf, L = 0.1 c, "
+                    "2048 modes, seed 1234)",
             "config": {"workload": f"{args.preset}: NACA 0012, 6 blocks "
                                    f"{'x'.join(str(v + 1) for v in (cfg.lxibk[0], cfg.letbk[0], cfg.lzebk[0]))}, "
                                    f"{npts} points, FP64, RK4, Re 4e5, M 0.24",

@@ -304,7 +304,8 @@ int ati_tiles(ati_handle_t *h, int32_t out[4]);
  * graphs at the next step. */
 int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
 /* Kernel options (no counterpart in the reference; results do not depend on
- * them, only timings do).  All are on by default.
+ * them, only timings do).  ATI_OPT_TMA and ATI_OPT_PAIRED_LINES are on by
+ * default, ATI_OPT_FUSED_FACES off (measured slower inside the step graphs).
  *  ATI_OPT_TMA: the mixed path's segmented eta and zeta derivative sweeps
  *    stage each tile of 32 lines into shared memory with one tensor copy
  *    (TMA, cp.async.bulk.tensor) on every direction whose blocks' FP32 planes
@@ -316,8 +317,8 @@ int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
  *    phases are ordered by grid barriers with bounded waits (see
  *    ati_set_spin_limit), instead of one launch per face kind and direction.
  *  ATI_OPT_PAIRED_LINES: the mixed path's segmented derivative sweeps solve
- *    two groups of 32 lines per CTA, each lane two lines (lines of up to
- *    about 800 points; longer ones one group per CTA).
+ *    two groups of 32 lines per CTA, each lane two lines, on lines of up to
+ *    four segments (192 points; longer ones one group per CTA).
  * *active (may be NULL) gets the options in effect, plus ATI_OPT_TMA_ETA and
  * ATI_OPT_TMA_ZETA for the directions staged by TMA.  Waits for the steps in
  * flight; the step graphs are captured again. */

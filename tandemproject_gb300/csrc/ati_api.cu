@@ -59,7 +59,7 @@ struct ati_handle {
   bool any_cfl = false;  // some case takes its dt from the CFL condition (dto < 0)
   bool tma[4] = {false, false, false, false};  // tensor maps exist for the mixed path's eta/zeta sweeps
   std::vector<TmaMap> htmaps;                   // host copy of the tensor maps (kept for the upload)
-  bool fused = true;                            // fused face chains (ati_set_options)
+  bool fused = false;                           // fused face chains (ati_set_options)
   unsigned spin_limit = 1u << 24;               // polls a device barrier wait may take (ati_set_spin_limit)
   int64_t *dcum = nullptr;                      // running face-line counts of the task list (fused chains)
   unsigned *dbar = nullptr;                     // grid-barrier counters of the fused chains

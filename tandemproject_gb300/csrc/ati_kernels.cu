@@ -1134,9 +1134,12 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
 // rows, as in k_sweep_seg); with TMA each half comes in as one tensor copy, both
 // counted on one mbarrier.
 // ---------------------------------------------------------------------------
-template <int NN, bool TMA>
+// ADJ: the second half's line l lies SEG_LINES points after the first half's (zeta lines, and eta lines in row
+// tiles): its results are stored at a fixed offset from the first half's, through one walking pointer.
+template <int NN, bool TMA, bool ADJ>
 __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<float, float, float> a, const float *rtab,
                                                                    int single) {
+  static_assert(!ADJ || NN != 1, "adjacent halves: eta/zeta lines");
   extern __shared__ __align__(16) unsigned char seg_smem[];
   constexpr int RS = TMA ? SEG_LINES : SEG_LINES + 1;
   __shared__ uint64_t tbar;
@@ -1389,9 +1392,13 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<flo
         }
         if constexpr (D) {
           *po0 = q[0];
-          if (act1) *po1 = q[1];
+          if constexpr (ADJ) {
+            if (act1) po0[SEG_LINES] = q[1];
+          } else {
+            if (act1) *po1 = q[1];
+            po1 -= stride;
+          }
           po0 -= stride;
-          po1 -= stride;
         } else {
           c[0] = q[0];
           c[HS] = q[1];
@@ -1508,9 +1515,13 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<flo
         float *po0 = out + base0 + (int64_t)i * stride, *po1 = out + base1 + (int64_t)i * stride;
         auto put = [&](const float r[2]) {
           *po0 = r[0];
-          if (act1) *po1 = r[1];
+          if constexpr (ADJ) {
+            if (act1) po0[SEG_LINES] = r[1];
+          } else {
+            if (act1) *po1 = r[1];
+            po1 += stride;
+          }
           po0 += stride;
-          po1 += stride;
         };
         for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
           const float2 n0 = l2(tr + 4 * SEG_RT), n1 = l2(tr + 5 * SEG_RT), n2 = l2(tr + 6 * SEG_RT);
@@ -2922,17 +2933,25 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
           // eta/zeta derivative sweeps of an array with tensor maps: tiles staged by TMA
           const int arr = io.in == e.prim ? 0 : (io.in == e.flx + (int64_t)(nn - 1) * e.N ? 1 : -1);
           const bool tma = !filt && nn >= 2 && e.tma[nn] && arr >= 0;
-          // paired lines: a CTA solves two groups of lines, lane l line l of each
+          // paired lines: a CTA solves two groups of lines, lane l line l of each (lines of up to PAIR_MAX_SEG
+          // segments: longer ones would halve the CTAs an SM holds, measured slower)
           const size_t psm = pair_smem_bytes(C.maxlen, G > 1) + 128;
-          if (!filt && e.pairs && psm <= SEG_SMEM_MAX) {
+          if (!filt && e.pairs && seg_count(C.maxlen) <= PAIR_MAX_SEG && psm <= SEG_SMEM_MAX) {
             const int single = G > 1 ? 1 : 0;
             const dim3 gp(single ? C.n : C.n / 2, io.nf);
             const int ntp = SEG_LINES * (single ? 1 : seg_count(C.maxlen));
+            const bool adj = nn == 3 || (nn == 2 && e.eta_rowtiles);
             if (tma) a.tmap = e.tmaps + (int64_t)(arr * 2 + nn - 2) * e.nblk;
-#define ATI_PAIR(D, T) k_sweep_pair<D, T><<<gp, ntp, psm, st>>>(a, seg, single)
-            if (nn == 1) ATI_PAIR(1, false);
-            else if (nn == 2) { if (tma) ATI_PAIR(2, true); else ATI_PAIR(2, false); }
-            else { if (tma) ATI_PAIR(3, true); else ATI_PAIR(3, false); }
+#define ATI_PAIR(D, T, J) k_sweep_pair<D, T, J><<<gp, ntp, psm, st>>>(a, seg, single)
+            if (nn == 1) ATI_PAIR(1, false, false);
+            else if (nn == 2) {
+              if (tma) ATI_PAIR(2, true, true);
+              else if (adj) ATI_PAIR(2, false, true);
+              else ATI_PAIR(2, false, false);
+            } else {
+              if (tma) ATI_PAIR(3, true, true);
+              else ATI_PAIR(3, false, true);
+            }
 #undef ATI_PAIR
             continue;
           }
@@ -2998,11 +3017,12 @@ static cudaError_t seg_attr() {
   if constexpr (std::is_same<TI, float>::value) {
     if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<2, false, true, TI, TO>);
     if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<3, false, true, TI, TO>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<1, false>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, false>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, false>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, true>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<1, false, false>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, false, false>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, false, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, false, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, true, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, true, true>);
   }
   return e;
 }

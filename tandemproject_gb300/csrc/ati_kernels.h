@@ -184,6 +184,8 @@ inline size_t seg_smem_bytes(int maxlen, int groups) {
   const int nwarp = groups > 1 ? groups : seg_count(maxlen);
   return (size_t)nwarp * SEG_LINES * 2 * 2 * sizeof(float) + (size_t)groups * maxlen * (SEG_LINES + 1) * sizeof(float);
 }
+// Paired sweeps (k_sweep_pair) take the classes of lines of up to PAIR_MAX_SEG segments
+constexpr int PAIR_MAX_SEG = 4;
 // ... and of a paired sweep (k_sweep_pair: two line groups, one warp per segment, or one warp when single)
 inline size_t pair_smem_bytes(int maxlen, bool single) {
   const int nwarp = single ? 1 : seg_count(maxlen);

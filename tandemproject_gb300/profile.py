@@ -5,12 +5,12 @@ every launch on the case's stream).
 The case first steps `--warmup` times through its CUDA graph, then `--steps`
 times through the graph (wall clock around the steps: the graph-timed step),
 then `--steps` times with the events; the table gives per class the time per
-launch, the launches and the share of the profiled time.  `--no-fused`,
-`--no-tma` and `--no-pairs` switch the fused face chains, the TMA staging and
-the paired-line sweeps off (ati_set_options).
+launch, the launches and the share of the profiled time.  `--fused` switches
+the fused face chains on, `--no-tma` and `--no-pairs` the TMA staging and the
+paired-line sweeps off (ati_set_options).
 
     python -m tandemproject_gb300.profile [--preset NAME] [--precision fp64|mixed|strict]
-                                          [--steps K] [--warmup W] [--no-fused] [--no-tma] [--no-pairs] [--json]
+                                          [--steps K] [--warmup W] [--fused] [--no-tma] [--no-pairs] [--json]
 """
 import argparse
 import json
@@ -18,7 +18,7 @@ import sys
 import time
 
 
-def profile_case(preset="naca0012_8p8m", precision="fp64", steps=10, warmup=3, fused=True, tma=True, pairs=True,
+def profile_case(preset="naca0012_8p8m", precision="fp64", steps=10, warmup=3, fused=False, tma=True, pairs=True,
                  timing=None):
     """{class: (microseconds per launch, launches, share)}, tiles, ms per step.  `timing` (a dict) receives the
     graph-timed milliseconds per step and the options in effect."""
@@ -54,13 +54,13 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "strict"])
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--no-fused", action="store_true")
+    ap.add_argument("--fused", action="store_true")
     ap.add_argument("--no-tma", action="store_true")
     ap.add_argument("--no-pairs", action="store_true")
     ap.add_argument("--json", action="store_true")
     a = ap.parse_args(argv)
     tm = {}
-    rows, tiles, ms_step = profile_case(a.preset, a.precision, a.steps, a.warmup, not a.no_fused, not a.no_tma,
+    rows, tiles, ms_step = profile_case(a.preset, a.precision, a.steps, a.warmup, a.fused, not a.no_tma,
                                         not a.no_pairs, tm)
     if a.json:
         print(json.dumps({"preset": a.preset, "precision": a.precision, "tiles": tiles, "ms_per_step": ms_step,

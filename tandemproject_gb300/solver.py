@@ -283,10 +283,10 @@ class Case:
         t = (ctypes.c_int32 * 4)(0, eta, zeta, points)
         self._chk(self.L.ati_set_tiles(self.h, t))
 
-    def set_options(self, tma=True, fused_faces=True, paired_lines=True):
-        """Kernel options (results do not depend on them): TMA staging of the mixed path's segmented eta/zeta
-        sweeps, fused face chains, paired-line segmented derivative sweeps.  Returns the options in effect as a
-        dict."""
+    def set_options(self, tma=True, fused_faces=False, paired_lines=True):
+        """Kernel options (results do not depend on them; the library's defaults): TMA staging of the mixed path's
+        segmented eta/zeta sweeps, fused face chains, paired-line segmented derivative sweeps.  Returns the options
+        in effect as a dict."""
         a = ctypes.c_int32()
         flags = ((OPT_TMA if tma else 0) | (OPT_FUSED_FACES if fused_faces else 0)
                  | (OPT_PAIRED_LINES if paired_lines else 0))
