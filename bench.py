@@ -65,15 +65,16 @@ FIELD_SWEEPS_PER_STEP = {"deriv": 4 * (4 + 5), "filter": 5}
 # 3.54 M-point case: 489.35 MB for 17.69 M units); the kernel streams, so the
 # traffic of a launch scales with the units it processes
 SWEEP_TRAFFIC_PER_UNIT = {"deriv_xi": 489.35e6 / (5 * 3538944)}
-# DRAM bytes per point of k_flux_visc measured with ncu on the 3.54 M-point case (None: not captured)
-FLUX_TRAFFIC_PER_POINT = None
+# DRAM bytes per point of k_flux_visc measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch
+# on the 3.54 M-point case: 906.4 + 395.5 MB); the kernel streams, so the traffic scales with the points
+FLUX_TRAFFIC_PER_POINT = (906.36e6 + 395.46e6) / 3538944
 # algorithmic bytes per point of the FP64 fast path's viscous flux kernel k_flux_visc (the stresses of k_visc taken
 # at the point): it reads the metrics (72 B), the twelve derivative planes of u, v, w, T (96 B), Jacobian and
 # viscosity (16 B), velocity (24 B), pressure (8 B) and the state (40 B), and writes 15 fluxes (120 B)
 FLUX_BYTES_FP64 = 376
-# its FP64 flops per point (an FMA counts two): 101 for the stresses, 115 for the fluxes, counted from the kernel's
-# expressions
-FLUX_FLOPS_FP64 = 216
+# its FP64 flops per point (an FMA counts two), from ncu's opcode counts of one launch on the 3.54 M-point case:
+# 81 DFMA, 42 DMUL and 15 DADD a point
+FLUX_FLOPS_FP64 = 219
 # canonical bytes per grid-point-stage of the whole stage: 141 FP64 words, or
 # the mixed data flow with FP32 intermediates and FP64 state/metrics
 STAGE_BYTES_FP64 = 1128

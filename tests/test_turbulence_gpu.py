@@ -178,7 +178,10 @@ def test_config2_inflow_turbulence_matches_oracle(ati_lib, oracle_lib):
     whose mode sum matches the restatement's.  The default FP64 mode sums the
     modes in FP32; its error against the same run is reported beside it."""
     from tandemproject_gb300.config import FP64, FP64_STRICT, PRESETS
-    cfg = PRESETS["naca0012_8p8m"].replace(precision=FP64_STRICT)
+    # from the impulsive start (the uniform freestream moving at once), which runs some 600 steps on this grid: the
+    # momentum is then of full size, and its relative error means what it says (under the preset's smooth start the
+    # momentum of the first steps is a small fraction of it)
+    cfg = PRESETS["naca0012_8p8m"].replace(precision=FP64_STRICT, nsmf=1)
     assert cfg.turb_intensity == 0.025 and cfg.turb_modes == 2048 and cfg.turb_seed == 1234
     gpu, orc = _pair_with_turbulence(cfg)
     gpu.step(25)
