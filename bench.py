@@ -522,8 +522,11 @@ def main():
                     "kernel": f"k_flux_visc (viscous fluxes with the stresses at the point): one launch = every point "
                               f"({npts}), {FLUX_BYTES_FP64} B and {FLUX_FLOPS_FP64} FP64 flop per point",
                     "fp64": {"achieved_tflops": fp64_ach, "peak_tflops": fp64_peak, "frac": fp64_ach / fp64_peak}}
-    else:
+    elif dom.startswith(("deriv", "filter")):
         roofline = sweep_roofline(dom)
+    else:  # (a class with no algorithmic count leads only when launches are serialised, e.g. under a profiler)
+        roofline = sweep_roofline(sweep_cls)
+        roofline["note"] = f"largest class {dom} has no algorithmic byte count; the largest sweep class is shown"
     roofline["fp64"]["peak_source"] = "measured FP64 FMA throughput of this GPU (ati_probe_fma_tflops)"
     roofline.update({
         "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
@@ -531,7 +534,7 @@ def main():
                  "frac is against HBM, fp64.frac against the FP64 FMA peak",
         "stage_hbm_frac": STAGE_BYTES_FP64 * value / ws / 1e9 / hbm_peak,
         "kernel_share": {k: round(v[0] / tot, 4) for k, v in prof.items() if v[1]}})
-    if dom != sweep_cls:
+    if dom != sweep_cls and "note" not in roofline:
         roofline["largest_sweep"] = sweep_roofline(sweep_cls)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
