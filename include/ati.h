@@ -304,8 +304,9 @@ int ati_tiles(ati_handle_t *h, int32_t out[4]);
  * graphs at the next step. */
 int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
 /* Kernel options (no counterpart in the reference; results do not depend on
- * them, only timings do).  ATI_OPT_TMA and ATI_OPT_PAIRED_LINES are on by
- * default, ATI_OPT_FUSED_FACES off (measured slower inside the step graphs).
+ * them, only timings do).  ATI_OPT_TMA, ATI_OPT_PAIRED_LINES and
+ * ATI_OPT_STRESS_AT_POINT are on by default, ATI_OPT_FUSED_FACES off
+ * (measured slower inside the step graphs).
  *  ATI_OPT_TMA: the mixed path's segmented eta and zeta derivative sweeps
  *    stage each tile of 32 lines into shared memory with one tensor copy
  *    (TMA, cp.async.bulk.tensor) on every direction whose blocks' FP32 planes
@@ -319,6 +320,11 @@ int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
  *  ATI_OPT_PAIRED_LINES: the mixed path's segmented derivative sweeps solve
  *    two groups of 32 lines per CTA, each lane two lines, on lines of up to
  *    four segments (192 points; longer ones one group per CTA).
+ *  ATI_OPT_STRESS_AT_POINT: the ATI_FP64 path's viscous fluxes take the
+ *    stresses at the point inside the flux kernel instead of writing and
+ *    reading nine stress planes (no effect in the strict mode, the mixed path
+ *    or with the LES term; the stress output and the forces rebuild the planes
+ *    on demand).
  * *active (may be NULL) gets the options in effect, plus ATI_OPT_TMA_ETA and
  * ATI_OPT_TMA_ZETA for the directions staged by TMA.  Waits for the steps in
  * flight; the step graphs are captured again. */
@@ -327,6 +333,7 @@ int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
 #define ATI_OPT_TMA_ETA 4
 #define ATI_OPT_TMA_ZETA 8
 #define ATI_OPT_PAIRED_LINES 16
+#define ATI_OPT_STRESS_AT_POINT 32
 int ati_set_options(ati_handle_t *h, int flags, int32_t *active);
 /* Device-side waits are bounded (no counterpart in the reference): a grid
  * barrier of the fused face chains gives up after this many polls (0 = the

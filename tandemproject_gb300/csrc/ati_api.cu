@@ -60,6 +60,7 @@ struct ati_handle {
   bool tma[4] = {false, false, false, false};  // tensor maps exist for the mixed path's eta/zeta sweeps
   std::vector<TmaMap> htmaps;                   // host copy of the tensor maps (kept for the upload)
   bool fused = false;                           // fused face chains (ati_set_options)
+  bool fp64_at_point = true;                    // FP64 viscous fluxes with the stresses at the point (ati_set_options)
   unsigned spin_limit = 1u << 24;               // polls a device barrier wait may take (ati_set_spin_limit)
   int64_t *dcum = nullptr;                      // running face-line counts of the task list (fused chains)
   unsigned *dbar = nullptr;                     // grid-barrier counters of the fused chains
@@ -1226,7 +1227,7 @@ static double *field_base(ati_handle *h, int field, int &ncomp, const float **f3
 // The step's viscous fluxes take the stresses at the point (no stress planes in a stage): the mixed path, and the
 // FP64 fast path without the LES term (whose stresses read rho of the stage's state)
 static bool stress_at_point(const ati_handle *h) {
-  return h->cfg.nviscous == 1 && (h->mixed || (h->cfg.precision == ATI_FP64 && h->cfg.les != 1));
+  return h->cfg.nviscous == 1 && (h->mixed || (h->cfg.precision == ATI_FP64 && h->cfg.les != 1 && h->fp64_at_point));
 }
 // ... the stress planes are then made on demand, from the last stage's derivative planes
 static void stress_planes(ati_handle *h) {
@@ -1420,17 +1421,18 @@ extern "C" int ati_set_tiles(ati_handle_t *h, const int32_t in[4]) {
 
 extern "C" int ati_set_options(ati_handle_t *h, int flags, int32_t *active) {
   if (!h) return fail(h, ATI_EINVAL, "null handle");
-  if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES | ATI_OPT_PAIRED_LINES))
+  if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES | ATI_OPT_PAIRED_LINES | ATI_OPT_STRESS_AT_POINT))
     return fail(h, ATI_EINVAL, "ati_set_options: unknown flag");
   CK(cudaStreamSynchronize(h->st));
   drop_graphs(h);
   for (int nn = 2; nn <= 3; nn++) h->ef.tma[nn] = (flags & ATI_OPT_TMA) != 0 && h->tma[nn];
   h->fused = (flags & ATI_OPT_FUSED_FACES) != 0;
   h->ef.pairs = (flags & ATI_OPT_PAIRED_LINES) != 0;
+  h->fp64_at_point = (flags & ATI_OPT_STRESS_AT_POINT) != 0;
   if (active)
     *active = (h->ef.tma[2] || h->ef.tma[3] ? ATI_OPT_TMA : 0) | (h->fused ? ATI_OPT_FUSED_FACES : 0) |
               (h->ef.tma[2] ? ATI_OPT_TMA_ETA : 0) | (h->ef.tma[3] ? ATI_OPT_TMA_ZETA : 0) |
-              (h->ef.pairs ? ATI_OPT_PAIRED_LINES : 0);
+              (h->ef.pairs ? ATI_OPT_PAIRED_LINES : 0) | (h->fp64_at_point ? ATI_OPT_STRESS_AT_POINT : 0);
   return ATI_OK;
 }
 

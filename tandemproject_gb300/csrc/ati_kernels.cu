@@ -1937,6 +1937,11 @@ __device__ __forceinline__ void flux_fast_point(const Eng<double> &e, int64_t N,
   double tv[9];
   if constexpr (VISC && AT_POINT) {
     stress_point<double>(PlaneIn<double>{e, N, g}, *V, x1, x2, x3, e1, e2, e3, z1, z2, z3, tv);
+    // each stress leaves the stress arithmetic rounded, as k_visc stores it: the (empty) register barrier keeps the
+    // compiler from contracting its last product into the flux arithmetic, so the fluxes round as when they read the
+    // stress planes, bit for bit
+#pragma unroll
+    for (int k = 0; k < 9; k++) asm volatile("" : "+d"(tv[k]));
   } else if constexpr (VISC) {
 #pragma unroll
     for (int k = 0; k < 9; k++) tv[k] = tp[g + k * N];

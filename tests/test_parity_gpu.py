@@ -267,3 +267,25 @@ def test_newton_reciprocal_and_rsqrt_bounds(ati_lib):
     print("Newton reciprocal / rsqrt, worst relative difference", worst[0], worst[1])
     assert 0.0 <= worst[0] <= 4 * 2.0 ** -53
     assert 0.0 <= worst[1] <= 4 * 2.0 ** -53
+
+
+@pytest.mark.parametrize("lxibk", [(24, 64, 24), (48, 120, 48)])
+def test_fp64_stresses_at_the_point_bit_identical(ati_lib, lxibk):
+    """The ATI_FP64 path's viscous fluxes with the stresses of k_visc taken at the
+    point (ATI_OPT_STRESS_AT_POINT, on by default) round exactly as the stress
+    planes written by k_visc and read by k_flux: states bit for bit after 12
+    steps, and the stress output rebuilt on demand equals the planes."""
+    from tandemproject_gb300.config import FP64
+    from tandemproject_gb300.solver import setup_case
+    cfg = small_case(lxibk=lxibk, letbk=(39, 39), lzebk=(12,), precision=FP64)
+    a, b = setup_case(cfg), setup_case(cfg)
+    assert a.set_options(stress_at_point=True)["stress_at_point"]
+    assert not b.set_options(stress_at_point=False)["stress_at_point"]
+    a.step(12)
+    b.step(12)
+    for mb in range(cfg.nblocks):
+        assert np.array_equal(a.get_state(mb), b.get_state(mb)), mb
+        assert np.array_equal(a.get_field(mb, 10), b.get_field(mb, 10)), mb
+    assert np.array_equal(a.forces(), b.forces())
+    a.close()
+    b.close()
