@@ -81,6 +81,18 @@ STAGE_BYTES_FP64 = 1128
 STAGE_BYTES_MIXED = 728
 
 
+def max_over_ranks(t, dist):
+    """The largest of every rank's t (the job's time is its slowest rank's): an all-reduce over the process group,
+    on the GPU under NCCL, on the host under gloo; t itself without a group."""
+    if dist is None:
+        return t
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -373,10 +385,7 @@ def main():
     ms = e0.elapsed_time(e1)
     launches = case.launch_count() - l0
     t_dev = ms / 1e3
-    if dist is not None:
-        tt = torch.tensor([t_dev], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
+    t_dev = max_over_ranks(t_dev, dist)
     value = npts * cfg.nkrk * args.steps * ws / t_dev
 
     # the mixed-precision path on the configuration it is quoted on (24.6 M points, 6 blocks 640 x 200 x 32), with
@@ -402,10 +411,7 @@ def main():
             m1.record(sm)
             barrier()
             t_run = m0.elapsed_time(m1) / 1e3
-            if dist is not None:
-                tt = torch.tensor([t_run], device="cuda")
-                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-                t_run = float(tt.item())
+            t_run = max_over_ranks(t_run, dist)
             runs[name] = (cm, t_run)
         (cd, t_d), (cm, t_mix) = runs["fp64"], runs["mixed"]
         num = np.zeros(5)
@@ -472,10 +478,7 @@ def main():
         case.get_state_all(out=hnp)
     barrier()
     t_e2e = time.perf_counter() - t0
-    if dist is not None:
-        tt = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = max_over_ranks(t_e2e, dist)
     bytes_state = 5 * npts * 8
     e2e = {"value": npts * cfg.nkrk * args.e2e_steps * ws / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": bytes_state, "d2h_bytes_per_step": bytes_state, "steps": args.e2e_steps}
