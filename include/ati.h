@@ -303,6 +303,18 @@ int ati_tiles(ati_handle_t *h, int32_t out[4]);
  * 256 in [256, 4096].  Waits for the steps in flight and re-captures the step
  * graphs at the next step. */
 int ati_set_tiles(ati_handle_t *h, const int32_t in[4]);
+/* The whole tile choice of a handle, to reuse it on a handle of the same
+ * block shapes without timing candidates again (a host that starts many
+ * similar cases; results do not depend on tiles): plan[0..3] as ati_tiles,
+ * plan[4 + k] the points per tile of pointwise kernel k (0: the shared queue
+ * of plan[3]; otherwise one of the sizes ati_init times).  ati_set_tuning(h, 0)
+ * before ati_init skips the timing (the handle then runs on the default tiles
+ * until ati_set_tile_plan); ati_set_tile_plan waits for the steps in flight and
+ * re-captures the step graphs at the next step. */
+#define ATI_TILE_PLAN 11
+int ati_set_tuning(ati_handle_t *h, int enable);
+int ati_get_tile_plan(ati_handle_t *h, int32_t plan[ATI_TILE_PLAN]);
+int ati_set_tile_plan(ati_handle_t *h, const int32_t plan[ATI_TILE_PLAN]);
 /* Kernel options (no counterpart in the reference; results do not depend on
  * them, only timings do).  ATI_OPT_TMA, ATI_OPT_PAIRED_LINES and
  * ATI_OPT_STRESS_AT_POINT are on by default, ATI_OPT_FUSED_FACES off

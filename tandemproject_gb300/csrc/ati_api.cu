@@ -59,6 +59,7 @@ struct ati_handle {
   bool any_cfl = false;  // some case takes its dt from the CFL condition (dto < 0)
   bool tma[4] = {false, false, false, false};  // tensor maps exist for the mixed path's eta/zeta sweeps
   std::vector<TmaMap> htmaps;                   // host copy of the tensor maps (kept for the upload)
+  bool tune = true;                             // time tile candidates at ati_init (ati_set_tuning)
   bool fused = false;                           // fused face chains (ati_set_options)
   bool fp64_at_point = true;                    // FP64 viscous fluxes with the stresses at the point (ati_set_options)
   unsigned spin_limit = 1u << 24;               // polls a device barrier wait may take (ati_set_spin_limit)
@@ -1419,6 +1420,35 @@ extern "C" int ati_set_tiles(ati_handle_t *h, const int32_t in[4]) {
   return ATI_OK;
 }
 
+extern "C" int ati_set_tuning(ati_handle_t *h, int enable) {
+  if (!h) return fail(h, ATI_EINVAL, "null handle");
+  h->tune = enable != 0;
+  return ATI_OK;
+}
+
+static_assert(ATI_TILE_PLAN == 4 + PW_KINDS, "a tile plan: the four shapes of ati_tiles, then one entry per pointwise kind");
+extern "C" int ati_get_tile_plan(ati_handle_t *h, int32_t plan[ATI_TILE_PLAN]) {
+  if (!h || !plan) return fail(h, ATI_EINVAL, "ati_get_tile_plan: bad argument");
+  if (int rc = ati_tiles(h, plan)) return rc;
+  for (int k = 0; k < PW_KINDS; k++) plan[4 + k] = h->pw_pt[k];
+  return ATI_OK;
+}
+
+extern "C" int ati_set_tile_plan(ati_handle_t *h, const int32_t plan[ATI_TILE_PLAN]) {
+  if (!h || !plan) return fail(h, ATI_EINVAL, "ati_set_tile_plan: bad argument");
+  if (!h->inited) return fail(h, ATI_ESTATE, "ati_set_tile_plan: handle not initialised");
+  for (int k = 0; k < PW_KINDS; k++) {
+    const int v = plan[4 + k];
+    if (v != 0 && v != PT_CAND[0] && v != PT_CAND[1] && v != PT_CAND[2])
+      return fail(h, ATI_EINVAL, "ati_set_tile_plan: a pointwise kernel's tile must be 0 or one of the timed sizes");
+  }
+  if (int rc = ati_set_tiles(h, plan)) return rc;  // (validates and applies the shapes; pins the shared queue)
+  for (int k = 0; k < PW_KINDS; k++) h->pw_pt[k] = plan[4 + k];
+  apply_pw_tiles(h);
+  h->pt_points = plan[3];
+  return ATI_OK;
+}
+
 extern "C" int ati_set_options(ati_handle_t *h, int flags, int32_t *active) {
   if (!h) return fail(h, ATI_EINVAL, "null handle");
   if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES | ATI_OPT_PAIRED_LINES | ATI_OPT_STRESS_AT_POINT))
@@ -1650,7 +1680,8 @@ extern "C" int ati_init(ati_handle_t *h) {
   strict::scalar(c, h->st, SC_INIT, 0);
   CKL();
   CK(cudaStreamSynchronize(h->st));
-  if (int rc = autotune(h)) return rc;
+  if (h->tune)
+    if (int rc = autotune(h)) return rc;
   h->n_host = 0;
   h->steps_done = 0;
   h->inited = true;

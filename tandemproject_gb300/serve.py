@@ -26,16 +26,28 @@ from .workloads import fold_free_case, footprint_bytes, relax, serving_requests,
 ATI_ENONFINITE = 4
 
 
-def _gpu_case(cfg, grid):
+def _gpu_case(cfg, grid, plan=None):
+    """A case set up on the GPU; with a tile plan of an earlier case of the same block shapes, ati_init does not time
+    tile candidates again (results do not depend on tiles)."""
     from .solver import Case
     c = Case(cfg)
+    if plan is not None:
+        c.set_tuning(False)
     for mb in range(cfg.nblocks):
         c.set_grid(mb, grid[mb])
     c.init()
     if c.folded_blocks():  # the grid folds under the compact metrics: take a relaxed grid of the same size
         c.close()
         _, _, c = fold_free_case(relax(cfg))
+        plan = None
+    if plan is not None:
+        c.set_tile_plan(plan)
     return c
+
+
+def plan_key(cfg):
+    """Cases that share their tile plan: the same numerics and block shapes."""
+    return (cfg.precision, cfg.nviscous, cfg.les, tuple(cfg.lxibk), tuple(cfg.letbk), tuple(cfg.lzebk))
 
 
 class Server:
@@ -50,6 +62,8 @@ class Server:
         self.footprint = footprint
         self.peak_bytes = 0
         self.bound = False  # some request waited for memory (admission held it back)
+        self.plans = {}     # tile plans by plan_key: a case of known shapes skips the tile timing at set-up
+        self.plan_hits = 0
 
     def run(self, requests, log=None):
         """Serve the requests (arrival times in seconds from the start);
@@ -59,7 +73,9 @@ class Server:
         built from arrival on (prefetch pool), and an admitted case is created
         and initialised (device arrays, metrics, tile timing) on a set-up
         thread while the loop keeps issuing steps to the running cases.  Its
-        memory counts against the budget from admission on."""
+        memory counts against the budget from admission on.  The tile timing
+        runs once per block shape: later cases of the same shapes reuse its
+        plan (plan_key)."""
         pending = sorted(requests, key=lambda r: r.arrival)
         waiting, starting, active, done, failed = [], [], [], [], []
         used = 0
@@ -71,7 +87,16 @@ class Server:
 
         def create(r):
             cfg, grid = grids.pop(r.rid).result()
-            return cfg, self.make_case(cfg, grid)
+            key = plan_key(cfg)
+            plan = self.plans.get(key)
+            if plan is None:
+                c = self.make_case(cfg, grid)
+                if hasattr(c, "tile_plan"):
+                    self.plans[key] = c.tile_plan()
+            else:
+                c = self.make_case(cfg, grid, plan=plan)
+                self.plan_hits += 1
+            return cfg, c
 
         while pending or waiting or starting or active:
             t = now()
@@ -158,6 +183,7 @@ class Server:
                    "admission_wait_s": {"p50": float(np.percentile(wait, 50)), "max": float(wait.max())},
                    "admission_bound": self.bound,
                    "updates_per_s": work / makespan, "peak_resident_gib": self.peak_bytes / 2**30,
+                   "tile_plans_reused": self.plan_hits,
                    "failed": len(failed),
                    "failed_requests": [{k: f[k] for k in ("id", "points", "steps", "steps_run", "params")}
                                        for f in failed]}

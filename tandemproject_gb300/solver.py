@@ -28,6 +28,7 @@ ATI_OK, ATI_EINVAL, ATI_ENOMEM, ATI_ECUDA, ATI_ENONFINITE, ATI_ETIMEDOUT, ATI_ES
 F_QA, F_QO, F_DE, F_RR, F_SS, F_XIM, F_ETM, F_ZEM, F_P, F_YACO, F_STRESS, F_SPONGE, F_CP = range(13)
 FACE_DRVA, FACE_DRVB, FACE_RECV, FACE_CM = range(4)
 OPT_TMA, OPT_FUSED_FACES, OPT_TMA_ETA, OPT_TMA_ZETA, OPT_PAIRED_LINES, OPT_STRESS_AT_POINT = 1, 2, 4, 8, 16, 32
+TILE_PLAN = 11  # ATI_TILE_PLAN
 NCOMP = {F_QA: 5, F_QO: 5, F_DE: 5, F_RR: 3, F_SS: 3, F_XIM: 3, F_ETM: 3, F_ZEM: 3, F_P: 1, F_YACO: 1,
          F_STRESS: 9, F_SPONGE: 2, F_CP: 1}
 
@@ -77,6 +78,9 @@ SIGNATURES = {
     "ati_step_async": ([_vp, _i32], ctypes.c_int),
     "ati_jacobian_sign": ([_vp, _vp], ctypes.c_int),
     "ati_tiles": ([_vp, _vp], ctypes.c_int),
+    "ati_set_tuning": ([_vp, _i32], ctypes.c_int),
+    "ati_get_tile_plan": ([_vp, _vp], ctypes.c_int),
+    "ati_set_tile_plan": ([_vp, _vp], ctypes.c_int),
     "ati_set_tiles": ([_vp, _vp], ctypes.c_int),
     "ati_set_options": ([_vp, _i32, _vp], ctypes.c_int),
     "ati_set_spin_limit": ([_vp, ctypes.c_int64], ctypes.c_int),
@@ -282,6 +286,21 @@ class Case:
         """Pin the eta/zeta lines per CTA and points per tile (0 keeps the current one)."""
         t = (ctypes.c_int32 * 4)(0, eta, zeta, points)
         self._chk(self.L.ati_set_tiles(self.h, t))
+
+    def set_tuning(self, enable):
+        """Before init: time tile candidates at init (the default) or run on the default tiles."""
+        self._chk(self.L.ati_set_tuning(self.h, 1 if enable else 0))
+
+    def tile_plan(self):
+        """The handle's whole tile choice (ATI_TILE_PLAN entries), to reuse on a handle of the same shapes."""
+        t = (ctypes.c_int32 * TILE_PLAN)()
+        self._chk(self.L.ati_get_tile_plan(self.h, t))
+        return tuple(t)
+
+    def set_tile_plan(self, plan):
+        """Apply a tile plan taken from tile_plan() (results do not depend on it)."""
+        t = (ctypes.c_int32 * TILE_PLAN)(*plan)
+        self._chk(self.L.ati_set_tile_plan(self.h, t))
 
     def set_options(self, tma=True, fused_faces=False, paired_lines=True, stress_at_point=True):
         """Kernel options (results do not depend on them; the library's defaults): TMA staging of the mixed path's

@@ -100,3 +100,37 @@ def test_pinned_tiles_give_identical_states(ati_lib, precision):
         a.set_tiles(points=300)
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_tile_plan_reused_without_timing(ati_lib, precision):
+    """A handle set up without the tile timing (ati_set_tuning(h, 0)) takes an
+    earlier handle's whole tile plan, each pointwise kernel's size included,
+    and steps bit for bit as it does; a plan with a size that was not timed is
+    refused."""
+    from tandemproject_gb300.config import small_case
+    from tandemproject_gb300.grid import aerofoil_grid
+    from tandemproject_gb300.solver import AtiError, Case, setup_case
+    cfg = small_case(lxibk=(48, 120, 48), letbk=(39, 39), lzebk=(12,), precision=precision)
+    g = aerofoil_grid(cfg)
+    a = setup_case(cfg, grid=g)
+    plan = a.tile_plan()
+    assert len(plan) == 11 and plan[:4] == a.tiles()
+    assert all(v in (0, 256, 1024, 4096) for v in plan[4:])
+    b = Case(cfg)
+    b.set_tuning(False)
+    for mb in range(cfg.nblocks):
+        b.set_grid(mb, g[mb])
+    b.init()
+    b.set_tile_plan(plan)
+    assert b.tile_plan() == plan
+    a.step(6)
+    b.step(6)
+    for mb in range(cfg.nblocks):
+        np.testing.assert_array_equal(a.get_state(mb), b.get_state(mb))
+    bad = list(plan)
+    bad[4] = 512
+    with pytest.raises(AtiError):
+        b.set_tile_plan(bad)
+    a.close()
+    b.close()

@@ -116,3 +116,31 @@ def test_scheduler_retires_a_diverged_request_and_serves_the_rest():
     assert FakeCase.live == 0  # every case closed, the failed ones too
     for d in done:
         assert d["forces"][0] == d["steps"]
+
+
+class PlannedCase(FakeCase):
+    """A stand-in that records whether it was given an earlier case's tile plan."""
+    made = []
+
+    def __init__(self, cfg, grid, plan=None):
+        super().__init__(cfg, grid)
+        self.plan = plan
+        PlannedCase.made.append((cfg.lxibk, plan))
+
+    def tile_plan(self):
+        return ("plan", self.cfg.lxibk)
+
+
+def test_scheduler_reuses_tile_plans_per_block_shape():
+    from tandemproject_gb300.config import small_case
+    from tandemproject_gb300.serve import Server
+    shapes = [(24, 64, 24), (32, 64, 32), (24, 64, 24), (24, 64, 24), (32, 64, 32)]
+    reqs = [Request(i, small_case(lxibk=s), 10, 0.001 * i, {}) for i, s in enumerate(shapes)]
+    srv = Server(budget_bytes=100, chunk=5, make_case=PlannedCase, make_grid=lambda cfg: (cfg, None),
+                 footprint=lambda cfg: 10)
+    PlannedCase.made = []
+    done, summary = srv.run(reqs)
+    assert len(done) == 5 and summary["tile_plans_reused"] == 3
+    # the first case of each shape times its tiles; the later ones get its plan
+    assert PlannedCase.made == [((24, 64, 24), None), ((32, 64, 32), None), ((24, 64, 24), ("plan", (24, 64, 24))),
+                                ((24, 64, 24), ("plan", (24, 64, 24))), ((32, 64, 32), ("plan", (32, 64, 32)))]
