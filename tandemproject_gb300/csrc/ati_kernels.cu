@@ -1136,12 +1136,10 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_seg(SweepArgs<TI, 
 // ---------------------------------------------------------------------------
 // ADJ: the second half's line l lies SEG_LINES points after the first half's (zeta lines, and eta lines in row
 // tiles): its results are stored at a fixed offset from the first half's, through one walking pointer.
-template <int NN, bool FILT, bool TMA, bool ADJ, typename TI, typename TO>
-__global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI, TO, float> a, const float *rtab,
+template <int NN, bool TMA, bool ADJ>
+__global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<float, float, float> a, const float *rtab,
                                                                    int single) {
   static_assert(!ADJ || NN != 1, "adjacent halves: eta/zeta lines");
-  static_assert(!TMA || std::is_same<TI, float>::value, "TMA staging: FP32 inputs");
-  constexpr bool ASYNC = std::is_same<TI, float>::value;
   extern __shared__ __align__(16) unsigned char seg_smem[];
   constexpr int RS = TMA ? SEG_LINES : SEG_LINES + 1;
   __shared__ uint64_t tbar;
@@ -1173,13 +1171,7 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
   int jk0 = 0, jk1 = 0, Lg = 0;
   line_geom<NN>(B, T0 + lane, base0, sdum, jk0, Lg);
   line_geom<NN>(B, T0 + SEG_LINES + lane, base1, sdum, jk1, Lg);
-  const TI *in = a.io.in + f * a.io.in_fs;
-  const TI ofs = a.io.ofs[f];
-  // (inputs wider than FP32 lose their offset and are rounded on the way in)
-  auto stage = [&](float *dst, const TI *src) {
-    if constexpr (ASYNC) cp_async<4>(dst, src);
-    else *dst = cvt_in<TI, float>(__ldg(src), ofs);
-  };
+  const float *in = a.io.in + f * a.io.in_fs;
 
   // 1. stage both halves
   bool tma_ok = true;
@@ -1211,25 +1203,23 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
       float *tile = tiles + hh * HS;
       if constexpr (NN == 1) {
         // xi lines are contiguous: a warp copies one line at a time, lanes along the line
-        const TI *src0 = in + B.off + (int64_t)(T0 + hh * SEG_LINES) * L;
+        const float *src0 = in + B.off + (int64_t)(T0 + hh * SEG_LINES) * L;
         for (int ln = w; ln < nl; ln += nwarp) {
-          const TI *src = src0 + (int64_t)ln * L + lane;
+          const float *src = src0 + (int64_t)ln * L + lane;
           float *dst = tile + lane * RS + ln;
 #pragma unroll 4
-          for (int i = lane; i < L; i += 32, src += 32, dst += 32 * RS) stage(dst, src);
+          for (int i = lane; i < L; i += 32, src += 32, dst += 32 * RS) cp_async<4>(dst, src);
         }
       } else if (lane < nl) {
         // consecutive eta/zeta lines are consecutive points of a row: a warp copies one row at a time
-        const TI *src = in + (hh ? base1 : base0) + (int64_t)w * stride;
+        const float *src = in + (hh ? base1 : base0) + (int64_t)w * stride;
         float *dst = tile + w * RS + lane;
 #pragma unroll 4
-        for (int i = w; i < L; i += nwarp, src += nwarp * stride, dst += nwarp * RS) stage(dst, src);
+        for (int i = w; i < L; i += nwarp, src += nwarp * stride, dst += nwarp * RS) cp_async<4>(dst, src);
       }
     }
-    if constexpr (ASYNC) {
-      cp_async_commit();
-      cp_async_wait<0>();
-    }
+    cp_async_commit();
+    cp_async_wait<0>();
   }
   __syncthreads();
 
@@ -1242,11 +1232,9 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
   const float *rt = rtab + (int64_t)B.fac_off[NN] * SEG_RT;
   auto row = [&](int i) { return rt + i * SEG_RT; };
   const Coef<float> &C = *a.cf;
-  const float k1 = FILT ? C.fa : C.aa, k2 = FILT ? C.fb : C.ab, k3 = FILT ? C.fc : C.ac;
+  const float k1 = C.aa, k2 = C.ab, k3 = C.ac;
   auto rhs = [&](float x0, float x1, float x2, float x3, float x4, float x5, float x6) {
-    if (!FILT) return k1 * (x4 - x2) + k2 * (x5 - x1) + k3 * (x6 - x0);
-    const float r = 2.f * x3;
-    return k1 * (x2 + x4 - r) + k2 * (x1 + x5 - r) + k3 * (x0 + x6 - r);
+    return k1 * (x4 - x2) + k2 * (x5 - x1) + k3 * (x6 - x0);
   };
   const int ilo = max(s0, 3), ihi = min(s1, L - 3);
   // 2. what a segment reads outside its own rows, before any row is overwritten (per half, as in k_sweep_seg)
@@ -1261,8 +1249,6 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
       if ((hh == 0 || act1) && (w == 0 || w == S - 1)) {
         const int jk = hh ? jk1 : jk0;
         const float *rcv = a.recv + f * a.recv_fs + B.face_off[NN] * 6;
-        // (a derivative closes a face periodic onto its own block from the staged line, as k_sweep_seg does; the
-        // filter's closures come from recv)
         auto closure = [&](int r0, int dir, float *o) {
           float c0 = 0, c1 = 0, sap0 = 0;
           for (int i = 0; i <= LMD; i++) {
@@ -1276,11 +1262,11 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
         float rl[6];
         for (int ip = 0; ip <= 1; ip++) {
           if (B.ndf[ip][NN] != 1) continue;
-          if (!FILT && B.nbc[ip][NN] == 45 && B.ncd[ip][NN] == LT.b) closure(ip == 0 ? L - 2 : 1, ip == 0 ? -1 : 1, rl + 3 * ip);
+          if (B.nbc[ip][NN] == 45 && B.ncd[ip][NN] == LT.b) closure(ip == 0 ? L - 2 : 1, ip == 0 ? -1 : 1, rl + 3 * ip);
           else for (int q = 0; q < 3; q++) rl[3 * ip + q] = rcv[jk + nbs * (3 * ip + q)];
         }
-        line_ends<FILT, float>(C, L, B.ndf[0][NN], B.ndf[1][NN], rl, 1, 0, sld, sbs0[hh], sbs1[hh], sbs2[hh],
-                               sbe0[hh], sbe1[hh], sbe2[hh]);
+        line_ends<false, float>(C, L, B.ndf[0][NN], B.ndf[1][NN], rl, 1, 0, sld, sbs0[hh], sbs1[hh], sbs2[hh],
+                                sbe0[hh], sbe1[hh], sbe2[hh]);
       }
       if (ilo < ihi) {
         a0[hh] = sld(ilo - 3); a1[hh] = sld(ilo - 2); a2[hh] = sld(ilo - 1);
@@ -1380,15 +1366,8 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
     }
     __syncthreads();
   }
-  TO *out = a.io.out + f * a.io.out_fs;
-  TO *out2 = FILT && a.io.out2 ? a.io.out2 + f * a.io.out_fs : nullptr;  // (a derivative has one output)
-  float *drv = (!FILT && a.io.drva) ? a.drva + B.face_off[NN] * 10 : nullptr;
-  // a result: the derivative itself, or the filter's correction added to its input (rr = rr + sb,
-  // src/Subroutines3D.f90:200-202), read before the store of the same point
-  auto res = [](float v, const TI *qi) -> TO {
-    if constexpr (FILT) return (TO)(*qi + cvt<TI>(v));
-    else return (TO)v;
-  };
+  float *out = a.io.out + f * a.io.out_fs;
+  float *drv = a.io.drva ? a.drva + B.face_off[NN] * 10 : nullptr;
   const int m = a.io.m0 + f;
   // 5. the segment's forward values, then its back substitution from zero values beyond its end; with one
   // segment that gives the results, which eta/zeta lines write straight to DRAM (a warp writes a row)
@@ -1399,9 +1378,7 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
     int i = s1 - 1;
     float *pc = col + i * RS;
     const float *tr = row(i);
-    TO *po0 = out + base0 + (int64_t)i * stride, *po1 = out + base1 + (int64_t)i * stride;
-    TO *pp0 = out2 ? out2 + base0 + (int64_t)i * stride : nullptr, *pp1 = out2 ? out2 + base1 + (int64_t)i * stride : nullptr;
-    const TI *pi0 = in + base0 + (int64_t)i * stride, *pi1 = in + base1 + (int64_t)i * stride;
+    float *po0 = out + base0 + (int64_t)i * stride, *po1 = out + base1 + (int64_t)i * stride;
     auto sweep = [&](auto direct) {
       constexpr bool D = decltype(direct)::value;
       auto l4 = [](const float *t) { return __ldg(reinterpret_cast<const float4 *>(t + 4)); };
@@ -1414,26 +1391,14 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
           q[hh] = g.z * v - g.w * q1[hh] - c4 * q2[hh];
         }
         if constexpr (D) {
-          const TO r0 = res(q[0], pi0);
-          *po0 = r0;
-          if (FILT && out2) *pp0 = r0;
+          *po0 = q[0];
           if constexpr (ADJ) {
-            if (act1) {
-              const TO r1 = res(q[1], pi0 + SEG_LINES);
-              po0[SEG_LINES] = r1;
-              if (FILT && out2) pp0[SEG_LINES] = r1;
-            }
+            if (act1) po0[SEG_LINES] = q[1];
           } else {
-            if (act1) {
-              const TO r1 = res(q[1], pi1);
-              *po1 = r1;
-              if (FILT && out2) *pp1 = r1;
-            }
+            if (act1) *po1 = q[1];
             po1 -= stride;
-            if (FILT) { pp1 -= stride; pi1 -= stride; }
           }
           po0 -= stride;
-          if (FILT) { pp0 -= stride; pi0 -= stride; }
         } else {
           c[0] = q[0];
           c[HS] = q[1];
@@ -1547,31 +1512,16 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
         }
       } else {
         // walking output pointers: one 64-bit add per row and half
-        TO *po0 = out + base0 + (int64_t)i * stride, *po1 = out + base1 + (int64_t)i * stride;
-        TO *pp0 = out2 ? out2 + base0 + (int64_t)i * stride : nullptr;
-        TO *pp1 = out2 ? out2 + base1 + (int64_t)i * stride : nullptr;
-        const TI *pi0 = in + base0 + (int64_t)i * stride, *pi1 = in + base1 + (int64_t)i * stride;
+        float *po0 = out + base0 + (int64_t)i * stride, *po1 = out + base1 + (int64_t)i * stride;
         auto put = [&](const float r[2]) {
-          const TO r0 = res(r[0], pi0);
-          *po0 = r0;
-          if (FILT && out2) *pp0 = r0;
+          *po0 = r[0];
           if constexpr (ADJ) {
-            if (act1) {
-              const TO r1 = res(r[1], pi0 + SEG_LINES);
-              po0[SEG_LINES] = r1;
-              if (FILT && out2) pp0[SEG_LINES] = r1;
-            }
+            if (act1) po0[SEG_LINES] = r[1];
           } else {
-            if (act1) {
-              const TO r1 = res(r[1], pi1);
-              *po1 = r1;
-              if (FILT && out2) *pp1 = r1;
-            }
+            if (act1) *po1 = r[1];
             po1 += stride;
-            if (FILT) { pp1 += stride; pi1 += stride; }
           }
           po0 += stride;
-          if (FILT) { pp0 += stride; pi0 += stride; }
         };
         for (; i + 3 < s1; i += 4, pc += 4 * RS, tr += 4 * SEG_RT) {
           const float2 n0 = l2(tr + 4 * SEG_RT), n1 = l2(tr + 5 * SEG_RT), n2 = l2(tr + 6 * SEG_RT);
@@ -1600,23 +1550,13 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<TI,
       for (int ln = w; ln < nl; ln += nwarp) {
         const int64_t lb = o0 + (int64_t)ln * L;
         int i = lane;
-        auto wr = [&](int64_t p, float v, TI qin) {
-          TO r;
-          if (FILT) r = (TO)(qin + cvt<TI>(v));  // rr = rr + sb (src/Subroutines3D.f90:200-202)
-          else r = (TO)v;
-          out[p] = r;
-          if (out2) out2[p] = r;
-        };
-        // four points a pass, their inputs read before any of them is stored (the filter runs in place)
         for (; i + 96 < L; i += 128) {
-          TI q0 = 0, q1 = 0, q2 = 0, q3 = 0;
-          if (FILT) { q0 = in[lb + i]; q1 = in[lb + i + 32]; q2 = in[lb + i + 64]; q3 = in[lb + i + 96]; }
-          wr(lb + i, tile[i * RS + ln], q0);
-          wr(lb + i + 32, tile[(i + 32) * RS + ln], q1);
-          wr(lb + i + 64, tile[(i + 64) * RS + ln], q2);
-          wr(lb + i + 96, tile[(i + 96) * RS + ln], q3);
+          out[lb + i] = tile[i * RS + ln];
+          out[lb + i + 32] = tile[(i + 32) * RS + ln];
+          out[lb + i + 64] = tile[(i + 64) * RS + ln];
+          out[lb + i + 96] = tile[(i + 96) * RS + ln];
         }
-        for (; i < L; i += 32) wr(lb + i, tile[i * RS + ln], FILT ? in[lb + i] : (TI)0);
+        for (; i < L; i += 32) out[lb + i] = tile[i * RS + ln];
       }
     }
   }
@@ -2994,40 +2934,32 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
         const size_t smem = seg_smem_bytes(C.maxlen, G);
         const dim3 g(C.n, io.nf);
 #define ATI_SEG(D, F) k_sweep_seg<D, F, false, TI, TO><<<g, nt, smem, st>>>(a, seg, G)
-        // eta/zeta derivative sweeps of an array with tensor maps: tiles staged by TMA
-        int arr = -1;
-        if constexpr (std::is_same<TI, float>::value)
-          arr = io.in == e.prim ? 0 : (io.in == e.flx + (int64_t)(nn - 1) * e.N ? 1 : -1);
-        const bool tma = !filt && nn >= 2 && e.tma[nn] && arr >= 0;
-        // paired lines: a CTA solves two groups of lines, lane l line l of each (lines of up to PAIR_MAX_SEG
-        // segments: longer ones would halve the CTAs an SM holds, measured slower): the derivatives of the FP32
-        // arrays and the filter of the FP64 state
-        constexpr bool PF = std::is_same<TI, float>::value && std::is_same<TO, float>::value;
-        constexpr bool PD = std::is_same<TI, double>::value && std::is_same<TO, double>::value;
-        if constexpr (PF || PD) {
+        if constexpr (std::is_same<TI, float>::value) {
+          // eta/zeta derivative sweeps of an array with tensor maps: tiles staged by TMA
+          const int arr = io.in == e.prim ? 0 : (io.in == e.flx + (int64_t)(nn - 1) * e.N ? 1 : -1);
+          const bool tma = !filt && nn >= 2 && e.tma[nn] && arr >= 0;
+          // paired lines: a CTA solves two groups of lines, lane l line l of each (lines of up to PAIR_MAX_SEG
+          // segments: longer ones would halve the CTAs an SM holds, measured slower)
           const size_t psm = pair_smem_bytes(C.maxlen, G > 1) + 128;
-          if ((PF ? !filt : filt) && e.pairs && seg_count(C.maxlen) <= PAIR_MAX_SEG && psm <= SEG_SMEM_MAX) {
+          if (!filt && e.pairs && seg_count(C.maxlen) <= PAIR_MAX_SEG && psm <= SEG_SMEM_MAX) {
             const int single = G > 1 ? 1 : 0;
             const dim3 gp(single ? C.n : C.n / 2, io.nf);
             const int ntp = SEG_LINES * (single ? 1 : seg_count(C.maxlen));
             const bool adj = nn == 3 || (nn == 2 && e.eta_rowtiles);
-            constexpr bool F = PD;
             if (tma) a.tmap = e.tmaps + (int64_t)(arr * 2 + nn - 2) * e.nblk;
-#define ATI_PAIR(D, T, J) k_sweep_pair<D, F, T, J, TI, TO><<<gp, ntp, psm, st>>>(a, seg, single)
+#define ATI_PAIR(D, T, J) k_sweep_pair<D, T, J><<<gp, ntp, psm, st>>>(a, seg, single)
             if (nn == 1) ATI_PAIR(1, false, false);
             else if (nn == 2) {
-              if (!F && tma) ATI_PAIR(2, !F, true);
+              if (tma) ATI_PAIR(2, true, true);
               else if (adj) ATI_PAIR(2, false, true);
               else ATI_PAIR(2, false, false);
             } else {
-              if (!F && tma) ATI_PAIR(3, !F, true);
+              if (tma) ATI_PAIR(3, true, true);
               else ATI_PAIR(3, false, true);
             }
 #undef ATI_PAIR
             continue;
           }
-        }
-        if constexpr (std::is_same<TI, float>::value) {
           if (tma) {
             a.tmap = e.tmaps + (int64_t)(arr * 2 + nn - 2) * e.nblk;
             const size_t sm = smem + 128;  // (alignment of the tensor copies' destination)
@@ -3090,19 +3022,12 @@ static cudaError_t seg_attr() {
   if constexpr (std::is_same<TI, float>::value) {
     if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<2, false, true, TI, TO>);
     if (e == cudaSuccess) e = seg_attr_one(k_sweep_seg<3, false, true, TI, TO>);
-  }
-  constexpr bool PF = std::is_same<TI, float>::value && std::is_same<TO, float>::value;
-  constexpr bool PD = std::is_same<TI, double>::value && std::is_same<TO, double>::value;
-  if constexpr (PF || PD) {  // the paired kernels: derivatives of FP32 arrays (TMA too), the filter of the FP64 state
-    constexpr bool F = PD;
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<1, F, false, false, TI, TO>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, F, false, false, TI, TO>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, F, false, true, TI, TO>);
-    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, F, false, true, TI, TO>);
-    if constexpr (!F) {
-      if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, F, true, true, TI, TO>);
-      if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, F, true, true, TI, TO>);
-    }
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<1, false, false>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, false, false>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, false, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, false, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<2, true, true>);
+    if (e == cudaSuccess) e = seg_attr_one(k_sweep_pair<3, true, true>);
   }
   return e;
 }
