@@ -316,9 +316,10 @@ int ati_set_tuning(ati_handle_t *h, int enable);
 int ati_get_tile_plan(ati_handle_t *h, int32_t plan[ATI_TILE_PLAN]);
 int ati_set_tile_plan(ati_handle_t *h, const int32_t plan[ATI_TILE_PLAN]);
 /* Kernel options (no counterpart in the reference; results do not depend on
- * them, only timings do).  ATI_OPT_TMA, ATI_OPT_PAIRED_LINES and
- * ATI_OPT_STRESS_AT_POINT are on by default, ATI_OPT_FUSED_FACES off
- * (measured slower inside the step graphs).
+ * them, only timings do, except ATI_OPT_DENSE_ZETA's by FP32 rounding).
+ * ATI_OPT_TMA, ATI_OPT_PAIRED_LINES and ATI_OPT_STRESS_AT_POINT are on by
+ * default, ATI_OPT_FUSED_FACES (measured slower inside the step graphs) and
+ * ATI_OPT_DENSE_ZETA off.
  *  ATI_OPT_TMA: the mixed path's segmented eta and zeta derivative sweeps
  *    stage each tile of 32 lines into shared memory with one tensor copy
  *    (TMA, cp.async.bulk.tensor) on every direction whose blocks' FP32 planes
@@ -332,6 +333,11 @@ int ati_set_tile_plan(ati_handle_t *h, const int32_t plan[ATI_TILE_PLAN]);
  *  ATI_OPT_PAIRED_LINES: the mixed path's segmented derivative sweeps solve
  *    two groups of 32 lines per CTA, each lane two lines, on lines of up to
  *    four segments (192 points; longer ones one group per CTA).
+ *  ATI_OPT_DENSE_ZETA (off by default; its results differ from the
+ *    recurrence's by FP32 rounding): the mixed path's zeta derivatives as
+ *    one dense L x L product per line, the operator of each block built once
+ *    from the line algorithm in FP64, where every zeta face is periodic onto
+ *    its own block and lines have 13 to 64 points (else it has no effect).
  *  ATI_OPT_STRESS_AT_POINT: the ATI_FP64 path's viscous fluxes take the
  *    stresses at the point inside the flux kernel instead of writing and
  *    reading nine stress planes (no effect in the strict mode, the mixed path
@@ -346,6 +352,7 @@ int ati_set_tile_plan(ati_handle_t *h, const int32_t plan[ATI_TILE_PLAN]);
 #define ATI_OPT_TMA_ZETA 8
 #define ATI_OPT_PAIRED_LINES 16
 #define ATI_OPT_STRESS_AT_POINT 32
+#define ATI_OPT_DENSE_ZETA 64
 int ati_set_options(ati_handle_t *h, int flags, int32_t *active);
 /* Device-side waits are bounded (no counterpart in the reference): a grid
  * barrier of the fused face chains gives up after this many polls (0 = the

@@ -8,7 +8,7 @@ case, for every output the solver produces:
   wall PSD      power spectral density of the wall-pressure time series
                 recorded every step (no counterpart in the reference)
 
-    python -m tandemproject_gb300.accuracy --preset naca0012_25m --steps 1000
+    python -m tandemproject_gb300.accuracy --preset naca0012_25m --steps 1000 [--dense-zeta]
 
 Both runs start from the same grid and initial state and take the same steps;
 the FP64 path itself matches the CPU restatement of the reference to ~1e-14.
@@ -44,7 +44,7 @@ def wall_psd(t, p):
     return freq, spec.mean(axis=1) * dtu / (w ** 2).sum()
 
 
-def compare(cfg, steps, probe=True, log=print):
+def compare(cfg, steps, probe=True, log=print, dense_zeta=False):
     from .config import FP64, MIXED
     from .grid import aerofoil_grid
     from .solver import setup_case
@@ -53,6 +53,8 @@ def compare(cfg, steps, probe=True, log=print):
     runs = {}
     for name, prec in (("fp64", FP64), ("mixed", MIXED)):
         c = setup_case(cfg.replace(precision=prec), grid=grid)
+        if dense_zeta and prec == MIXED:
+            out["dense_zeta"] = c.set_options(dense_zeta=True)["dense_zeta"]
         if probe:
             c.wall_probe(steps)
         t0 = time.time()
@@ -97,11 +99,12 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--nsmf", type=int, default=None, help="override the start (0 = the reference deck's ramp)")
     ap.add_argument("--timf", type=float, default=None)
+    ap.add_argument("--dense-zeta", action="store_true", help="the mixed run's zeta derivatives as dense products")
     args = ap.parse_args()
     cfg = PRESETS[args.preset]
     kw = {k: v for k, v in (("nsmf", args.nsmf), ("timf", args.timf)) if v is not None}
     cfg = cfg.replace(**kw)
-    res = compare(cfg, args.steps)
+    res = compare(cfg, args.steps, dense_zeta=args.dense_zeta)
     res["preset"] = args.preset
     res["nsmf"], res["timf"] = cfg.nsmf, cfg.timf
     print(json.dumps(res))

@@ -809,6 +809,72 @@ static void seg_tables(const ati_handle *h, const std::vector<double> &fac, std:
   }
 }
 
+// Dense zeta derivative operators of the mixed path (k_sweep_dense): on a block whose two zeta faces are periodic
+// onto the block itself, the derivative of a zeta line is a fixed linear map d = M f of the line's L values: the
+// closure values of the line ends are sums over the other end of the same line (k_mpigo's closure, taken inside the
+// sweep), the end rows those of deriv's closures (line_ends), the interior rows the compact right-hand side, then
+// the LU solve (src/Subroutines3D.f90:84-141).  Column j of M is that algorithm applied in FP64 to the unit line
+// e_j; M is stored rounded to FP32, row-major in DENSE_MAX x DENSE_MAX storage per block.  Returns the largest
+// line length, or 0 if some block's zeta lines do not qualify (a face of another kind, lines outside
+// LMD + 2..DENSE_MAX).
+static int dense_zeta(const ati_handle *h, const std::vector<double> &fac, std::vector<float> &out) {
+  const Scheme &S = h->sh.s;
+  int lmax = 0;
+  for (int gb = 0; gb < h->nb; gb++) {
+    const BlockDev &B = h->blk[gb];
+    const int L = B.lze + 1;
+    for (int ip = 0; ip <= 1; ip++)
+      if (B.ndf[ip][3] != 1 || B.nbc[ip][3] != 45 || B.ncd[ip][3] != gb) return 0;
+    if (L < LMD + 2 || L > DENSE_MAX) return 0;  // the closure sums reach LMD + 1 points in from the far end
+    lmax = std::max(lmax, L);
+  }
+  out.assign((size_t)h->nb * DENSE_MAX * DENSE_MAX, 0.f);
+  std::vector<double> f(DENSE_MAX), r(DENSE_MAX), v(DENSE_MAX), b(DENSE_MAX + 2);
+  for (int gb = 0; gb < h->nb; gb++) {
+    const BlockDev &B = h->blk[gb];
+    const int L = B.lze + 1;
+    const double *fc = &fac[(size_t)B.fac_off[3] * 5];
+    for (int j = 0; j < L; j++) {
+      std::fill(f.begin(), f.end(), 0.0);
+      f[j] = 1.0;
+      double rl[6];
+      auto closure = [&](int r0, int dir, double *o) {  // the sums k_mpigo forms for the periodic face
+        double c0 = 0, c1 = 0;
+        for (int i = 0; i <= LMD; i++) {
+          c0 += S.pbco[0][0][i] * f[r0 + i * dir];
+          c1 += S.pbco[0][1][i] * f[r0 + i * dir];
+        }
+        o[0] = c0; o[1] = c1; o[2] = f[r0];
+      };
+      closure(L - 2, -1, rl);
+      closure(1, 1, rl + 3);
+      double s0 = 0, s1 = 0, e0 = 0, e1 = 0;
+      for (int q = 0; q <= LMD; q++) {
+        s0 += S.pbci[0][0][q] * f[q];
+        s1 += S.pbci[0][1][q] * f[q];
+        e0 += S.pbci[0][0][q] * f[L - 1 - q];
+        e1 += S.pbci[0][1][q] * f[L - 1 - q];
+      }
+      r[0] = s0 + rl[0];
+      r[1] = s1 + rl[1];
+      r[2] = S.aa * (f[3] - f[1]) + S.ab * (f[4] - f[0]) + S.ac * (f[5] - rl[2]);
+      for (int i = 3; i < L - 3; i++)
+        r[i] = S.aa * (f[i + 1] - f[i - 1]) + S.ab * (f[i + 2] - f[i - 2]) + S.ac * (f[i + 3] - f[i - 3]);
+      r[L - 3] = S.aa * (f[L - 2] - f[L - 4]) + S.ab * (f[L - 1] - f[L - 5]) + S.ac * (rl[5] - f[L - 6]);
+      r[L - 2] = -e1 - rl[4];
+      r[L - 1] = -e0 - rl[3];
+      for (int i = 0; i < L; i++)
+        v[i] = r[i] - (i >= 2 ? fc[i * 5 + 0] * v[i - 2] : 0.0) - (i >= 1 ? fc[i * 5 + 1] * v[i - 1] : 0.0);
+      b[L] = b[L + 1] = 0.0;
+      for (int i = L - 1; i >= 0; i--)
+        b[i] = fc[i * 5 + 2] * v[i] - (i <= L - 2 ? fc[i * 5 + 3] * b[i + 1] : 0.0) -
+               (i <= L - 3 ? fc[i * 5 + 4] * b[i + 2] : 0.0);
+      for (int i = 0; i < L; i++) out[((size_t)gb * DENSE_MAX + i) * DENSE_MAX + j] = (float)b[i];
+    }
+  }
+  return lmax;
+}
+
 // Scaled-factor row tables of the FP64 fast path's line solves (solve_line_u,
 // layout at FU_RT): forward factors rescaled to carry u = c2 v, the stencil
 // weights k1..k3 times c2, the back-substitution factors with the entries past
@@ -938,7 +1004,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
                o_facud = take((size_t)h->nfac * FU_RT * D8), o_facuf = take((size_t)h->nfac * FU_RT * D8);
   // FP32 set (mixed): de(5) prim(4) mu p(1) dv(12) tau(9) flx(15) fw(3 x 5) xim etm zem(3) yaco asz bsz(1) gm(3)
   size_t o_ff = 0, o_fdrva = 0, o_fdrvb = 0, o_frecv = 0, o_fcm = 0, o_ffacd = 0, o_ffacf = 0, o_fsbcc = 0,
-         o_frpex = 0, o_cff = 0, o_fdrvm = 0, o_lts[4] = {0, 0, 0, 0}, o_segd = 0, o_segf = 0, o_tmap = 0;
+         o_frpex = 0, o_cff = 0, o_fdrvm = 0, o_lts[4] = {0, 0, 0, 0}, o_segd = 0, o_segf = 0, o_tmap = 0, o_dzm = 0;
   const int np32 = 5 + 4 + 1 + 1 + 12 + 9 + 15 + 15 + 9 + 1 + 1 + 1 + 3;
   if (h->mixed) {
     o_ff = take((size_t)np32 * N * F4);
@@ -952,6 +1018,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     o_segd = take((size_t)(h->nfac + 2 * SEG_PAD) * SEG_RT * F4);
     o_segf = take((size_t)(h->nfac + 2 * SEG_PAD) * SEG_RT * F4);
     o_tmap = take(sizeof(TmaMap) * 4 * (size_t)h->nb);
+    o_dzm = take(sizeof(float) * DENSE_MAX * DENSE_MAX * (size_t)h->nb);
   }
   cudaError_t e = cudaMalloc(&h->arena, bytes);
   if (e != cudaSuccess) {
@@ -1017,6 +1084,8 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
       for (int c = 0; c < SEG_NCLASS; c++) m.segc[nn][c] = h->segc[nn][c];
     }
     m.segd = Fp(o_segd) + SEG_PAD * SEG_RT; m.segf = Fp(o_segf) + SEG_PAD * SEG_RT;
+    m.dzm = Fp(o_dzm);
+    m.dense = false;
     m.tmaps = (const TmaMap *)(h->arena + o_tmap);
     m.nblk = h->nb;
     for (int nn = 0; nn < 4; nn++) m.tma[nn] = h->tma[nn];
@@ -1053,10 +1122,11 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   const Coef<float> cff = make_coef<float>(h->sh.s);
   std::vector<Scheme> schemes;
   for (int c = 0; c < ncase; c++) schemes.push_back(h->shc[c].s);
-  std::vector<float> facd32(facd.begin(), facd.end()), facf32(facf.begin(), facf.end()), segd32, segf32;
+  std::vector<float> facd32(facd.begin(), facd.end()), facf32(facf.begin(), facf.end()), segd32, segf32, dzm32;
   if (h->mixed) {
     seg_tables(h, facd, segd32);
     seg_tables(h, facf, segf32);
+    h->ef.dzl = dense_zeta(h, facd, dzm32);
   }
   e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaStreamCreateWithFlags(&h->side[q], cudaStreamNonBlocking);
@@ -1092,6 +1162,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
     up(h->ef.facf, facf32.data(), facf32.size() * F4);
     up(h->ef.segd, segd32.data(), segd32.size() * F4);
     up(h->ef.segf, segf32.data(), segf32.size() * F4);
+    up(h->ef.dzm, dzm32.data(), dzm32.size() * F4);
     if (h->tma[2] || h->tma[3]) {
       if (encode_tmaps(h, h->htmaps) != ATI_OK) {
         if (e == cudaSuccess) e = cudaErrorInvalidValue;
@@ -1451,7 +1522,7 @@ extern "C" int ati_set_tile_plan(ati_handle_t *h, const int32_t plan[ATI_TILE_PL
 
 extern "C" int ati_set_options(ati_handle_t *h, int flags, int32_t *active) {
   if (!h) return fail(h, ATI_EINVAL, "null handle");
-  if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES | ATI_OPT_PAIRED_LINES | ATI_OPT_STRESS_AT_POINT))
+  if (flags & ~(ATI_OPT_TMA | ATI_OPT_FUSED_FACES | ATI_OPT_PAIRED_LINES | ATI_OPT_STRESS_AT_POINT | ATI_OPT_DENSE_ZETA))
     return fail(h, ATI_EINVAL, "ati_set_options: unknown flag");
   CK(cudaStreamSynchronize(h->st));
   drop_graphs(h);
@@ -1459,10 +1530,12 @@ extern "C" int ati_set_options(ati_handle_t *h, int flags, int32_t *active) {
   h->fused = (flags & ATI_OPT_FUSED_FACES) != 0;
   h->ef.pairs = (flags & ATI_OPT_PAIRED_LINES) != 0;
   h->fp64_at_point = (flags & ATI_OPT_STRESS_AT_POINT) != 0;
+  h->ef.dense = (flags & ATI_OPT_DENSE_ZETA) != 0 && h->ef.dzl > 0;
   if (active)
     *active = (h->ef.tma[2] || h->ef.tma[3] ? ATI_OPT_TMA : 0) | (h->fused ? ATI_OPT_FUSED_FACES : 0) |
               (h->ef.tma[2] ? ATI_OPT_TMA_ETA : 0) | (h->ef.tma[3] ? ATI_OPT_TMA_ZETA : 0) |
-              (h->ef.pairs ? ATI_OPT_PAIRED_LINES : 0) | (h->fp64_at_point ? ATI_OPT_STRESS_AT_POINT : 0);
+              (h->ef.pairs ? ATI_OPT_PAIRED_LINES : 0) | (h->fp64_at_point ? ATI_OPT_STRESS_AT_POINT : 0) |
+              (h->ef.dense ? ATI_OPT_DENSE_ZETA : 0);
   return ATI_OK;
 }
 

@@ -1567,6 +1567,96 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<flo
 }
 
 // ---------------------------------------------------------------------------
+// Dense zeta derivative (mixed path, FP32 inputs and outputs; blocks whose zeta faces are periodic onto the
+// block): d = M f for every zeta line, M the block's L x L operator built on the host from the line algorithm
+// itself (the periodic faces' closures, the end rows, the interior right-hand side and the LU solve, in FP64,
+// rounded once).  A CTA takes one tile of lines through every field, the operator staged in shared memory once; a
+// thread takes one line into registers less the line's first value (M's rows sum to zero, the derivative of a
+// constant being zero: a spanwise-uniform line keeps an exactly zero derivative, and the differences of a nearly
+// uniform one are exact), then forms four rows at a time, the matrix rows read from shared memory four entries a
+// load and broadcast to the warp: LM / 4 loads and LM / 2 packed FMAs (fma.rn.f32x2) a row and line, with no serial
+// chain across rows.  Lines of up to 32 points load the next field's line before the products of this one.  Lines
+// shorter than LM read zeros past their end.
+// ---------------------------------------------------------------------------
+template <int LM>
+__global__ void __launch_bounds__(256) k_sweep_dense(SweepArgs<float, float, float> a, const float *dzm) {
+  extern __shared__ __align__(16) float dmat[];  // LM rows of LM floats (rows past L uninitialised, never stored)
+  constexpr bool PF = LM <= 32;                   // the next field's line loaded during this one's products
+  const LTile LT = a.lt[blockIdx.x];
+  const BlockDev &B = a.blk[LT.b];
+  const int L = B.lze + 1;
+  const int64_t plane = (int64_t)(B.lxi + 1) * (B.let + 1);
+  const int64_t t = (int64_t)LT.t0 + threadIdx.x;
+  const bool live = t < plane;
+  const int nf = a.io.nf;
+  float g[LM], h[PF ? LM : 1];
+  auto load = [&](int f, float *v) {
+    const float *in = a.io.in + f * a.io.in_fs + B.off + t;
+#pragma unroll
+    for (int j = 0; j < LM; j++) v[j] = j < L ? in[(int64_t)j * plane] : 0.f;
+  };
+  if (live) load(0, g);  // the first field's loads in flight while the operator is staged
+  const float4 *src = reinterpret_cast<const float4 *>(dzm + (size_t)LT.b * DENSE_MAX * DENSE_MAX);
+  for (int q = threadIdx.x; q < L * (LM / 4); q += blockDim.x) {
+    const int i = q / (LM / 4), j4 = q - i * (LM / 4);
+    reinterpret_cast<float4 *>(dmat)[q] = src[i * (DENSE_MAX / 4) + j4];
+  }
+  __syncthreads();
+  if (!live) return;  // (no barrier below)
+  float *drv = a.io.drva ? a.drva + B.face_off[3] * 10 : nullptr;
+  const int64_t nbs = B.nbsize[3];
+  for (int f = 0; f < nf; f++) {
+    if (f > 0) {
+      if constexpr (PF) {
+#pragma unroll
+        for (int j = 0; j < LM; j++) g[j] = h[j];
+      } else {
+        load(f, g);
+      }
+    }
+    if constexpr (PF) {
+      if (f + 1 < nf) load(f + 1, h);
+    }
+    const float f0 = g[0];
+    float2 gp[LM / 2];
+#pragma unroll
+    for (int j = 0; j < LM; j++) g[j] = j < L ? g[j] - f0 : 0.f;
+#pragma unroll
+    for (int k = 0; k < LM / 2; k++) gp[k] = make_float2(g[2 * k], g[2 * k + 1]);
+    float *out = a.io.out + f * a.io.out_fs + B.off + t;
+    const int m = a.io.m0 + f;
+    for (int i = 0; i < L; i += 4) {
+      const float4 *row = reinterpret_cast<const float4 *>(dmat + i * LM);
+      // four partial sums a row: columns 4k, 4k+1 (ea) and 4k+2, 4k+3 (eb), each pair one packed FMA
+      float2 ea[4], eb[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) ea[u] = eb[u] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j4 = 0; j4 < LM / 4; j4++) {
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const float4 mv = row[u * (LM / 4) + j4];
+          ea[u] = __ffma2_rn(make_float2(mv.x, mv.y), gp[2 * j4], ea[u]);
+          eb[u] = __ffma2_rn(make_float2(mv.z, mv.w), gp[2 * j4 + 1], eb[u]);
+        }
+      }
+      float acc[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) acc[u] = (ea[u].x + ea[u].y) + (eb[u].x + eb[u].y);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int r = i + u;
+        if (r < L) {
+          out[(int64_t)r * plane] = acc[u];
+          if (drv && r == 0) drv[t + nbs * ((m - 1) + 5 * 0)] = acc[u];      // drva(jk,m,0) = sb(is)
+          if (drv && r == L - 1) drv[t + nbs * ((m - 1) + 5 * 1)] = acc[u];  // drva(jk,m,1) = sb(ie)
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // mpigo (src/Subroutines3D.f90:16-80): closure values of every face with
 // ndf = 1.  The thread of face (A, nn, ip), line jk, field f computes what the
 // neighbour B sends from its face 1-ip (the reference's tag pairing) and
@@ -2921,6 +3011,14 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
   a.scal = e.scal;
   a.rowtiles = false;
   if constexpr (std::is_same<TC, float>::value) {
+    if constexpr (std::is_same<TI, float>::value && std::is_same<TO, float>::value) {
+      // the zeta derivative by the blocks' dense operators (every zeta line periodic onto its block; k_sweep_dense)
+      if (nn == 3 && !filt && e.dense && e.dzl > 0 && !io.out2) {
+        if (e.dzl <= 32) k_sweep_dense<32><<<e.nlt[3], e.sg_lines[3], 32 * 32 * sizeof(float), st>>>(a, e.dzm);
+        else k_sweep_dense<64><<<e.nlt[3], e.sg_lines[3], 64 * 64 * sizeof(float), st>>>(a, e.dzm);
+        return;
+      }
+    }
     // the mixed path: segmented solves over tiles of SEG_LINES lines
     const float *seg = filt ? e.segf : e.segd;
     a.rowtiles = e.eta_rowtiles;

@@ -54,6 +54,9 @@ struct Eng {
   SegClass segc[4][SEG_NCLASS];
   int nsegc[4];
   const float *segd, *segf;  // their row tables (SEG_RT floats per factor row; derivative, filter)
+  const float *dzm;          // dense zeta derivative operators, DENSE_MAX^2 floats per block (k_sweep_dense)
+  int dzl;                   // their largest line length (0: the dense zeta sweep is not available)
+  bool dense;                // the zeta derivative sweeps take the dense operators (ATI_OPT_DENSE_ZETA)
   const double *facud, *facuf;  // FP64 fast path: scaled-factor row tables (FU_RT per row; derivative, filter)
   int sg_lines[4];      // lines per CTA of the eta (2) and zeta (3) sweeps: the tiles of lt[2], lt[3]
   int maxlen[4];        // longest line per direction
@@ -184,6 +187,9 @@ inline size_t seg_smem_bytes(int maxlen, int groups) {
   const int nwarp = groups > 1 ? groups : seg_count(maxlen);
   return (size_t)nwarp * SEG_LINES * 2 * 2 * sizeof(float) + (size_t)groups * maxlen * (SEG_LINES + 1) * sizeof(float);
 }
+// Dense zeta derivative sweeps (k_sweep_dense): lines of up to DENSE_MAX points, each block's operator an
+// L x L matrix in DENSE_MAX x DENSE_MAX storage
+constexpr int DENSE_MAX = 64;
 // Paired sweeps (k_sweep_pair) take the classes of lines of up to PAIR_MAX_SEG segments
 constexpr int PAIR_MAX_SEG = 4;
 // ... and of a paired sweep (k_sweep_pair: two line groups, one warp per segment, or one warp when single)

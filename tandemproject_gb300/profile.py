@@ -7,10 +7,11 @@ times through the graph (wall clock around the steps: the graph-timed step),
 then `--steps` times with the events; the table gives per class the time per
 launch, the launches and the share of the profiled time.  `--fused` switches
 the fused face chains on, `--no-tma` and `--no-pairs` the TMA staging and the
-paired-line sweeps off (ati_set_options).
+paired-line sweeps off, `--dense-zeta` the dense zeta derivatives on (ati_set_options).
 
     python -m tandemproject_gb300.profile [--preset NAME] [--precision fp64|mixed|strict]
-                                          [--steps K] [--warmup W] [--fused] [--no-tma] [--no-pairs] [--json]
+                                          [--steps K] [--warmup W] [--fused] [--no-tma] [--no-pairs] [--dense-zeta]
+                                          [--json]
 """
 import argparse
 import json
@@ -19,7 +20,7 @@ import time
 
 
 def profile_case(preset="naca0012_8p8m", precision="fp64", steps=10, warmup=3, fused=False, tma=True, pairs=True,
-                 timing=None):
+                 timing=None, dense_zeta=False):
     """{class: (microseconds per launch, launches, share)}, tiles, ms per step.  `timing` (a dict) receives the
     graph-timed milliseconds per step and the options in effect."""
     from .config import FP64, FP64_STRICT, MIXED, PRESETS
@@ -27,7 +28,7 @@ def profile_case(preset="naca0012_8p8m", precision="fp64", steps=10, warmup=3, f
     prec = {"fp64": FP64, "mixed": MIXED, "strict": FP64_STRICT}[precision]
     case = setup_case(PRESETS[preset].replace(precision=prec))
     try:
-        opts = case.set_options(tma=tma, fused_faces=fused, paired_lines=pairs)
+        opts = case.set_options(tma=tma, fused_faces=fused, paired_lines=pairs, dense_zeta=dense_zeta)
         case.step(warmup)
         case.synchronize()
         t0 = time.perf_counter()
@@ -57,11 +58,12 @@ def main(argv=None):
     ap.add_argument("--fused", action="store_true")
     ap.add_argument("--no-tma", action="store_true")
     ap.add_argument("--no-pairs", action="store_true")
+    ap.add_argument("--dense-zeta", action="store_true")
     ap.add_argument("--json", action="store_true")
     a = ap.parse_args(argv)
     tm = {}
     rows, tiles, ms_step = profile_case(a.preset, a.precision, a.steps, a.warmup, a.fused, not a.no_tma,
-                                        not a.no_pairs, tm)
+                                        not a.no_pairs, tm, a.dense_zeta)
     if a.json:
         print(json.dumps({"preset": a.preset, "precision": a.precision, "tiles": tiles, "ms_per_step": ms_step,
                           "graph_ms_per_step": tm["graph_ms_per_step"], "options": tm["options"],

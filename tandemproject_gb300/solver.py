@@ -28,6 +28,7 @@ ATI_OK, ATI_EINVAL, ATI_ENOMEM, ATI_ECUDA, ATI_ENONFINITE, ATI_ETIMEDOUT, ATI_ES
 F_QA, F_QO, F_DE, F_RR, F_SS, F_XIM, F_ETM, F_ZEM, F_P, F_YACO, F_STRESS, F_SPONGE, F_CP = range(13)
 FACE_DRVA, FACE_DRVB, FACE_RECV, FACE_CM = range(4)
 OPT_TMA, OPT_FUSED_FACES, OPT_TMA_ETA, OPT_TMA_ZETA, OPT_PAIRED_LINES, OPT_STRESS_AT_POINT = 1, 2, 4, 8, 16, 32
+OPT_DENSE_ZETA = 64
 TILE_PLAN = 11  # ATI_TILE_PLAN
 NCOMP = {F_QA: 5, F_QO: 5, F_DE: 5, F_RR: 3, F_SS: 3, F_XIM: 3, F_ETM: 3, F_ZEM: 3, F_P: 1, F_YACO: 1,
          F_STRESS: 9, F_SPONGE: 2, F_CP: 1}
@@ -302,18 +303,20 @@ class Case:
         t = (ctypes.c_int32 * TILE_PLAN)(*plan)
         self._chk(self.L.ati_set_tile_plan(self.h, t))
 
-    def set_options(self, tma=True, fused_faces=False, paired_lines=True, stress_at_point=True):
-        """Kernel options (results do not depend on them; the library's defaults): TMA staging of the mixed path's
-        segmented eta/zeta sweeps, fused face chains, paired-line segmented derivative sweeps, the FP64 path's
-        viscous fluxes with the stresses at the point.  Returns the options in effect as a dict."""
+    def set_options(self, tma=True, fused_faces=False, paired_lines=True, stress_at_point=True, dense_zeta=False):
+        """Kernel options (the library's defaults; results do not depend on them, except dense_zeta's by FP32
+        rounding): TMA staging of the mixed path's segmented eta/zeta sweeps, fused face chains, paired-line
+        segmented derivative sweeps, the FP64 path's viscous fluxes with the stresses at the point, the mixed path's
+        zeta derivatives as dense products.  Returns the options in effect as a dict."""
         a = ctypes.c_int32()
         flags = ((OPT_TMA if tma else 0) | (OPT_FUSED_FACES if fused_faces else 0)
-                 | (OPT_PAIRED_LINES if paired_lines else 0) | (OPT_STRESS_AT_POINT if stress_at_point else 0))
+                 | (OPT_PAIRED_LINES if paired_lines else 0) | (OPT_STRESS_AT_POINT if stress_at_point else 0)
+                 | (OPT_DENSE_ZETA if dense_zeta else 0))
         self._chk(self.L.ati_set_options(self.h, flags, ctypes.byref(a)))
         v = a.value
         return {"tma_eta": bool(v & OPT_TMA_ETA), "tma_zeta": bool(v & OPT_TMA_ZETA),
                 "fused_faces": bool(v & OPT_FUSED_FACES), "paired_lines": bool(v & OPT_PAIRED_LINES),
-                "stress_at_point": bool(v & OPT_STRESS_AT_POINT)}
+                "stress_at_point": bool(v & OPT_STRESS_AT_POINT), "dense_zeta": bool(v & OPT_DENSE_ZETA)}
 
     def set_spin_limit(self, polls):
         """Polls a device-side barrier wait may take before it gives up (0: the default)."""
