@@ -1575,8 +1575,9 @@ __global__ void __launch_bounds__(SEG_LINES *SEG_MAX) k_sweep_pair(SweepArgs<flo
 // constant being zero: a spanwise-uniform line keeps an exactly zero derivative, and the differences of a nearly
 // uniform one are exact), then forms four rows at a time, the matrix rows read from shared memory four entries a
 // load and broadcast to the warp: LM / 4 loads and LM / 2 packed FMAs (fma.rn.f32x2) a row and line, with no serial
-// chain across rows.  Lines of up to 32 points load the next field's line before the products of this one.  Lines
-// shorter than LM read zeros past their end.
+// chain across rows.  Lines of up to 32 points load the next field's line before the products of this one.  The
+// kernel comes in widths LM of 16, 24, 32, 48 and 64 points, the narrowest that holds the longest line taken;
+// shorter lines read zeros past their end.
 // ---------------------------------------------------------------------------
 template <int LM>
 __global__ void __launch_bounds__(256) k_sweep_dense(SweepArgs<float, float, float> a, const float *dzm) {
@@ -1623,9 +1624,8 @@ __global__ void __launch_bounds__(256) k_sweep_dense(SweepArgs<float, float, flo
     for (int j = 0; j < LM; j++) g[j] = j < L ? g[j] - f0 : 0.f;
 #pragma unroll
     for (int k = 0; k < LM / 2; k++) gp[k] = make_float2(g[2 * k], g[2 * k + 1]);
-    float *out = a.io.out + f * a.io.out_fs + B.off + t;
-    const int m = a.io.m0 + f;
-    for (int i = 0; i < L; i += 4) {
+    float *out = a.io.out + f * a.io.out_fs + B.off + t, *o = out;
+    for (int i = 0; i < L; i += 4, o += 4 * plane) {
       const float4 *row = reinterpret_cast<const float4 *>(dmat + i * LM);
       // four partial sums a row: columns 4k, 4k+1 (ea) and 4k+2, 4k+3 (eb), each pair one packed FMA
       float2 ea[4], eb[4];
@@ -1643,15 +1643,21 @@ __global__ void __launch_bounds__(256) k_sweep_dense(SweepArgs<float, float, flo
       float acc[4];
 #pragma unroll
       for (int u = 0; u < 4; u++) acc[u] = (ea[u].x + ea[u].y) + (eb[u].x + eb[u].y);
+      if (i + 4 <= L) {
+        o[0] = acc[0];
+        o[plane] = acc[1];
+        o[2 * plane] = acc[2];
+        o[3 * plane] = acc[3];
+      } else {
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const int r = i + u;
-        if (r < L) {
-          out[(int64_t)r * plane] = acc[u];
-          if (drv && r == 0) drv[t + nbs * ((m - 1) + 5 * 0)] = acc[u];      // drva(jk,m,0) = sb(is)
-          if (drv && r == L - 1) drv[t + nbs * ((m - 1) + 5 * 1)] = acc[u];  // drva(jk,m,1) = sb(ie)
-        }
+        for (int u = 0; u < 3; u++)
+          if (i + u < L) o[u * plane] = acc[u];
       }
+    }
+    if (drv) {  // the line ends, read back from this thread's own stores
+      const int m = a.io.m0 + f;
+      drv[t + nbs * ((m - 1) + 5 * 0)] = out[0];                         // drva(jk,m,0) = sb(is)
+      drv[t + nbs * ((m - 1) + 5 * 1)] = out[(int64_t)(L - 1) * plane];  // drva(jk,m,1) = sb(ie)
     }
   }
 }
@@ -3014,8 +3020,13 @@ static void sweep_t(const Eng<TC> &e, cudaStream_t st, int nn, bool filt, const 
     if constexpr (std::is_same<TI, float>::value && std::is_same<TO, float>::value) {
       // the zeta derivative by the blocks' dense operators (every zeta line periodic onto its block; k_sweep_dense)
       if (nn == 3 && !filt && e.dense && e.dzl > 0 && !io.out2) {
-        if (e.dzl <= 32) k_sweep_dense<32><<<e.nlt[3], e.sg_lines[3], 32 * 32 * sizeof(float), st>>>(a, e.dzm);
-        else k_sweep_dense<64><<<e.nlt[3], e.sg_lines[3], 64 * 64 * sizeof(float), st>>>(a, e.dzm);
+        const int lm = e.dzl <= 16 ? 16 : e.dzl <= 24 ? 24 : e.dzl <= 32 ? 32 : e.dzl <= 48 ? 48 : 64;
+        const size_t smem = sizeof(float) * lm * lm;
+        if (lm == 16) k_sweep_dense<16><<<e.nlt[3], e.sg_lines[3], smem, st>>>(a, e.dzm);
+        else if (lm == 24) k_sweep_dense<24><<<e.nlt[3], e.sg_lines[3], smem, st>>>(a, e.dzm);
+        else if (lm == 32) k_sweep_dense<32><<<e.nlt[3], e.sg_lines[3], smem, st>>>(a, e.dzm);
+        else if (lm == 48) k_sweep_dense<48><<<e.nlt[3], e.sg_lines[3], smem, st>>>(a, e.dzm);
+        else k_sweep_dense<64><<<e.nlt[3], e.sg_lines[3], smem, st>>>(a, e.dzm);
         return;
       }
     }

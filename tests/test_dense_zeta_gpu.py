@@ -7,8 +7,9 @@ end rows, interior stencil, LU solve; src/Subroutines3D.f90:84-141) and the
 kernel forms the product in FP32.  Its rounding differs from the recurrence's,
 so the checks are against the FP64 path: after a few steps the dense run's
 error per conserved variable stays within a small factor of the recurrence's.
-Lines of 13 to 32 points take the 32-wide kernel, 33 to 64 the 64-wide one;
-longer lines and the FP64 path leave the option off.
+The kernel comes in widths of 16, 24, 32, 48 and 64 points (the cases take
+the 16-, 24-, 32-, 48- and 64-wide ones); longer lines and the FP64 path leave
+the option off.
 """
 import numpy as np
 import pytest
@@ -25,7 +26,7 @@ def _err(run, ref, nblocks):
     return np.sqrt(num / den)
 
 
-@pytest.mark.parametrize("lze", [12, 31, 47, 63])
+@pytest.mark.parametrize("lze", [12, 23, 31, 47, 63])
 def test_dense_zeta_against_fp64(ati_lib, lze):
     from tandemproject_gb300.config import FP64, MIXED, small_case
     from tandemproject_gb300.grid import aerofoil_grid
