@@ -354,6 +354,14 @@ int ati_set_tile_plan(ati_handle_t *h, const int32_t plan[ATI_TILE_PLAN]);
 #define ATI_OPT_STRESS_AT_POINT 32
 #define ATI_OPT_DENSE_ZETA 64
 int ati_set_options(ati_handle_t *h, int flags, int32_t *active);
+/* The dense zeta operator ATI_OPT_DENSE_ZETA applies (no counterpart in the
+ * reference; host only, needs no device): M (*L x *L, row-major, FP64, room
+ * for 64 x 64 doubles) with d = M f the zeta derivative of a zeta line f of
+ * block blk, src/Subroutines3D.f90:84-141 with the periodic closure of
+ * src/Subroutines3D.f90:16-80 (n45 = 0) folded in.  The device takes M
+ * rounded to FP32.  ATI_EINVAL where the case's zeta lines do not qualify
+ * (see ATI_OPT_DENSE_ZETA). */
+int ati_dense_zeta_operator(const ati_config_t *cfg, int blk, double *M, int32_t *L);
 /* Device-side waits are bounded (no counterpart in the reference): a grid
  * barrier of the fused face chains gives up after this many polls (0 = the
  * default, 2^24, seconds), marks every case of the handle, and the next

@@ -21,6 +21,7 @@
 #include <string>
 #include <thread>
 #include <type_traits>
+#include <memory>
 #include <vector>
 
 #include "../../include/ati.h"
@@ -814,10 +815,11 @@ static void seg_tables(const ati_handle *h, const std::vector<double> &fac, std:
 // closure values of the line ends are sums over the other end of the same line (k_mpigo's closure, taken inside the
 // sweep), the end rows those of deriv's closures (line_ends), the interior rows the compact right-hand side, then
 // the LU solve (src/Subroutines3D.f90:84-141).  Column j of M is that algorithm applied in FP64 to the unit line
-// e_j; M is stored rounded to FP32, row-major in DENSE_MAX x DENSE_MAX storage per block.  Returns the largest
+// e_j; M is returned in FP64 (rounded to FP32 for the device), row-major in DENSE_MAX x DENSE_MAX storage per
+// block.  Returns the largest
 // line length, or 0 if some block's zeta lines do not qualify (a face of another kind, lines outside
 // LMD + 2..DENSE_MAX).
-static int dense_zeta(const ati_handle *h, const std::vector<double> &fac, std::vector<float> &out) {
+static int dense_zeta(const ati_handle *h, const std::vector<double> &fac, std::vector<double> &out) {
   const Scheme &S = h->sh.s;
   int lmax = 0;
   for (int gb = 0; gb < h->nb; gb++) {
@@ -828,7 +830,7 @@ static int dense_zeta(const ati_handle *h, const std::vector<double> &fac, std::
     if (L < LMD + 2 || L > DENSE_MAX) return 0;  // the closure sums reach LMD + 1 points in from the far end
     lmax = std::max(lmax, L);
   }
-  out.assign((size_t)h->nb * DENSE_MAX * DENSE_MAX, 0.f);
+  out.assign((size_t)h->nb * DENSE_MAX * DENSE_MAX, 0.0);
   std::vector<double> f(DENSE_MAX), r(DENSE_MAX), v(DENSE_MAX), b(DENSE_MAX + 2);
   for (int gb = 0; gb < h->nb; gb++) {
     const BlockDev &B = h->blk[gb];
@@ -869,7 +871,7 @@ static int dense_zeta(const ati_handle *h, const std::vector<double> &fac, std::
       for (int i = L - 1; i >= 0; i--)
         b[i] = fc[i * 5 + 2] * v[i] - (i <= L - 2 ? fc[i * 5 + 3] * b[i + 1] : 0.0) -
                (i <= L - 3 ? fc[i * 5 + 4] * b[i + 2] : 0.0);
-      for (int i = 0; i < L; i++) out[((size_t)gb * DENSE_MAX + i) * DENSE_MAX + j] = (float)b[i];
+      for (int i = 0; i < L; i++) out[((size_t)gb * DENSE_MAX + i) * DENSE_MAX + j] = b[i];
     }
   }
   return lmax;
@@ -1126,7 +1128,9 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
   if (h->mixed) {
     seg_tables(h, facd, segd32);
     seg_tables(h, facf, segf32);
-    h->ef.dzl = dense_zeta(h, facd, dzm32);
+    std::vector<double> dzm;
+    h->ef.dzl = dense_zeta(h, facd, dzm);
+    dzm32.assign(dzm.begin(), dzm.end());
   }
   e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaStreamCreateWithFlags(&h->side[q], cudaStreamNonBlocking);
@@ -1187,6 +1191,39 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
 }
 
 extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) { return create_impl(cfg, 1, out); }
+
+// The dense zeta operator of one block, built on the host as ati_init builds it for ATI_OPT_DENSE_ZETA (scheme,
+// topology and LU factors of the case, then dense_zeta), in FP64 and without a device.
+extern "C" int ati_dense_zeta_operator(const ati_config_t *cfg, int blk, double *M, int32_t *L) {
+  if (!cfg || !M || !L) return fail(nullptr, ATI_EINVAL, "ati_dense_zeta_operator: null argument");
+  if (cfg->bkx != 3 || cfg->bky != 2 || cfg->bkz != 1)
+    return fail(nullptr, ATI_EINVAL, "the aerofoil H-grid topology has bkx=3, bky=2, bkz=1 blocks");
+  if (blk < 0 || blk >= 6) return fail(nullptr, ATI_EINVAL, "ati_dense_zeta_operator: block index out of range");
+  std::unique_ptr<ati_handle> h(new ati_handle());
+  h->ncase = 1;
+  h->cfgs.assign(cfg, cfg + 1);
+  h->cfg = *cfg;
+  h->mixed = cfg->precision == ATI_MIXED;
+  h->nb = 6;
+  h->blk.resize(h->nb);
+  h->grid_set.assign(h->nb, 0);
+  h->shc.resize(1);
+  build_scheme(*cfg, h->shc[0]);
+  h->sh = h->shc[0];
+  std::vector<double> facd, facf, spg, ops;
+  if (int rc = build_tables(h.get(), facd, facf, spg)) {
+    g_create_err = h->err;
+    return rc;
+  }
+  if (!dense_zeta(h.get(), facd, ops))
+    return fail(nullptr, ATI_EINVAL, "the zeta lines do not qualify: every zeta face periodic onto its own block "
+                                     "and lines of LMD + 2 to DENSE_MAX points");
+  const int n = h->blk[blk].lze + 1;
+  *L = n;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) M[(size_t)i * n + j] = ops[((size_t)blk * DENSE_MAX + i) * DENSE_MAX + j];
+  return ATI_OK;
+}
 
 extern "C" int ati_create_batch(const ati_config_t *cfgs, int ncase, ati_handle_t **out) {
   return create_impl(cfgs, ncase, out);

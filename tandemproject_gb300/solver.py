@@ -87,6 +87,7 @@ SIGNATURES = {
     "ati_set_spin_limit": ([_vp, ctypes.c_int64], ctypes.c_int),
     "ati_check_conversions": ([ctypes.c_int64, _vp], ctypes.c_int),
     "ati_check_recip": ([ctypes.c_int64, _dp], ctypes.c_int),
+    "ati_dense_zeta_operator": ([_vp, _i32, _dp, _vp], ctypes.c_int),
     "ati_turbulence_modes": ([_vp, _i32, _vp, _vp], ctypes.c_int),
     "ati_turbulence_sample": ([_vp, _i32, ctypes.c_double, ctypes.c_int64, _dp, _dp], ctypes.c_int),
     "ati_query": ([_vp, _vp], ctypes.c_int),
@@ -482,6 +483,18 @@ def probe_fma_tflops(fp64=True):
     if rc:
         raise AtiError(rc, "ati_probe_fma_tflops failed")
     return v.value
+
+
+def dense_zeta_operator(cfg: CaseConfig, blk):
+    """The L x L FP64 operator of block blk's zeta derivative that the dense zeta option applies (host only)."""
+    L = load_library()
+    c = cfg.to_c()
+    m = np.zeros(64 * 64)
+    n = ctypes.c_int32()
+    rc = L.ati_dense_zeta_operator(ctypes.byref(c), blk, m.ctypes.data_as(_dp), ctypes.byref(n))
+    if rc:
+        raise AtiError(rc, L.ati_last_error(None).decode())
+    return m[:n.value * n.value].reshape(n.value, n.value).copy()
 
 
 def setup_case(cfg: CaseConfig, grid=None, cls=Case):
