@@ -816,9 +816,8 @@ static void seg_tables(const ati_handle *h, const std::vector<double> &fac, std:
 // sweep), the end rows those of deriv's closures (line_ends), the interior rows the compact right-hand side, then
 // the LU solve (src/Subroutines3D.f90:84-141).  Column j of M is that algorithm applied in FP64 to the unit line
 // e_j; M is returned in FP64 (rounded to FP32 for the device), row-major in DENSE_MAX x DENSE_MAX storage per
-// block.  Returns the largest
-// line length, or 0 if some block's zeta lines do not qualify (a face of another kind, lines outside
-// LMD + 2..DENSE_MAX).
+// block.  Returns the largest line length, or 0 if some block's zeta lines do not qualify (a face of another kind,
+// lines outside LMD + 2..DENSE_MAX).
 static int dense_zeta(const ati_handle *h, const std::vector<double> &fac, std::vector<double> &out) {
   const Scheme &S = h->sh.s;
   int lmax = 0;
@@ -1192,7 +1191,7 @@ static int create_impl(const ati_config_t *cfgs, int ncase, ati_handle_t **out) 
 
 extern "C" int ati_create(const ati_config_t *cfg, ati_handle_t **out) { return create_impl(cfg, 1, out); }
 
-// The dense zeta operator of one block, built on the host as ati_init builds it for ATI_OPT_DENSE_ZETA (scheme,
+// The dense zeta operator of one block, built on the host as ati_create builds it for ATI_OPT_DENSE_ZETA (scheme,
 // topology and LU factors of the case, then dense_zeta), in FP64 and without a device.
 extern "C" int ati_dense_zeta_operator(const ati_config_t *cfg, int blk, double *M, int32_t *L) {
   if (!cfg || !M || !L) return fail(nullptr, ATI_EINVAL, "ati_dense_zeta_operator: null argument");
