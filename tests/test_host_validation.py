@@ -1,8 +1,12 @@
-"""ati_create / ati_create_batch reject a bad configuration before they look
-for a device, with ATI_EINVAL and a message naming the field (host logic,
-no GPU needed): the aerofoil H-grid topology, the RK stage count, the
-precision, a batch whose cases differ in their numerics, and a batch of
-more blocks than a handle holds."""
+"""Argument checks that run on the host before any device work (no GPU
+needed), each returning ATI_EINVAL with a message naming what is wrong:
+- ati_create / ati_create_batch: the aerofoil H-grid topology, the RK stage
+  count, the precision, a batch whose cases differ in their numerics, a batch
+  of more blocks than a handle holds;
+- ati_deriv_lines_noalloc: null arrays, a negative line count, lines shorter
+  than the 7-point closures or longer than ATI_NOALLOC_MAX_LEN, more points
+  than ATI_NOALLOC_MAX_POINTS; an empty call returns ATI_OK untouched.
+No call here reaches a pointer: every case is refused (or empty) first."""
 import ctypes
 
 import pytest
@@ -67,3 +71,21 @@ def test_empty_batch_rejected(lib):
     h = ctypes.c_void_p()
     rc = lib.ati_create_batch((AtiConfig * 1)(), 0, ctypes.byref(h))
     assert rc == ATI_EINVAL and not h.value
+
+
+@pytest.mark.parametrize("args,words", [
+    ((None, 16, 1, 10), b"null pointer"),
+    ((16, None, 1, 10), b"null pointer"),
+    ((16, 16, -1, 10), b"negative line count"),
+    ((16, 16, 1, 6), b"line length"),
+    ((16, 16, 1, 4097), b"ATI_NOALLOC_MAX_LEN"),
+    ((16, 16, 200_001, 10), b"ATI_NOALLOC_MAX_POINTS"),
+])
+def test_noalloc_arguments_rejected(lib, args, words):
+    src, dst, nlines, n = args
+    rc = lib.ati_deriv_lines_noalloc(ctypes.c_void_p(src), ctypes.c_void_p(dst), nlines, n, None)
+    assert rc == ATI_EINVAL and words in lib.ati_last_error(None)
+
+
+def test_noalloc_empty_call(lib):
+    assert lib.ati_deriv_lines_noalloc(ctypes.c_void_p(16), ctypes.c_void_p(16), 0, 10, None) == 0
