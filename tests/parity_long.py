@@ -4,8 +4,8 @@ relative L2 per conserved variable every `--every` steps.
 
     python tests/parity_long.py --preset naca0012_8p8m --steps 1000 --every 100
 
-The 8.85 M-point preset is config 2 of the plain FP64 method (seeded von
-Karman inflow turbulence); with --precision strict the GPU sums the
+The 8.85 M-point preset is the plain FP64 method's case with seeded von
+Karman inflow turbulence; with --precision strict the GPU sums the
 turbulence modes in FP64 in the oracle's order.  The oracle takes about 1.5 s
 a step on 16 host cores.
 """

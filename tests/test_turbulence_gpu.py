@@ -169,8 +169,8 @@ def test_turbulent_inflow_matches_oracle_small(ati_lib, oracle_lib):
     o2.close()
 
 
-def test_config2_inflow_turbulence_matches_oracle(ati_lib, oracle_lib):
-    """Config 2: the 8.85 M-point NACA 0012 case (6 blocks 384 x 120 x 32) with
+def test_8p8m_inflow_turbulence_matches_oracle(ati_lib, oracle_lib):
+    """The 8.85 M-point NACA 0012 case (6 blocks 384 x 120 x 32) with
     seeded von Karman inflow turbulence (2.5 % of U_inf, L = 0.1 c, 2048 modes,
     seed 1234), compared field by field with the CPU restatement after 25
     steps (gust targets evaluated at steps 0, 1, 11 and 21): the reference
@@ -187,14 +187,14 @@ def test_config2_inflow_turbulence_matches_oracle(ati_lib, oracle_lib):
     gpu.step(25)
     assert orc.step(25) == 0
     e = _state_errors(gpu, orc)
-    print("config 2, strict vs oracle after 25 steps", e)
+    print("8.85 M points with inflow turbulence, strict vs oracle after 25 steps", e)
     assert np.all(e < 1e-10), e
     gpu.close()
     from tandemproject_gb300.solver import setup_case
     fast = setup_case(cfg.replace(precision=FP64))
     fast.step(25)
     e2 = _state_errors(fast, orc)
-    print("config 2, FP64 (FP32 mode sum) vs oracle after 25 steps", e2)
+    print("8.85 M points with inflow turbulence, FP64 (FP32 mode sum) vs oracle after 25 steps", e2)
     assert np.all(e2 < 1e-6), e2
     fast.close()
     orc.close()
