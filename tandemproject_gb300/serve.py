@@ -12,7 +12,9 @@ alone: cases share nothing on the device.  A request whose state turns
 non-finite (ATI_ENONFINITE after one of its chunks: the compact scheme has no
 shock capturing, and the upper corner of the parameter ranges can diverge) is
 retired as failed, with the steps it had run, and its memory goes to the
-others; the latency percentiles are those of the completed requests.
+others; so is a request whose set-up the library refuses (an error status
+from ati_create or ati_init, such as device memory taken by other processes).
+The latency percentiles are those of the completed requests.
 """
 import argparse
 import concurrent.futures as cf
@@ -21,6 +23,7 @@ import time
 
 import numpy as np
 
+from .solver import AtiError
 from .workloads import fold_free_case, footprint_bytes, relax, serving_requests, valid_grid
 
 ATI_ENONFINITE = 4
@@ -43,6 +46,11 @@ def _gpu_case(cfg, grid, plan=None):
     if plan is not None:
         c.set_tile_plan(plan)
     return c
+
+
+def _params(cfg):
+    """The drawn parameters of a request, for the record of a failed one."""
+    return {k: getattr(cfg, k) for k in ("mach", "aoa_deg", "thick", "turb_intensity")}
 
 
 def plan_key(cfg):
@@ -120,8 +128,18 @@ class Server:
                         f"{used / 2**30:.1f} GiB in use")
             for s in list(starting):
                 if s["job"].done():
-                    cfg, c = s["job"].result()
                     starting.remove(s)
+                    try:
+                        cfg, c = s["job"].result()
+                    except AtiError as err:  # the library refused the case (device memory, configuration)
+                        r = s["req"]
+                        used -= s["fp"]
+                        failed.append({"id": r.rid, "points": r.cfg.npoints, "steps": r.steps, "steps_run": 0,
+                                       "arrival": r.arrival, "failed_at": now(), "error": str(err),
+                                       "params": _params(r.cfg)})
+                        if log:
+                            log(f"t={now():7.2f}s FAILED #{r.rid} at set-up: {err}")
+                        continue
                     active.append({"req": s["req"], "case": c, "left": s["req"].steps, "fp": s["fp"],
                                    "admitted": s["admitted"], "started": now(), "npts": cfg.npoints,
                                    "issued": 0, "checked": 0})
@@ -137,7 +155,7 @@ class Server:
                         r = a["req"]
                         rec = {"id": r.rid, "points": a["npts"], "steps": r.steps, "steps_run": a["issued"],
                                "arrival": r.arrival, "failed_at": now(), "error": str(err),
-                               "params": {k: getattr(r.cfg, k) for k in ("mach", "aoa_deg", "thick", "turb_intensity")}}
+                               "params": _params(r.cfg)}
                         a["case"].close()
                         used -= a["fp"]
                         active.remove(a)

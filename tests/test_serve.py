@@ -144,3 +144,29 @@ def test_scheduler_reuses_tile_plans_per_block_shape():
     # the first case of each shape times its tiles; the later ones get its plan
     assert PlannedCase.made == [((24, 64, 24), None), ((32, 64, 32), None), ((24, 64, 24), ("plan", (24, 64, 24))),
                                 ((24, 64, 24), ("plan", (24, 64, 24))), ((32, 64, 32), ("plan", (32, 64, 32)))]
+
+
+class RefusedCase(FakeCase):
+    """A stand-in the library refuses at set-up for the cases of Mach 0.35 (as ati_create does when device memory
+    is short)."""
+
+    def __init__(self, cfg, grid):
+        from tandemproject_gb300.solver import AtiError
+        if cfg.mach == 0.35:
+            raise AtiError(3, "cudaMalloc of the case's arena failed: out of memory")
+        super().__init__(cfg, grid)
+
+
+def test_scheduler_retires_a_request_refused_at_set_up_and_serves_the_rest():
+    from tandemproject_gb300.config import small_case
+    from tandemproject_gb300.serve import Server
+    reqs = [Request(i, small_case(mach=0.35 if i == 3 else 0.24), 20 + i, 0.001 * i, {}) for i in range(6)]
+    srv = Server(budget_bytes=10, chunk=7, make_case=RefusedCase, make_grid=lambda cfg: (cfg, None),
+                 footprint=lambda cfg: 10)  # one case at a time
+    FakeCase.live = FakeCase.peak = 0
+    done, summary = srv.run(reqs)
+    assert sorted(d["id"] for d in done) == [0, 1, 2, 4, 5]
+    assert summary["failed"] == 1 and summary["failed_requests"][0]["id"] == 3
+    assert summary["failed_requests"][0]["steps_run"] == 0
+    # the refused case's memory went back to the budget: held, the next admission would have gone past it
+    assert FakeCase.live == 0 and srv.peak_bytes <= 10
