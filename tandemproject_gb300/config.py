@@ -4,6 +4,7 @@ read at src/SingleTurbulence3D.f90:39-62), mirrored as the C struct
 ``ati_config_t`` of include/ati.h.
 
 Presets name the workloads by what they are:
+  naca0012_0p2m  NACA 0012, 6 blocks (49/121/49)x40x13 = 0.23 M points, FP64 (quick checks)
   naca0012_0p6m  NACA 0012, 6 blocks (91/201/91)x40x20 = 0.61 M points, FP64
   naca0012_3p5m  NACA 0012, 6 blocks 256x96x24 = 3.54 M points, FP64 (profiler captures)
   naca0012_8p8m  NACA 0012, 6 blocks 384x120x32 = 8.85 M points, FP64

@@ -1,6 +1,7 @@
 """Host-side helpers of the batched and serving workloads
 (tandemproject_gb300.workloads) on the CPU: the sizing rule, the grid
-relaxation used when a grid folds, and the fold-free grid search."""
+relaxation used when a grid folds, and the fold-free grid search; and the
+named presets' sizes."""
 import numpy as np
 import pytest
 
@@ -36,3 +37,12 @@ def test_valid_grid_is_fold_free():
     j = min_cell_jacobian(g)
     assert len(g) == cfg.nblocks
     assert all(a < 0 and b < 0 for a, b in j) or all(a > 0 and b > 0 for a, b in j), j
+
+
+@pytest.mark.parametrize("name,points,precision", [
+    ("naca0012_0p2m", 227_760, 0), ("naca0012_0p6m", 612_800, 0), ("naca0012_3p5m", 3_538_944, 0),
+    ("naca0012_8p8m", 8_847_360, 0), ("naca0012_25m", 24_576_000, 1)])
+def test_presets_are_the_named_workloads(name, points, precision):
+    from tandemproject_gb300.config import PRESETS
+    cfg = PRESETS[name]
+    assert cfg.npoints == points and cfg.precision == precision and cfg.nblocks == 6
