@@ -44,6 +44,8 @@ def test_dense_zeta_against_fp64(ati_lib, lze):
     e_seg, e_dense = _err(seg, ref, cfg.nblocks), _err(dense, ref, cfg.nblocks)
     assert np.all(e_seg[[0, 4]] < 1e-6), e_seg  # density and energy; the small w momentum has the largest error
     assert np.all(e_dense <= 3.0 * e_seg + 1e-9), (e_dense, e_seg)
+    # the option took effect: the dense products round differently from the recurrence
+    assert any(not np.array_equal(dense.get_state(mb), seg.get_state(mb)) for mb in range(cfg.nblocks))
     for c in (ref, seg, dense):
         c.close()
 
@@ -88,5 +90,6 @@ def test_dense_zeta_in_a_batch(ati_lib):
     nb = sum(c.nblocks for c in cfgs)
     e_seg, e_dense = _err(seg, ref, nb), _err(dense, ref, nb)
     assert np.all(e_dense <= 3.0 * e_seg + 1e-9), (e_dense, e_seg)
+    assert any(not np.array_equal(dense.get_state(b), seg.get_state(b)) for b in range(nb))
     for c in (ref, seg, dense):
         c.close()
