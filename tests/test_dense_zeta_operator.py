@@ -5,7 +5,9 @@ one matrix M a block built on the host from the line algorithm;
 ati_dense_zeta_operator exports that builder in FP64.  Here M is applied to
 every zeta line of a random field and compared with the oracle's periodic
 closure (mpigo with n45 = 0) and derivative along zeta
-(src/Subroutines3D.f90:16-141) of the same field: equal to FP64 rounding.
+(src/Subroutines3D.f90:16-141) of the same field: equal to FP64 rounding;
+and equal to the committed golden operators of periodic lines, which a second,
+independent numpy restatement made.
 The rows of M sum to zero, which the kernel relies on when it takes each
 line's first value out before the product; zeta lines past 64 points have no
 operator.
@@ -70,3 +72,15 @@ def test_operator_of_the_0p6m_preset(ati_lib):
     assert ms[0].shape == (cfg.lzebk[0] + 1,) * 2
     for m in ms[1:]:
         assert np.array_equal(m, ms[0])
+
+
+@pytest.mark.parametrize("L", [13, 20])
+def test_operator_equals_the_golden_periodic_operator(ati_lib, L):
+    """the committed golden operator of a periodic zeta line (tests/golden/make_golden.py: an independent numpy
+    restatement, closure rows on unit vectors and numpy.linalg.solve for the left-hand side)"""
+    import os
+    from tandemproject_gb300.config import small_case
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "line_operators.npz"))[f"deriv_p{L}"]
+    M = dense_zeta_operator(small_case(lzebk=(L - 1,)), 0)
+    assert M.shape == gold.shape
+    assert np.max(np.abs(M - gold)) <= 1e-13 * np.max(np.abs(gold))  # measured 3.2e-15 (13 points), 4.1e-15 (20)
